@@ -1,0 +1,175 @@
+/*
+ * g4hepem_gb300.h -- C-ABI of the GB300-native G4HepEmRun stepping-physics path.
+ *
+ * The reference exposes this path as C++ static functions over one track at a
+ * time (G4HepEmElectronManager / G4HepEmGammaManager, tables in G4HepEmData,
+ * loaded by G4HepEmDataJsonIO, uniforms from a consumer-supplied
+ * G4HepEmRandomEngine::flat()).  This header replaces that surface by batch
+ * entry points over structure-of-arrays (SoA) track batches in GPU memory.
+ * Plain C: pointers, sizes, integer status codes; no CUDA or torch types.
+ *
+ * Conventions
+ *  - Every function returns an int status (HEPEM_OK == 0); none calls exit().
+ *  - A context owns the tables (device arena) and is immutable after
+ *    hepem_create(); it may be shared by host threads.  Launches go to the
+ *    stream passed by the caller (a cudaStream_t passed as void*, NULL = the
+ *    legacy default stream).  The caller owns every track buffer.
+ *  - Device-pointer entry points return once the work is enqueued; the
+ *    *_host variants copy host buffers in and out and return when done.
+ *  - Particle type codes: 0 = e-, 1 = e+, 2 = gamma.
+ *
+ * Per-track uniform random streams (replaces G4HepEmRandomEngine::flat/flatArray,
+ * reference G4HepEm/G4HepEmRun/include/G4HepEmRandomEngine.hh:40-51 and
+ * G4HepEm/G4HepEmRun/src/G4HepEmRandomEngine.cc:5-11):
+ *   uniform k of track i is  uniforms[i*n_uniform + k]          for k <  n_uniform
+ *                            hepem_philox_uniform(seed, id[i], k) for k >= n_uniform
+ *   starting at k = rng_cursor[i]; the cursor is advanced by the number of
+ *   uniforms the step consumed.  Tracks that read past n_uniform get bit 0 of
+ *   flags set and are counted in hepem_step_counters.rng_overflow; the stream
+ *   continues deterministically instead of wrapping.  Filling the buffer with
+ *   hepem_philox_uniform() makes the stream seamless.
+ */
+#ifndef G4HEPEM_GB300_H
+#define G4HEPEM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  HEPEM_OK            = 0,
+  HEPEM_BAD_ARG       = 1,  /* null pointer, negative size, bad index range  */
+  HEPEM_PARSE_ERROR   = 2,  /* state JSON does not follow the schema          */
+  HEPEM_CUDA_ERROR    = 3,  /* a CUDA runtime call failed                     */
+  HEPEM_RNG_EXHAUSTED = 4,  /* informational: some track read past n_uniform  */
+  HEPEM_TIMEOUT       = 5,  /* a bounded wait gave up                          */
+  HEPEM_OOM_ADMISSION = 6,  /* serving: request does not fit the memory budget */
+  HEPEM_NO_DEVICE     = 7   /* no CUDA device visible                         */
+};
+
+typedef struct hepem_ctx hepem_ctx;
+
+/* ---- track batches ----------------------------------------------------- */
+/* Persistent per-track state, SoA, arrays of length n.  Mirrors the fields of
+ * G4HepEmTrack (G4HepEm/G4HepEmRun/include/G4HepEmTrack.hh:246-264),
+ * G4HepEmElectronTrack (.../G4HepEmElectronTrack.hh:20-93), the persistent part
+ * of G4HepEmMSCTrackData (.../G4HepEmMSCTrackData.hh:14-133) and the Gauss
+ * cache of G4HepEmRandomEngine (.../G4HepEmRandomEngine.hh:50-70). */
+typedef struct hepem_track_state {
+  int8_t*  type;           /* 0 e-, 1 e+, 2 gamma                              */
+  int32_t* imc;            /* material-cuts couple index (G4HepEmMCCData)     */
+  int32_t* id;             /* track id: RNG stream id and parent id           */
+  double*  ekin;           /* kinetic energy [MeV]                            */
+  double*  dir_x;          /* unit direction                                  */
+  double*  dir_y;
+  double*  dir_z;
+  double*  nia0;           /* number-of-interaction-left per process; <=0     */
+  double*  nia1;           /*   means "sample a new one" (gamma uses nia0)    */
+  double*  nia2;
+  double*  nia3;
+  double*  safety;         /* isotropic safety [mm] (e+- MSC step limit)      */
+  uint8_t* on_boundary;    /* step starts and ends on a volume boundary       */
+  double*  msc_init_range; /* MSC fInitialRange        (1e21 for a new track) */
+  double*  msc_dyn_factor; /* MSC fDynamicRangeFactor  (0.04)                 */
+  double*  msc_tlimit_min; /* MSC fTlimitMin           (1e-7 mm)              */
+  uint8_t* msc_first_step; /* MSC fIsFirstStep         (1)                    */
+  uint8_t* gauss_valid;    /* cached second Gaussian of the polar method      */
+  double*  gauss_value;
+  int32_t* rng_cursor;     /* next uniform index of this track's stream       */
+} hepem_track_state;
+
+/* Per-step results and secondaries (at most 2 per step, fixed slots 2i, 2i+1). */
+typedef struct hepem_step_out {
+  double*  edep;           /* energy deposit of the step [MeV]                */
+  double*  gstep;          /* geometrical step length [mm]                    */
+  double*  pstep;          /* true (physical) step length [mm]                */
+  int8_t*  winner;         /* e+-: -2 MSC, -1 continuous, 0 ioni, 1 brem,
+                              2 annihilation, 3 nuclear; gamma: 0 conversion,
+                              1 Compton, 2 photoelectric, 3 nuclear           */
+  double*  disp_x;         /* MSC lateral displacement (lab frame) [mm]       */
+  double*  disp_y;
+  double*  disp_z;
+  uint8_t* flags;          /* bit0: read past n_uniform                       */
+  int8_t*  n_sec;          /* number of secondaries of track i (0..2)         */
+  int8_t*  sec_type;       /* [2n] particle type of the secondary             */
+  double*  sec_ekin;       /* [2n]                                            */
+  double*  sec_dir_x;      /* [2n]                                            */
+  double*  sec_dir_y;
+  double*  sec_dir_z;
+} hepem_step_out;
+
+typedef struct hepem_step_counters {
+  uint64_t steps;          /* tracks stepped                                  */
+  uint64_t uniforms;       /* uniforms consumed                               */
+  uint64_t rng_overflow;   /* tracks that read past n_uniform                 */
+  uint64_t secondaries;    /* secondaries produced                            */
+  uint64_t interactions[8];/* e+- winner 0..3, gamma winner 0..3              */
+} hepem_step_counters;
+
+/* ---- context ------------------------------------------------------------ */
+/* Parse a G4HepEmState JSON document (the schema of G4HepEmStateFromJson,
+ * reference G4HepEm/G4HepEmDataJsonIO/include/G4HepEmDataJsonIO.hh:84 and
+ * src/G4HepEmDataJsonIOImpl.hh:125-981) and build the device table arena on
+ * the current CUDA device.  Replaces G4HepEmStateFromJson +
+ * CopyG4HepEmDataToGPU (G4HepEm/G4HepEmData/src/G4HepEmData.cc:78-101). */
+int  hepem_create(const char* state_json, size_t len, hepem_ctx** out);
+int  hepem_create_from_file(const char* path, hepem_ctx** out);
+/* Replaces FreeG4HepEmData / FreeG4HepEmDataOnGPU (G4HepEmData.hh:80-88). */
+int  hepem_destroy(hepem_ctx* ctx);
+/* Table sizes: number of couples, materials, regions; bytes of the arena. */
+int  hepem_info(const hepem_ctx* ctx, int32_t* n_couples, int32_t* n_materials,
+                int32_t* n_regions, int64_t* arena_bytes);
+const char* hepem_status_string(int status);
+/* Last error message of the calling thread (empty if none). */
+const char* hepem_last_error(void);
+
+/* ---- electron table lookups (device pointers) ---------------------------- */
+/* For each track: restricted macroscopic ionisation and brem cross sections,
+ * restricted dE/dx, range, and inverse range at 0.5*range.  Replaces
+ * G4HepEmElectronManager::GetRestMacXSec / GetRestDEDX / GetRestRange /
+ * GetInvRange (G4HepEm/G4HepEmRun/include/G4HepEmElectronManager.hh:230-248,
+ * .icc:486-532).  log(ekin) is computed on the device. */
+int  hepem_electron_lookup(const hepem_ctx* ctx, int64_t n, int is_positron,
+                           const double* ekin, const int32_t* imc,
+                           double* xs_ioni, double* xs_brem, double* dedx,
+                           double* range, double* invrange_half, void* stream);
+
+/* ---- one physics step (device pointers) ---------------------------------- */
+/* e+-: G4HepEmElectronManager::HowFar then ::Perform
+ *      (G4HepEm/G4HepEmRun/include/G4HepEmElectronManager.hh:71,222).
+ * gamma: G4HepEmGammaManager::HowFar, ::SelectInteraction, ::Perform
+ *      (G4HepEm/G4HepEmRun/include/G4HepEmGammaManager.hh:32,39,51),
+ * in the call order of the reference client
+ * (apps/examples/TestEm3/src/G4HepEmProcess.cc:119-200) with the geometrical
+ * step equal to the proposed one.  `out` may alias `in` (in-place stepping).
+ * counters: device pointer or NULL; accumulated with atomics. */
+int  hepem_step(const hepem_ctx* ctx, int64_t n, const hepem_track_state* in,
+                hepem_track_state* out, const double* uniforms, int32_t n_uniform,
+                uint64_t seed, hepem_step_out* res, hepem_step_counters* counters,
+                void* stream);
+
+/* Same with HOST buffers: copies the batch in, steps it, copies the results
+ * back and synchronises.  Pinned host memory is fastest. */
+int  hepem_step_host(const hepem_ctx* ctx, int64_t n, const hepem_track_state* in,
+                     hepem_track_state* out, const double* uniforms,
+                     int32_t n_uniform, uint64_t seed, hepem_step_out* res,
+                     hepem_step_counters* counters, void* stream);
+
+/* ---- RNG stream helpers --------------------------------------------------- */
+/* Philox4x32-10 (Salmon et al., SC'11) uniform in (0,1): counter
+ * (k>>1, id, 0, 0x48455045), key (seed lo, seed hi); 52 random bits. */
+double hepem_philox_uniform(uint64_t seed, int32_t id, int32_t k);
+/* Fill uniforms[i*n_uniform + k] = hepem_philox_uniform(seed, id[i], k) on the
+ * device (ids: device pointer). */
+int  hepem_fill_uniforms(int64_t n, const int32_t* id, int32_t n_uniform,
+                         uint64_t seed, double* uniforms, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* G4HEPEM_GB300_H */
