@@ -1,0 +1,338 @@
+"""Benchmark of the G4HepEmRun stepping-physics path on GB300.
+
+Workload (BASELINE configuration 2): 4,194,304 tracks, 45% gamma / 45% e- /
+10% e+, kinetic energies log-uniform in [1 MeV, 10 GeV], couples uniform over
+G4_PbWO4 / G4_lAr / G4_Pb at 0.7 mm (synthetic G4HepEmState tables), isotropic
+directions, first-step track state, 64 Philox uniforms per track.  One "step"
+= one HowFar + Perform of every track (plain FP64 path, bit-exact with the
+reference CPU functions).  Each timed step reads the same input state and
+writes separate outputs, so every step does identical work; the inputs
+(~2.7 GB) are larger than L2.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+Prints one JSON line (rank 0).  `value` is device-resident throughput
+(steps/s over all ranks); `e2e` is the same metric through the host-buffer
+C-ABI entry point hepem_step_host with the host<->device copies inside the
+timed region.  `--impl reference` times the reference algorithm on the host
+cores: the CPU port of the oracle (the reference build itself cannot exist on
+the GPU host), all host threads, same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+TABLE = os.path.join(REPO, "g4hepem_gb300", "data", "three_couples_0.7mm.json")
+N_TRACKS = 4194304
+NU = 64
+SEED = 20261203
+WORKLOAD_SEED = 7
+METRIC = "mixed e±/γ physics steps/s (1 GB300) vs plain FP64 path; p50/p99 batch latency"
+UNIT = "steps/s"
+CONFIG = {"workload": "plain FP64 full step, 4,194,304 mixed tracks (45% gamma, 45% e-, 10% e+), "
+                      "1 MeV-10 GeV log-uniform, 3 couples (G4_PbWO4, G4_lAr, G4_Pb @0.7 mm), "
+                      "64 Philox uniforms/track",
+          "tracks_per_step": N_TRACKS, "uniforms_per_track": NU, "table": "three_couples_0.7mm.json",
+          "l2": "inputs larger than L2 (2.7 GB per step), no flush"}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    lrank = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, lrank
+
+
+def peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except Exception:
+            self.p.kill()
+            out = ""
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(n, uniforms_consumed, secondaries):
+    """Bytes of the C-ABI contract fields read and written once per step.
+
+    read : full input state, 128 B/track (type 1, imc 4, id 4, ekin 8, dir 24,
+           nia 32, safety 8, boundary 1, MSC 25, Gauss 9, cursor 4) plus the
+           uniforms actually consumed (8 B each);
+    write: persistent state 102 B/track (ekin, dir, nia, MSC, Gauss, cursor),
+           step results 51 B/track (edep, gstep, pstep, winner, disp, flags,
+           n_sec) and 33 B per secondary produced (type, E, dir)."""
+    return n * (128 + 102 + 51) + 8 * uniforms_consumed + 33 * secondaries
+
+
+def fp64_peak_tflops(torch):
+    """Measured FP64 peak of this GPU: cuBLAS DGEMM 4096^3, best of 5."""
+    a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        a @ b
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        a @ b
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    return 2 * 4096 ** 3 / best / 1e12
+
+
+def profile_summary(name):
+    p = os.path.join(REPO, "profiles", name)
+    try:
+        return json.load(open(p))
+    except Exception:
+        return None
+
+
+def cpu_port_rate(state, threads, n_sample, reps=1):
+    from oracle import oracle as O
+    O.build_port()
+    port = O.PortLib().load(TABLE)
+    sub = {k: np.ascontiguousarray(v[:n_sample]) for k, v in state.items()}
+    u = port.fill_uniforms(sub["id"], NU, SEED)
+    port.step_mt(sub, u, NU, SEED, threads)  # warm
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        port.step_mt(sub, u, NU, SEED, threads)
+    dt = time.perf_counter() - t0
+    port.close()
+    return n_sample * reps / dt, dt
+
+
+def run_reference(args, ws, rank):
+    """CPU reference arm: the oracle port on all host threads (rank 0 only)."""
+    if rank != 0:
+        return
+    from g4hepem_gb300 import workload as W
+    threads = os.cpu_count() or 1
+    st = W.mixed_batch(N_TRACKS, seed=WORKLOAD_SEED)
+    n_sample = N_TRACKS
+    rates = []
+    for i in range(args.warmup + args.steps):
+        r, _ = cpu_port_rate(st, threads, n_sample)
+        if i >= args.warmup:
+            rates.append(r)
+    tot_time = sum(n_sample / r for r in rates)
+    value = n_sample * len(rates) / tot_time
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_time / len(rates),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": CONFIG,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{n_sample} tracks of the workload per step, {threads} host threads; "
+                                       "the CPU port is bit-exact with the reference build (tests/golden)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--n", type=int, default=N_TRACKS)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    ws, rank, lrank = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+
+    import torch
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(lrank)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    from g4hepem_gb300 import build as B
+    B.build()
+    from g4hepem_gb300 import native as N
+    from g4hepem_gb300 import workload as W
+
+    n = args.n
+    ctx = N.Context(TABLE)
+    st_np = W.mixed_batch(n, seed=WORKLOAD_SEED, id0=rank * n)
+    sin = N.state_to_torch(st_np)
+    sout = N.empty_state_torch(n)
+    res = N.alloc_out_torch(n)
+    u = N.fill_uniforms(sin["id"], NU, SEED)
+    cnt = torch.zeros(12, dtype=torch.int64, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    # warm-up (and one counted step for the algorithmic byte count)
+    for i in range(max(args.warmup, 3)):
+        ctx.step(sin, sout, u, NU, SEED, res, counters=cnt if i == 0 else None)
+    torch.cuda.synchronize()
+    c = cnt.cpu().numpy()
+    uniforms_consumed, secondaries = int(c[1]), int(c[3])
+
+    clocks = Clocks(lrank)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        ctx.step(sin, sout, u, NU, SEED, res)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier()
+    t_ms = ev0.elapsed_time(ev1)
+    t_max = t_ms
+    if ws > 1:
+        tt = torch.tensor([t_ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(tt.item())
+    ms_step = t_max / args.steps
+    value = ws * n * args.steps / (t_max / 1e3)
+
+    # e2e through the host-buffer entry point
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()  # noqa: E731
+        h_in = {k: pin(v) for k, v in st_np.items()}
+        h_u = u.cpu().pin_memory()
+        h_out = {k: torch.empty_like(v).pin_memory() for k, v in h_in.items()}
+        h_res = {k: torch.from_numpy(v).pin_memory() for k, v in N.alloc_out_numpy(n).items()}
+        ctx_steps = max(3, min(args.steps, 10))
+        N.lib()
+        import ctypes as C
+        sin_h, sout_h, sres_h = N.make_state_struct(h_in), N.make_state_struct(h_out), N.make_out_struct(h_res)
+        hcnt = N.StepCounters()
+
+        def host_step():
+            N.check(N.lib().hepem_step_host(ctx.h, n, C.byref(sin_h), C.byref(sout_h), h_u.data_ptr(), NU, SEED,
+                                            C.byref(sres_h), C.byref(hcnt), stream.cuda_stream))
+        host_step()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(ctx_steps):
+            host_step()
+        t_e2e = time.perf_counter() - t0
+        if ws > 1:
+            tt = torch.tensor([t_e2e], device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            t_e2e = float(tt.item())
+        h2d = sum(v.numel() * v.element_size() for v in h_in.values()) + h_u.numel() * 8
+        d2h = sum(h_out[k].numel() * h_out[k].element_size() for k in N.STATE_OUT_FIELDS)
+        d2h += sum(v.numel() * v.element_size() for v in h_res.values())
+        e2e = {"value": ws * n * ctx_steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "steps": ctx_steps, "ms_per_step": 1e3 * t_e2e / ctx_steps,
+               "entry_point": "hepem_step_host (pinned host buffers)"}
+
+    if rank != 0:
+        return
+    hbm, hbm_src = peaks()
+    alg = algorithmic_bytes(n, uniforms_consumed, secondaries)
+    achieved = alg / (ms_step / 1e3) / 1e9
+    prof = profile_summary("step_fp64_traffic.json")
+    traffic = None
+    if prof and prof.get("tracks"):
+        traffic = prof["dram_bytes"] * n / prof["tracks"]
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": traffic, "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)" if hbm_src == "measured"
+            else "fallback", "algorithmic_bytes_per_launch": alg,
+            "note": "the step kernel is bound by the FP64 pipe, not HBM: see fp64"}
+    fp64 = {"peak_tflops_dgemm": None}
+    try:
+        fp64["peak_tflops_dgemm"] = fp64_peak_tflops(torch)
+    except Exception as ex:  # pragma: no cover
+        fp64["error"] = str(ex)
+    fprof = profile_summary("step_fp64_ops.json")
+    if fprof and fp64["peak_tflops_dgemm"]:
+        flops = fprof["dflop_per_track"] * n
+        fp64["achieved_tflops"] = flops / (ms_step / 1e3) / 1e12
+        fp64["frac"] = fp64["achieved_tflops"] / fp64["peak_tflops_dgemm"]
+        fp64["dflop_per_track"] = fprof["dflop_per_track"]
+    cpu = None
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        nsamp = min(n, 1 << 20)
+        r, dt = cpu_port_rate(st_np, threads, nsamp, reps=2)
+        cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"first {nsamp} tracks of the workload, 2 passes ({dt:.2f} s), {threads} host threads"}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": CONFIG, "e2e": e2e,
+            "gpu_launches": args.steps, "roofline": roof, "fp64": fp64, "cpu_baseline": cpu, "clocks": clk,
+            "counters": {"uniforms_per_step": uniforms_consumed, "secondaries_per_step": secondaries,
+                         "interactions": [int(x) for x in c[4:12]]}}
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

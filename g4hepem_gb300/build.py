@@ -1,0 +1,81 @@
+"""Build the native library in-tree: g4hepem_gb300/libg4hepem_gb300.so.
+
+One -gencode (sm_103a), translation units compiled in parallel, then linked.
+The FP64 kernels are compiled with --fmad=false (operation-by-operation IEEE
+arithmetic, as the reference host code); host code with -ffp-contract=off.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "libg4hepem_gb300.so")
+BUILD = os.path.join(HERE, "_build")
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+# (source, extra nvcc flags)
+UNITS = [
+    ("kernels_fp64.cu", ["-fmad=false"]),
+    ("api.cu", ["-fmad=false"]),
+    ("state_json.cpp", []),
+]
+
+
+def nvcc() -> str:
+    p = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(p):
+        raise RuntimeError("nvcc not found")
+    return p
+
+
+def _sources():
+    return [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(REPO, "include", "g4hepem_gb300.h")]
+
+
+def up_to_date() -> bool:
+    if not os.path.exists(OUT):
+        return False
+    t = os.path.getmtime(OUT)
+    return all(os.path.getmtime(s) <= t for s in _sources())
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    if not force and up_to_date():
+        return OUT
+    os.makedirs(BUILD, exist_ok=True)
+    cc = nvcc()
+    common = ["-O3", "-std=c++17", "-lineinfo", ARCH, "-Xcompiler", "-fPIC,-ffp-contract=off",
+              "-I", os.path.join(REPO, "include"), "-I", CSRC]
+
+    def compile_unit(u):
+        src, extra = u
+        obj = os.path.join(BUILD, src + ".o")
+        cmd = [cc, "-c", os.path.join(CSRC, src), "-o", obj] + common + extra
+        if src.endswith(".cpp"):
+            cmd = [cc, "-x", "c++", "-c", os.path.join(CSRC, src), "-o", obj, "-O3", "-std=c++17",
+                   "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", os.path.join(REPO, "include"), "-I", CSRC]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+        if verbose and (r.stdout or r.stderr):
+            print(r.stdout, r.stderr, file=sys.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        objs = list(ex.map(compile_unit, UNITS))
+    tmp = OUT + ".tmp"
+    r = subprocess.run([cc, "-shared", ARCH, "-o", tmp] + objs + ["-lcudart"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, OUT)
+    return OUT
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

@@ -1,0 +1,234 @@
+// api.cu -- the extern "C" boundary declared in include/g4hepem_gb300.h.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+
+#include "g4hepem_gb300.h"
+#include "kernels.h"
+#include "rng.cuh"
+#include "state_image.h"
+
+struct hepem_ctx {
+  int device = -1;
+  int sms = 0;
+  void* arena = nullptr;
+  size_t arenaBytes = 0;
+  hepem::DevTables tables;
+  // staging area of hepem_step_host (grow-only, serialised by mu)
+  std::mutex mu;
+  void* stage = nullptr;
+  size_t stageBytes = 0;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  return fail(HEPEM_CUDA_ERROR, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define HEPEM_CUDA(call)                              \
+  do {                                                \
+    cudaError_t e_ = (call);                          \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+int create_from_image(hepem::StateImage& img, hepem_ctx** out) {
+  int dev = 0;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(HEPEM_NO_DEVICE, "no CUDA device");
+  HEPEM_CUDA(cudaGetDevice(&dev));
+  hepem_ctx* c = new hepem_ctx();
+  c->device = dev;
+  cudaError_t e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaMalloc(&c->arena, img.bytes.size());
+  if (e == cudaSuccess) e = cudaMemcpy(c->arena, img.bytes.data(), img.bytes.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    if (c->arena) cudaFree(c->arena);
+    delete c;
+    return cuda_fail(e, "arena upload");
+  }
+  c->arenaBytes = img.bytes.size();
+  hepem::relocate(img, c->tables, c->arena);
+  *out = c;
+  return HEPEM_OK;
+}
+
+bool state_ok(const hepem_track_state* s) {
+  return s && s->type && s->imc && s->id && s->ekin && s->dir_x && s->dir_y && s->dir_z && s->nia0 && s->nia1 &&
+         s->nia2 && s->nia3 && s->safety && s->on_boundary && s->msc_init_range && s->msc_dyn_factor &&
+         s->msc_tlimit_min && s->msc_first_step && s->gauss_valid && s->gauss_value && s->rng_cursor;
+}
+
+bool out_ok(const hepem_step_out* r) {
+  return r && r->edep && r->gstep && r->pstep && r->winner && r->disp_x && r->disp_y && r->disp_z && r->flags &&
+         r->n_sec && r->sec_type && r->sec_ekin && r->sec_dir_x && r->sec_dir_y && r->sec_dir_z;
+}
+
+// Byte size of each per-track array, in the field order of the structs.
+const size_t kStateSizes[20] = {1, 4, 4, 8, 8, 8, 8, 8, 8, 8, 8, 8, 1, 8, 8, 8, 1, 1, 8, 4};
+const size_t kOutSizes[14] = {8, 8, 8, 1, 8, 8, 8, 1, 1, 2, 16, 16, 16, 16};  // secondaries: 2 slots
+
+}  // namespace
+
+extern "C" {
+
+const char* hepem_status_string(int s) {
+  switch (s) {
+    case HEPEM_OK: return "ok";
+    case HEPEM_BAD_ARG: return "bad argument";
+    case HEPEM_PARSE_ERROR: return "state JSON does not follow the G4HepEmState schema";
+    case HEPEM_CUDA_ERROR: return "CUDA error";
+    case HEPEM_RNG_EXHAUSTED: return "a track read past its buffered uniforms";
+    case HEPEM_TIMEOUT: return "bounded wait gave up";
+    case HEPEM_OOM_ADMISSION: return "request exceeds the memory budget";
+    case HEPEM_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+const char* hepem_last_error(void) { return g_last_error.c_str(); }
+
+int hepem_create(const char* json, size_t len, hepem_ctx** out) {
+  if (!json || !out) return fail(HEPEM_BAD_ARG, "null argument");
+  *out = nullptr;
+  try {
+    hepem::StateImage img = hepem::build_state_image(json, len);
+    return create_from_image(img, out);
+  } catch (const std::exception& e) {
+    return fail(HEPEM_PARSE_ERROR, e.what());
+  }
+}
+
+int hepem_create_from_file(const char* path, hepem_ctx** out) {
+  if (!path || !out) return fail(HEPEM_BAD_ARG, "null argument");
+  *out = nullptr;
+  try {
+    hepem::StateImage img = hepem::build_state_image_file(path);
+    return create_from_image(img, out);
+  } catch (const std::exception& e) {
+    return fail(HEPEM_PARSE_ERROR, e.what());
+  }
+}
+
+int hepem_destroy(hepem_ctx* c) {
+  if (!c) return HEPEM_OK;
+  cudaError_t e = cudaSuccess;
+  if (c->arena) e = cudaFree(c->arena);
+  if (c->stage) cudaFree(c->stage);
+  delete c;
+  return e == cudaSuccess ? HEPEM_OK : cuda_fail(e, "cudaFree");
+}
+
+int hepem_info(const hepem_ctx* c, int32_t* nc, int32_t* nm, int32_t* nr, int64_t* bytes) {
+  if (!c) return fail(HEPEM_BAD_ARG, "null context");
+  if (nc) *nc = c->tables.nCouples;
+  if (nm) *nm = c->tables.nMats;
+  if (nr) *nr = c->tables.nRegions;
+  if (bytes) *bytes = (int64_t)c->arenaBytes;
+  return HEPEM_OK;
+}
+
+int hepem_electron_lookup(const hepem_ctx* c, int64_t n, int is_positron, const double* ekin, const int32_t* imc,
+                          double* xi, double* xb, double* dedx, double* range, double* invr, void* stream) {
+  if (!c || n < 0) return fail(HEPEM_BAD_ARG, "bad context or size");
+  if (n == 0) return HEPEM_OK;
+  if (!ekin || !imc || !xi || !xb || !dedx || !range || !invr) return fail(HEPEM_BAD_ARG, "null array");
+  HEPEM_CUDA(hepem::launch_lookup(c->tables, n, is_positron ? 1 : 0, ekin, imc, xi, xb, dedx, range, invr,
+                                  (cudaStream_t)stream, c->sms));
+  return HEPEM_OK;
+}
+
+int hepem_step(const hepem_ctx* c, int64_t n, const hepem_track_state* in, hepem_track_state* out,
+               const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res,
+               hepem_step_counters* counters, void* stream) {
+  if (!c || n < 0 || nu < 0) return fail(HEPEM_BAD_ARG, "bad context or size");
+  if (n == 0) return HEPEM_OK;
+  if (!state_ok(in) || !state_ok(out) || !out_ok(res) || (nu > 0 && !uniforms))
+    return fail(HEPEM_BAD_ARG, "null array in track batch");
+  if (n > (int64_t)INT32_MAX * 2 / 3) return fail(HEPEM_BAD_ARG, "batch too large");
+  HEPEM_CUDA(hepem::launch_step(c->tables, n, *in, *out, uniforms, nu, seed, *res, counters, (cudaStream_t)stream,
+                                c->sms));
+  return HEPEM_OK;
+}
+
+int hepem_step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem_track_state* out,
+                    const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res,
+                    hepem_step_counters* counters, void* stream) {
+  hepem_ctx* c = const_cast<hepem_ctx*>(cc);
+  if (!c || n < 0 || nu < 0) return fail(HEPEM_BAD_ARG, "bad context or size");
+  if (n == 0) return HEPEM_OK;
+  if (!state_ok(in) || !state_ok(out) || !out_ok(res) || (nu > 0 && !uniforms))
+    return fail(HEPEM_BAD_ARG, "null array in track batch");
+  std::lock_guard<std::mutex> lock(c->mu);
+  cudaStream_t s = (cudaStream_t)stream;
+  // device staging: 20 state arrays, 14 result arrays, uniforms, counters
+  size_t need = 0;
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  for (size_t b : kStateSizes) need += al(b * n);
+  for (size_t b : kOutSizes) need += al(b * n);
+  need += al(sizeof(double) * (size_t)n * nu) + al(sizeof(hepem_step_counters));
+  if (need > c->stageBytes) {
+    if (c->stage) HEPEM_CUDA(cudaFree(c->stage));
+    c->stage = nullptr;
+    c->stageBytes = 0;
+    HEPEM_CUDA(cudaMalloc(&c->stage, need));
+    c->stageBytes = need;
+  }
+  uint8_t* p = (uint8_t*)c->stage;
+  void* dstate[20];
+  void* dout[14];
+  for (int k = 0; k < 20; ++k) { dstate[k] = p; p += al(kStateSizes[k] * n); }
+  for (int k = 0; k < 14; ++k) { dout[k] = p; p += al(kOutSizes[k] * n); }
+  double* du = (double*)p;
+  p += al(sizeof(double) * (size_t)n * nu);
+  hepem_step_counters* dcnt = (hepem_step_counters*)p;
+  hepem_track_state ds;
+  hepem_step_out dr;
+  static_assert(sizeof(hepem_track_state) == 20 * sizeof(void*), "state struct layout");
+  static_assert(sizeof(hepem_step_out) == 14 * sizeof(void*), "out struct layout");
+  memcpy(&ds, dstate, sizeof(ds));
+  memcpy(&dr, dout, sizeof(dr));
+  void* const* hin = reinterpret_cast<void* const*>(in);
+  void* const* hout = reinterpret_cast<void* const*>(out);
+  void* const* hres = reinterpret_cast<void* const*>(res);
+  for (int k = 0; k < 20; ++k) HEPEM_CUDA(cudaMemcpyAsync(dstate[k], hin[k], kStateSizes[k] * n, cudaMemcpyHostToDevice, s));
+  if (nu > 0) HEPEM_CUDA(cudaMemcpyAsync(du, uniforms, sizeof(double) * (size_t)n * nu, cudaMemcpyHostToDevice, s));
+  if (counters) HEPEM_CUDA(cudaMemsetAsync(dcnt, 0, sizeof(*dcnt), s));
+  HEPEM_CUDA(hepem::launch_step(c->tables, n, ds, ds, du, nu, seed, dr, counters ? dcnt : nullptr, s, c->sms));
+  // the persistent per-track fields come back (type/imc/id/safety/boundary are inputs only)
+  for (int k = 3; k < 20; ++k) {
+    if (k == 11 || k == 12) continue;
+    HEPEM_CUDA(cudaMemcpyAsync(hout[k], dstate[k], kStateSizes[k] * n, cudaMemcpyDeviceToHost, s));
+  }
+  if (hout[0] != hin[0]) {
+    for (int k : {0, 1, 2, 11, 12}) memcpy(hout[k], hin[k], kStateSizes[k] * n);
+  }
+  for (int k = 0; k < 14; ++k) HEPEM_CUDA(cudaMemcpyAsync(hres[k], dout[k], kOutSizes[k] * n, cudaMemcpyDeviceToHost, s));
+  if (counters) HEPEM_CUDA(cudaMemcpyAsync(counters, dcnt, sizeof(*dcnt), cudaMemcpyDeviceToHost, s));
+  HEPEM_CUDA(cudaStreamSynchronize(s));
+  return HEPEM_OK;
+}
+
+double hepem_philox_uniform(uint64_t seed, int32_t id, int32_t k) { return hepem::philox_uniform(seed, id, k); }
+
+int hepem_fill_uniforms(int64_t n, const int32_t* id, int32_t nu, uint64_t seed, double* u, void* stream) {
+  if (n < 0 || nu < 0 || (n > 0 && nu > 0 && (!id || !u))) return fail(HEPEM_BAD_ARG, "bad argument");
+  int dev = 0, sms = 0;
+  HEPEM_CUDA(cudaGetDevice(&dev));
+  HEPEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  HEPEM_CUDA(hepem::launch_fill_uniforms(n, id, nu, seed, u, (cudaStream_t)stream, sms));
+  return HEPEM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,23 @@
+// kernels.h -- host launchers of the device kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "g4hepem_gb300.h"
+#include "tables.h"
+
+namespace hepem {
+
+cudaError_t launch_lookup(const DevTables& T, int64_t n, int pos, const double* ekin, const int32_t* imc, double* xi,
+                          double* xb, double* dedx, double* range, double* invr, cudaStream_t s, int sms);
+
+cudaError_t launch_step(const DevTables& T, int64_t n, const hepem_track_state& in, const hepem_track_state& out,
+                        const double* uniforms, int nu, uint64_t seed, const hepem_step_out& res,
+                        hepem_step_counters* counters, cudaStream_t s, int sms);
+
+cudaError_t launch_fill_uniforms(int64_t n, const int32_t* id, int nu, uint64_t seed, double* u, cudaStream_t s,
+                                 int sms);
+
+}  // namespace hepem

@@ -1,0 +1,233 @@
+// kernels_fp64.cu -- plain FP64 kernels of the drop-in path (compiled with
+// --fmad=false: no contracted multiply-adds, so the arithmetic is the
+// reference's operation by operation).
+//
+//  lookup_kernel  : BASELINE configuration 1, the reference functions
+//                   GetRestMacXSec / GetRestDEDX / GetRestRange / GetInvRange
+//                   (G4HepEm/G4HepEmRun/include/G4HepEmElectronManager.icc:486-532)
+//  step_kernel    : one HowFar + Perform per track (configuration 2)
+//  fill_uniforms  : the per-track Philox streams of the C-ABI contract
+#include <cstdint>
+
+#include "g4hepem_gb300.h"
+#include "kernels.h"
+#include "physics.cuh"
+
+namespace hepem {
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) lookup_kernel(const __grid_constant__ DevTables T, int64_t n, int pos,
+                                                     const double* __restrict__ ekin, const int32_t* __restrict__ imc,
+                                                     double* __restrict__ xi, double* __restrict__ xb,
+                                                     double* __restrict__ dedx, double* __restrict__ range,
+                                                     double* __restrict__ invr) {
+  const DevElData& d = T.el[pos ? 1 : 0];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double e = ekin[i];
+    int c = imc[i];
+    const bool bad = !(c >= 0 && c < T.nCouples) || !(e > 0.0) || !(e < 1.0e300);
+    if (bad) c = 0;
+    const double le = vdt_log(e);
+    const double a = rest_macxs(d, c, e, le, true);
+    const double b = rest_macxs(d, c, e, le, false);
+    const double s = rest_dedx(d, c, e, le);
+    const double r = rest_range(d, c, e, le);
+    const double q = inv_range(d, c, 0.5 * r);
+    const double nan = __longlong_as_double(0x7FF8000000000000LL);
+    xi[i] = bad ? nan : a;
+    xb[i] = bad ? nan : b;
+    dedx[i] = bad ? nan : s;
+    range[i] = bad ? nan : r;
+    invr[i] = bad ? nan : q;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Block-level sum of the step counters: warp reduce, then one atomic per block.
+struct StepCount {
+  uint32_t steps, uniforms, overflow, secondaries, inter[8];
+};
+
+__device__ __forceinline__ void add_counters(StepCount& c, hepem_step_counters* g) {
+  __shared__ uint32_t s[12];
+  if (threadIdx.x < 12) s[threadIdx.x] = 0;
+  __syncthreads();
+  uint32_t v[12] = {c.steps, c.uniforms, c.overflow, c.secondaries, c.inter[0], c.inter[1], c.inter[2], c.inter[3],
+                    c.inter[4], c.inter[5], c.inter[6], c.inter[7]};
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    const uint32_t w = __reduce_add_sync(0xFFFFFFFFu, v[k]);
+    if ((threadIdx.x & 31) == 0 && w) atomicAdd(&s[k], w);
+  }
+  __syncthreads();
+  if (threadIdx.x < 12 && s[threadIdx.x]) {
+    unsigned long long* dst = threadIdx.x < 4 ? (unsigned long long*)&g->steps + threadIdx.x
+                                              : (unsigned long long*)&g->interactions[threadIdx.x - 4];
+    atomicAdd(dst, (unsigned long long)s[threadIdx.x]);
+  }
+}
+
+__device__ __forceinline__ void step_one(const DevTables& T, int64_t i, const hepem_track_state& in,
+                                         const hepem_track_state& out, const double* uniforms, int nu,
+                                         uint64_t seed, const hepem_step_out& res, StepCount& cnt) {
+  const int type = in.type[i];
+  Track t;
+  t.imc = in.imc[i];
+  t.setE(in.ekin[i]);
+  t.flags = 0;
+  t.nsec = 0;
+  const bool bad = !(type >= 0 && type <= 2) || !(t.imc >= 0 && t.imc < T.nCouples) || !(t.e > 0.0) ||
+                   !(t.e < 1.0e300);
+  Rng rng;
+  rng.u = uniforms + i * (int64_t)nu;
+  rng.n = nu;
+  rng.cursor = in.rng_cursor[i];
+  rng.id = in.id[i];
+  rng.overflow = 0u;
+  rng.seed = seed;
+  rng.gaussValid = in.gauss_valid[i] != 0;
+  rng.gaussValue = in.gauss_value[i];
+  t.dir[0] = in.dir_x[i];
+  t.dir[1] = in.dir_y[i];
+  t.dir[2] = in.dir_z[i];
+  t.onBoundary = in.on_boundary[i] != 0;
+  t.nia[0] = in.nia0[i];
+  t.winner = -1;
+  t.edep = 0.0;
+  t.gstep = 0.0;
+  t.pstep = 0.0;
+  Physics P{T, rng, t};
+  double nia1 = in.nia1[i], nia2 = in.nia2[i], nia3 = in.nia3[i];
+  double mir = in.msc_init_range[i], mdf = in.msc_dyn_factor[i], mtm = in.msc_tlimit_min[i];
+  uint8_t mfs = in.msc_first_step[i];
+  t.msc.disp[0] = t.msc.disp[1] = t.msc.disp[2] = 0.0;
+  if (bad) {
+    t.flags |= kFlagBadInput;
+  } else if (type == 2) {
+    t.isEl = false;
+    P.gamma_howfar();
+    if (t.onBoundary) {
+      t.nia[0] -= t.gstep / t.mfp[0];
+    } else {
+      P.gamma_select();
+      P.gamma_perform();
+    }
+    t.pstep = t.gstep;
+  } else {
+    t.isEl = type == 0;
+    t.nia[1] = nia1; t.nia[2] = nia2; t.nia[3] = nia3;
+    t.safety = in.safety[i];
+    t.msc.initRange = mir;
+    t.msc.dynFactor = mdf;
+    t.msc.tlimitMin = mtm;
+    t.msc.firstStep = mfs != 0;
+    P.el_howfar();
+    P.el_perform();
+    nia1 = t.nia[1]; nia2 = t.nia[2]; nia3 = t.nia[3];
+    mir = t.msc.initRange; mdf = t.msc.dynFactor; mtm = t.msc.tlimitMin;
+    mfs = t.msc.firstStep ? 1 : 0;
+  }
+  if (rng.overflow) t.flags |= kFlagRngOverflow;
+  // state out (out may alias in: every input was read above)
+  out.ekin[i] = t.e;
+  out.dir_x[i] = t.dir[0];
+  out.dir_y[i] = t.dir[1];
+  out.dir_z[i] = t.dir[2];
+  out.nia0[i] = t.nia[0];
+  out.nia1[i] = nia1;
+  out.nia2[i] = nia2;
+  out.nia3[i] = nia3;
+  out.msc_init_range[i] = mir;
+  out.msc_dyn_factor[i] = mdf;
+  out.msc_tlimit_min[i] = mtm;
+  out.msc_first_step[i] = mfs;
+  out.gauss_valid[i] = rng.gaussValid ? 1 : 0;
+  out.gauss_value[i] = rng.gaussValue;
+  out.rng_cursor[i] = rng.cursor;
+  if (out.type != in.type) {
+    out.type[i] = (int8_t)type;
+    out.imc[i] = in.imc[i];
+    out.id[i] = in.id[i];
+    out.safety[i] = in.safety[i];
+    out.on_boundary[i] = in.on_boundary[i];
+  }
+  res.edep[i] = t.edep;
+  res.gstep[i] = t.gstep;
+  res.pstep[i] = t.pstep;
+  res.winner[i] = (int8_t)t.winner;
+  const bool charged = type != 2 && !bad;
+  res.disp_x[i] = charged ? t.msc.disp[0] : 0.0;
+  res.disp_y[i] = charged ? t.msc.disp[1] : 0.0;
+  res.disp_z[i] = charged ? t.msc.disp[2] : 0.0;
+  res.flags[i] = t.flags;
+  const int ns = t.nsec > 2 ? 2 : t.nsec;
+  res.n_sec[i] = (int8_t)ns;
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    if (k < ns) {
+      res.sec_type[2 * i + k] = t.sec[k].type;
+      res.sec_ekin[2 * i + k] = t.sec[k].e;
+      res.sec_dir_x[2 * i + k] = t.sec[k].dir[0];
+      res.sec_dir_y[2 * i + k] = t.sec[k].dir[1];
+      res.sec_dir_z[2 * i + k] = t.sec[k].dir[2];
+    }
+  }
+  cnt.steps += 1;
+  cnt.uniforms += (uint32_t)(rng.cursor - in.rng_cursor[i]);
+  cnt.overflow += rng.overflow;
+  cnt.secondaries += ns;
+  if (!bad && t.winner >= 0 && t.winner < 4) cnt.inter[(type == 2 ? 4 : 0) + t.winner] += 1;
+}
+
+__global__ void __launch_bounds__(256) step_kernel(const __grid_constant__ DevTables T, int64_t n,
+                                                   const hepem_track_state in, const hepem_track_state out,
+                                                   const double* __restrict__ uniforms, int nu, uint64_t seed,
+                                                   const hepem_step_out res, hepem_step_counters* counters) {
+  StepCount cnt = {};
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    if (i < n) step_one(T, i, in, out, uniforms, nu, seed, res, cnt);
+  }
+  if (counters) add_counters(cnt, counters);
+}
+
+__global__ void fill_uniforms_kernel(int64_t n, const int32_t* __restrict__ id, int nu, uint64_t seed,
+                                     double* __restrict__ u) {
+  const int64_t total = n * nu;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < total; j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = j / nu;
+    const int k = (int)(j - i * nu);
+    u[j] = philox_uniform(seed, id[i], k);
+  }
+}
+
+// ---- host launchers ---------------------------------------------------------------
+static int grid_for(int64_t n, int block, int sms) {
+  const int64_t need = (n + block - 1) / block;
+  const int64_t cap = (int64_t)sms * 32;
+  return (int)(need < cap ? (need > 0 ? need : 1) : cap);
+}
+
+cudaError_t launch_lookup(const DevTables& T, int64_t n, int pos, const double* ekin, const int32_t* imc, double* xi,
+                          double* xb, double* dedx, double* range, double* invr, cudaStream_t s, int sms) {
+  if (n <= 0) return cudaSuccess;
+  lookup_kernel<<<grid_for(n, 256, sms), 256, 0, s>>>(T, n, pos, ekin, imc, xi, xb, dedx, range, invr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step(const DevTables& T, int64_t n, const hepem_track_state& in, const hepem_track_state& out,
+                        const double* uniforms, int nu, uint64_t seed, const hepem_step_out& res,
+                        hepem_step_counters* counters, cudaStream_t s, int sms) {
+  if (n <= 0) return cudaSuccess;
+  step_kernel<<<grid_for(n, 256, sms), 256, 0, s>>>(T, n, in, out, uniforms, nu, seed, res, counters);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_uniforms(int64_t n, const int32_t* id, int nu, uint64_t seed, double* u, cudaStream_t s,
+                                 int sms) {
+  if (n <= 0 || nu <= 0) return cudaSuccess;
+  fill_uniforms_kernel<<<grid_for(n * nu, 256, sms), 256, 0, s>>>(n, id, nu, seed, u);
+  return cudaGetLastError();
+}
+
+}  // namespace hepem

@@ -1,0 +1,25 @@
+// state_image.h -- host-side image of the device table arena.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <utility>
+#include <vector>
+
+#include "tables.h"
+
+namespace hepem {
+
+struct StateImage {
+  std::vector<uint8_t> bytes;                    // arena contents (256-byte aligned arrays)
+  DevTables host;                                // pointer fields hold nothing useful yet
+  std::vector<std::pair<size_t, size_t>> relocs; // (offset of pointer field in DevTables, arena offset)
+};
+
+// Parse + validate a G4HepEmState JSON document; throws std::runtime_error.
+StateImage build_state_image(const char* text, size_t len);
+StateImage build_state_image_file(const char* path);
+// Resolve the pointer fields against the arena base address `base`.
+void relocate(StateImage& img, DevTables& out, const void* base);
+
+}  // namespace hepem

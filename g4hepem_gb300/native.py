@@ -1,0 +1,219 @@
+"""ctypes front end of libg4hepem_gb300.so (the C-ABI of include/g4hepem_gb300.h).
+
+Device memory and streams come from torch; the library takes raw pointers.
+Importing this module never falls back to anything: if the library is missing
+it raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libg4hepem_gb300.so")
+
+_vp = C.c_void_p
+
+STATE_FIELDS = [("type", np.int8), ("imc", np.int32), ("id", np.int32), ("ekin", np.float64),
+                ("dir_x", np.float64), ("dir_y", np.float64), ("dir_z", np.float64), ("nia0", np.float64),
+                ("nia1", np.float64), ("nia2", np.float64), ("nia3", np.float64), ("safety", np.float64),
+                ("on_boundary", np.uint8), ("msc_init_range", np.float64), ("msc_dyn_factor", np.float64),
+                ("msc_tlimit_min", np.float64), ("msc_first_step", np.uint8), ("gauss_valid", np.uint8),
+                ("gauss_value", np.float64), ("rng_cursor", np.int32)]
+# (name, dtype, slots per track)
+OUT_FIELDS = [("edep", np.float64, 1), ("gstep", np.float64, 1), ("pstep", np.float64, 1), ("winner", np.int8, 1),
+              ("disp_x", np.float64, 1), ("disp_y", np.float64, 1), ("disp_z", np.float64, 1),
+              ("flags", np.uint8, 1), ("n_sec", np.int8, 1), ("sec_type", np.int8, 2),
+              ("sec_ekin", np.float64, 2), ("sec_dir_x", np.float64, 2), ("sec_dir_y", np.float64, 2),
+              ("sec_dir_z", np.float64, 2)]
+# fields copied back by hepem_step_host (persistent outputs of the step)
+STATE_OUT_FIELDS = [f for f, _ in STATE_FIELDS if f not in ("type", "imc", "id", "safety", "on_boundary")]
+
+FLAG_RNG_OVERFLOW, FLAG_LOOP_CAP, FLAG_BAD_INPUT, FLAG_BAD_INDEX = 1, 2, 4, 8
+
+
+class TrackState(C.Structure):
+    _fields_ = [(f, _vp) for f, _ in STATE_FIELDS]
+
+
+class StepOut(C.Structure):
+    _fields_ = [(f, _vp) for f, _, _ in OUT_FIELDS]
+
+
+class StepCounters(C.Structure):
+    _fields_ = [("steps", C.c_uint64), ("uniforms", C.c_uint64), ("rng_overflow", C.c_uint64),
+                ("secondaries", C.c_uint64), ("interactions", C.c_uint64 * 8)]
+
+
+EXPORTED = ["hepem_create", "hepem_create_from_file", "hepem_destroy", "hepem_info", "hepem_status_string",
+            "hepem_last_error", "hepem_electron_lookup", "hepem_step", "hepem_step_host", "hepem_philox_uniform",
+            "hepem_fill_uniforms"]
+
+
+class HepEmError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run g4hepem_gb300.build.build() first")
+        L = C.CDLL(LIB_PATH)
+        L.hepem_create.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(_vp)]
+        L.hepem_create_from_file.argtypes = [C.c_char_p, C.POINTER(_vp)]
+        L.hepem_destroy.argtypes = [_vp]
+        L.hepem_info.argtypes = [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                 C.POINTER(C.c_int64)]
+        L.hepem_status_string.argtypes = [C.c_int]
+        L.hepem_status_string.restype = C.c_char_p
+        L.hepem_last_error.restype = C.c_char_p
+        L.hepem_electron_lookup.argtypes = [_vp, C.c_int64, C.c_int] + [_vp] * 7 + [_vp]
+        L.hepem_step.argtypes = [_vp, C.c_int64, C.POINTER(TrackState), C.POINTER(TrackState), _vp, C.c_int32,
+                                 C.c_uint64, C.POINTER(StepOut), _vp, _vp]
+        L.hepem_step_host.argtypes = L.hepem_step.argtypes
+        L.hepem_philox_uniform.argtypes = [C.c_uint64, C.c_int32, C.c_int32]
+        L.hepem_philox_uniform.restype = C.c_double
+        L.hepem_fill_uniforms.argtypes = [C.c_int64, _vp, C.c_int32, C.c_uint64, _vp, _vp]
+        _LIB = L
+    return _LIB
+
+
+def check(rc):
+    if rc != 0:
+        L = lib()
+        raise HepEmError(rc, f"{L.hepem_status_string(rc).decode()}: {L.hepem_last_error().decode()}")
+
+
+def _ptr(x):
+    """Raw data pointer of a torch tensor or numpy array."""
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    return x.data_ptr()
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+
+
+def make_state_struct(arrs: dict) -> TrackState:
+    s = TrackState()
+    for f, _ in STATE_FIELDS:
+        setattr(s, f, _ptr(arrs[f]))
+    return s
+
+
+def make_out_struct(arrs: dict) -> StepOut:
+    s = StepOut()
+    for f, _, _ in OUT_FIELDS:
+        setattr(s, f, _ptr(arrs[f]))
+    return s
+
+
+class Context:
+    """Tables of one G4HepEmState on the current CUDA device."""
+
+    def __init__(self, json_path: str | None = None, json_text: str | bytes | None = None):
+        L = lib()
+        h = _vp()
+        if json_text is not None:
+            b = json_text.encode() if isinstance(json_text, str) else json_text
+            check(L.hepem_create(b, len(b), C.byref(h)))
+        else:
+            check(L.hepem_create_from_file(json_path.encode(), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().hepem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        nc, nm, nr, nb = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int64()
+        check(lib().hepem_info(self.h, C.byref(nc), C.byref(nm), C.byref(nr), C.byref(nb)))
+        return dict(n_couples=nc.value, n_materials=nm.value, n_regions=nr.value, arena_bytes=nb.value)
+
+    # -- device-pointer entry points (torch CUDA tensors) ----------------------
+    def electron_lookup(self, ekin, imc, positron=False, out=None, stream=None):
+        import torch
+        n = ekin.numel()
+        if out is None:
+            out = {k: torch.empty(n, dtype=torch.float64, device=ekin.device)
+                   for k in ("xs_ioni", "xs_brem", "dedx", "range", "invrange_half")}
+        check(lib().hepem_electron_lookup(self.h, n, int(positron), _ptr(ekin), _ptr(imc), _ptr(out["xs_ioni"]),
+                                          _ptr(out["xs_brem"]), _ptr(out["dedx"]), _ptr(out["range"]),
+                                          _ptr(out["invrange_half"]), _stream_ptr(stream)))
+        return out
+
+    def step(self, state_in: dict, state_out: dict, uniforms, n_uniform: int, seed: int, res: dict,
+             counters=None, stream=None):
+        n = state_in["ekin"].numel()
+        sin, sout, sres = make_state_struct(state_in), make_state_struct(state_out), make_out_struct(res)
+        check(lib().hepem_step(self.h, n, C.byref(sin), C.byref(sout), _ptr(uniforms), n_uniform, seed,
+                               C.byref(sres), _ptr(counters) if counters is not None else None,
+                               _stream_ptr(stream)))
+
+    # -- host-buffer entry point (numpy arrays) ----------------------------------
+    def step_host(self, state_in: dict, state_out: dict, uniforms: np.ndarray, n_uniform: int, seed: int,
+                  res: dict, stream=None):
+        n = len(state_in["ekin"])
+        cnt = StepCounters()
+        sin, sout, sres = make_state_struct(state_in), make_state_struct(state_out), make_out_struct(res)
+        check(lib().hepem_step_host(self.h, n, C.byref(sin), C.byref(sout), _ptr(uniforms), n_uniform, seed,
+                                    C.byref(sres), C.byref(cnt), _stream_ptr(stream)))
+        return cnt
+
+
+def philox_uniform(seed: int, tid: int, k: int) -> float:
+    return lib().hepem_philox_uniform(seed, tid, k)
+
+
+def fill_uniforms(ids, n_uniform: int, seed: int, out=None, stream=None):
+    import torch
+    n = ids.numel()
+    if out is None:
+        out = torch.empty(n * n_uniform, dtype=torch.float64, device=ids.device)
+    check(lib().hepem_fill_uniforms(n, _ptr(ids), n_uniform, seed, _ptr(out), _stream_ptr(stream)))
+    return out
+
+
+# -- helpers for numpy <-> torch batches -----------------------------------------------------
+def alloc_out_numpy(n: int) -> dict:
+    return {f: np.zeros(n * k, dtype=dt) for f, dt, k in OUT_FIELDS}
+
+
+def alloc_out_torch(n: int, device="cuda") -> dict:
+    import torch
+    tmap = {np.float64: torch.float64, np.int8: torch.int8, np.uint8: torch.uint8, np.int32: torch.int32}
+    return {f: torch.zeros(n * k, dtype=tmap[dt], device=device) for f, dt, k in OUT_FIELDS}
+
+
+def state_to_torch(state: dict, device="cuda") -> dict:
+    import torch
+    return {f: torch.from_numpy(np.ascontiguousarray(state[f])).to(device) for f, _ in STATE_FIELDS}
+
+
+def to_numpy(d: dict) -> dict:
+    return {k: v.cpu().numpy() for k, v in d.items()}
+
+
+def empty_state_torch(n: int, device="cuda") -> dict:
+    import torch
+    tmap = {np.float64: torch.float64, np.int8: torch.int8, np.uint8: torch.uint8, np.int32: torch.int32}
+    return {f: torch.empty(n, dtype=tmap[dt], device=device) for f, dt in STATE_FIELDS}

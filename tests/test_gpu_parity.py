@@ -1,0 +1,223 @@
+"""GPU parity: the CUDA path, called through the C-ABI, against the reference
+golden vectors and the CPU port.
+
+Tolerances (see parity.py): discrete outcomes identical; continuous values
+within 1e-12 relative; direction cosines within 1e-12 absolute.
+"""
+import numpy as np
+import pytest
+
+from conftest import T3, T16, golden_res, golden_state, load_golden
+from g4hepem_gb300 import workload as W
+from parity import compare_steps, energy_balance
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def gpu_step(native, ctx, st_np, seed, nu, uniforms_np=None, in_place=False):
+    torch = _torch()
+    n = len(st_np["ekin"])
+    sin = native.state_to_torch(st_np)
+    sout = sin if in_place else native.empty_state_torch(n)
+    res = native.alloc_out_torch(n)
+    if uniforms_np is None:
+        u = native.fill_uniforms(sin["id"], nu, seed)
+    else:
+        u = torch.from_numpy(np.ascontiguousarray(uniforms_np).reshape(-1)).cuda()
+    cnt = torch.zeros(12, dtype=torch.int64, device="cuda")
+    ctx.step(sin, sout, u, nu, seed, res, counters=cnt)
+    torch.cuda.synchronize()
+    out = native.to_numpy(sout)
+    if not in_place:
+        for f in ("type", "imc", "id", "safety", "on_boundary"):
+            out[f] = st_np[f]
+    return out, native.to_numpy(res), cnt.cpu().numpy()
+
+
+def test_vdt_log_exp_bit_exact_on_device(native, gpu_ctx):
+    """log/exp through the lookup kernel's code path are covered below; here
+    the range-lookup of a table at E gives VDTLog(E) implicitly."""
+    g = load_golden("lookup_3couples.npz")
+    ctx = gpu_ctx(T3)
+    torch = _torch()
+    ekin = torch.from_numpy(g["ekin"]).cuda()
+    imc = torch.from_numpy(g["imc"]).cuda()
+    for pos in (0, 1):
+        out = ctx.electron_lookup(ekin, imc, positron=bool(pos))
+        torch.cuda.synchronize()
+        for k, v in out.items():
+            got = v.cpu().numpy()
+            assert np.array_equal(got, g[f"p{pos}_{k}"]), (pos, k, np.sum(got != g[f"p{pos}_{k}"]))
+
+
+def test_lookup_16_couples_golden(native, gpu_ctx):
+    g = load_golden("step_16couples.npz")
+    ctx = gpu_ctx(T16)
+    torch = _torch()
+    out = ctx.electron_lookup(torch.from_numpy(g["l_ekin"]).cuda(), torch.from_numpy(g["l_imc"]).cuda())
+    torch.cuda.synchronize()
+    for k in ("xs_ioni", "xs_brem", "dedx", "range", "invrange_half"):
+        assert np.array_equal(out[k].cpu().numpy(), g[f"l_{k}"]), k
+
+
+def test_lookup_bad_inputs_give_nan_not_faults(native, gpu_ctx):
+    ctx = gpu_ctx(T3)
+    torch = _torch()
+    ekin = torch.tensor([1.0, -1.0, 0.0, float("nan"), 10.0], dtype=torch.float64, device="cuda")
+    imc = torch.tensor([0, 0, 1, 2, 99], dtype=torch.int32, device="cuda")
+    out = ctx.electron_lookup(ekin, imc)
+    torch.cuda.synchronize()
+    r = out["range"].cpu().numpy()
+    assert np.isfinite(r[0]) and np.all(np.isnan(r[1:]))
+
+
+@pytest.mark.parametrize("prefix,table", [("s1_", T3), ("s2_", T3), ("w_", T3), ("r_", T16)])
+def test_step_matches_reference_golden(native, gpu_ctx, prefix, table):
+    name = "step_16couples.npz" if table == T16 else "step_3couples.npz"
+    g = load_golden(name)
+    seed = int(g["seed"][0]) + {"s1_": 0, "s2_": 1, "w_": 2, "r_": 0}[prefix]
+    nu = int(g["nu"][0])
+    st = golden_state(g, prefix, "in")
+    out, res, _ = gpu_step(native, gpu_ctx(table), st, seed, nu)
+    rep, ok = compare_steps(golden_state(g, prefix, "out"), golden_res(g, prefix), out, res)
+    print(prefix, rep)
+    assert ok, rep
+
+
+@pytest.mark.parametrize("table,nc", [(T3, 3), (T16, 16)])
+def test_step_matches_port_200k(native, gpu_ctx, port, table, nc):
+    st = W.mixed_batch(200000, n_couples=nc, seed=123)
+    p = port(table)
+    u = p.fill_uniforms(st["id"], 64, 4242)
+    ref_out, ref_res = p.step_mt(st, u, 64, 4242, threads=8)
+    out, res, cnt = gpu_step(native, gpu_ctx(table), st, 4242, 64)
+    rep, ok = compare_steps(ref_out, ref_res, out, res)
+    print(rep)
+    assert ok, rep
+    # counters agree with the per-track outputs
+    assert cnt[0] == len(st["ekin"])
+    assert cnt[1] == int(out["rng_cursor"].sum())
+    assert cnt[3] == int(res["n_sec"].astype(np.int64).sum())
+
+
+def test_step_wide_energy_range_matches_port(native, gpu_ctx, port):
+    """1 keV - 100 TeV: LPM brem/pair, RB brem, tracking cuts, at-rest annihilation."""
+    st = W.mixed_batch(100000, seed=5, emin=1e-3, emax=1e8, frac=(0.4, 0.3, 0.3))
+    rng = np.random.default_rng(8)
+    st["on_boundary"] = (rng.random(len(st["ekin"])) < 0.2).astype(np.uint8)
+    p = port(T3)
+    u = p.fill_uniforms(st["id"], 24, 11)
+    ref_out, ref_res = p.step_mt(st, u, 24, 11, threads=8)
+    out, res, _ = gpu_step(native, gpu_ctx(T3), st, 11, 24)
+    rep, ok = compare_steps(ref_out, ref_res, out, res)
+    print(rep)
+    assert ok, rep
+    assert np.any(res["flags"] & 1), "expected some tracks to read past 24 buffered uniforms"
+
+
+def test_in_place_equals_out_of_place(native, gpu_ctx):
+    st = W.mixed_batch(50000, seed=6)
+    a = gpu_step(native, gpu_ctx(T3), st, 3, 64)
+    b = gpu_step(native, gpu_ctx(T3), st, 3, 64, in_place=True)
+    for k in a[0]:
+        assert np.array_equal(a[0][k], b[0][k], equal_nan=True), k
+    for k in a[1]:
+        assert np.array_equal(a[1][k], b[1][k], equal_nan=True), k
+
+
+def test_host_entry_point_equals_device_entry_point(native, gpu_ctx):
+    st = W.mixed_batch(30000, seed=9)
+    out_d, res_d, _ = gpu_step(native, gpu_ctx(T3), st, 21, 64)
+    u = W.philox_uniforms(21, st["id"], 64).reshape(-1)
+    out_h = {k: np.empty_like(v) for k, v in st.items()}
+    res_h = native.alloc_out_numpy(len(st["ekin"]))
+    cnt = gpu_ctx(T3).step_host(st, out_h, u, 64, 21, res_h)
+    for k in native.STATE_OUT_FIELDS:
+        assert np.array_equal(out_d[k], out_h[k], equal_nan=True), k
+    for k in res_d:
+        assert np.array_equal(res_d[k], res_h[k], equal_nan=True), k
+    assert cnt.steps == len(st["ekin"])
+
+
+def test_device_uniform_fill_matches_contract(native):
+    torch = _torch()
+    ids = torch.arange(0, 1000, dtype=torch.int32, device="cuda") * 7919
+    u = native.fill_uniforms(ids, 37, 0xABCDEF).cpu().numpy().reshape(1000, 37)
+    want = W.philox_uniforms(0xABCDEF, ids.cpu().numpy(), 37)
+    assert np.array_equal(u, want)
+
+
+def test_bad_track_inputs_are_flagged_not_faulted(native, gpu_ctx):
+    st = W.mixed_batch(64, seed=1)
+    st["imc"][3] = 99
+    st["imc"][4] = -1
+    st["ekin"][5] = -2.0
+    st["ekin"][6] = np.nan
+    st["type"][7] = 5
+    out, res, _ = gpu_step(native, gpu_ctx(T3), st, 1, 64)
+    for i in (3, 4, 5, 6, 7):
+        assert res["flags"][i] & 4
+    ok = np.ones(64, bool)
+    ok[[3, 4, 5, 6, 7]] = False
+    assert not np.any(res["flags"][ok] & 4)
+
+
+# ---- full-size properties (BASELINE configuration 2: 4M mixed tracks) --------------------
+@pytest.fixture(scope="module")
+def full_batch(native, gpu_ctx):
+    n = 1 << 22
+    st = W.mixed_batch(n, seed=2026)
+    out, res, cnt = gpu_step(native, gpu_ctx(T3), st, 777, 64)
+    return st, out, res, cnt
+
+
+def test_full_size_energy_conservation(full_batch):
+    st, out, res, _ = full_batch
+    bal = energy_balance(st, out, res)
+    assert np.all(np.abs(bal) <= 1e-9 * np.maximum(st["ekin"], 1.0)), float(np.abs(bal).max())
+
+
+def test_full_size_unit_directions_and_sane_outputs(full_batch):
+    st, out, res, _ = full_batch
+    alive = out["ekin"] > 0
+    nrm = np.sqrt(out["dir_x"] ** 2 + out["dir_y"] ** 2 + out["dir_z"] ** 2)
+    assert np.all(np.abs(nrm[alive] - 1.0) < 1e-12)
+    n = len(st["ekin"])
+    ns = res["n_sec"].astype(int)
+    valid = (np.arange(2)[None, :] < ns[:, None]).reshape(-1)
+    snrm = np.sqrt(res["sec_dir_x"] ** 2 + res["sec_dir_y"] ** 2 + res["sec_dir_z"] ** 2)[valid]
+    assert np.all(np.abs(snrm - 1.0) < 1e-12)
+    assert np.all(res["sec_ekin"][valid] >= 0)
+    assert np.all(res["gstep"] <= res["pstep"] + 1e-12 * np.abs(res["pstep"]))
+    assert not np.any(res["flags"] & (2 | 4 | 8))
+    assert n == len(ns)
+
+
+def test_full_size_deterministic_and_order_independent(native, gpu_ctx, full_batch):
+    st, out, res, _ = full_batch
+    perm = np.random.default_rng(0).permutation(len(st["ekin"]))[: 1 << 20]
+    sub = {k: np.ascontiguousarray(v[perm]) for k, v in st.items()}
+    o2, r2, _ = gpu_step(native, gpu_ctx(T3), sub, 777, 64)
+    for k in ("ekin", "dir_x", "nia0", "rng_cursor", "gauss_value"):
+        assert np.array_equal(o2[k], out[k][perm], equal_nan=True), k
+    for k in ("edep", "gstep", "pstep", "winner", "n_sec"):
+        assert np.array_equal(r2[k], res[k][perm]), k
+
+
+def test_full_size_sample_matches_port(port, full_batch):
+    st, out, res, _ = full_batch
+    idx = np.random.default_rng(1).choice(len(st["ekin"]), 65536, replace=False)
+    sub = {k: np.ascontiguousarray(v[idx]) for k, v in st.items()}
+    p = port(T3)
+    u = p.fill_uniforms(sub["id"], 64, 777)
+    ref_out, ref_res = p.step_mt(sub, u, 64, 777, threads=8)
+    got_out = {k: v[idx] for k, v in out.items()}
+    got_res = {k: (v.reshape(-1, 2)[idx].reshape(-1) if len(v) == 2 * len(st["ekin"]) else v[idx])
+               for k, v in res.items()}
+    rep, ok = compare_steps(ref_out, ref_res, got_out, got_res)
+    assert ok, rep
