@@ -38,6 +38,7 @@ N_TRACKS = 4194304
 NU = 64
 SEED = 20261203
 WORKLOAD_SEED = 7
+LAUNCHES_PER_STEP = 12  # classify, 2 stage-A kernels, 9 interaction kernels (plus one memset)
 METRIC = "mixed e±/γ physics steps/s (1 GB300) vs plain FP64 path; p50/p99 batch latency"
 UNIT = "steps/s"
 CONFIG = {"workload": "plain FP64 full step, 4,194,304 mixed tracks (45% gamma, 45% e-, 10% e+), "
@@ -231,32 +232,39 @@ def main():
 
     # warm-up (and one counted step for the algorithmic byte count)
     for i in range(max(args.warmup, 3)):
-        ctx.step(sin, sout, u, NU, SEED, res, counters=cnt if i == 0 else None)
+        ctx.step(sin, sout, u, NU, SEED, res, counters=cnt if i == 0 else None, form="batched")
     torch.cuda.synchronize()
     c = cnt.cpu().numpy()
     uniforms_consumed, secondaries = int(c[1]), int(c[3])
 
+    def timed(form, steps):
+        """K steps of one form between barriers; max over ranks; ms per step."""
+        for _ in range(args.warmup):
+            ctx.step(sin, sout, u, NU, SEED, res, form=form)
+        barrier()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(steps):
+            ctx.step(sin, sout, u, NU, SEED, res, form=form)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        t = ev0.elapsed_time(ev1)
+        if ws > 1:
+            tt = torch.tensor([t], device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            t = float(tt.item())
+        return t / steps
+
+    # the plain form (one thread per track), the denominator of the batched form
+    ms_plain = timed("plain", max(3, args.steps // 3))
     clocks = Clocks(lrank)
-    barrier()
-    torch.cuda.synchronize()
     clocks.start()
     time.sleep(0.3)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    for _ in range(args.steps):
-        ctx.step(sin, sout, u, NU, SEED, res)
-    ev1.record(stream)
-    torch.cuda.synchronize()
+    ms_step = timed("batched", args.steps)
     clk = clocks.stop()
-    barrier()
-    t_ms = ev0.elapsed_time(ev1)
-    t_max = t_ms
-    if ws > 1:
-        tt = torch.tensor([t_ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(tt.item())
-    ms_step = t_max / args.steps
-    value = ws * n * args.steps / (t_max / 1e3)
+    value = ws * n / (ms_step / 1e3)
 
     # e2e through the host-buffer entry point
     e2e = None
@@ -326,7 +334,11 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": CONFIG, "e2e": e2e,
-            "gpu_launches": args.steps, "roofline": roof, "fp64": fp64, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": LAUNCHES_PER_STEP * args.steps,
+            "form": "batched FP64 (hepem_step_batched): bit-identical to the plain FP64 path",
+            "plain_fp64": {"value": ws * n / (ms_plain / 1e3), "unit": UNIT, "ms_per_step": ms_plain,
+                           "entry_point": "hepem_step"},
+            "vs_plain_fp64": ms_plain / ms_step, "roofline": roof, "fp64": fp64, "cpu_baseline": cpu, "clocks": clk,
             "counters": {"uniforms_per_step": uniforms_consumed, "secondaries_per_step": secondaries,
                          "interactions": [int(x) for x in c[4:12]]}}
     print(json.dumps(line), flush=True)

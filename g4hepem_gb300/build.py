@@ -22,6 +22,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 # (source, extra nvcc flags)
 UNITS = [
     ("kernels_fp64.cu", ["-fmad=false"]),
+    ("kernels_batched.cu", ["-fmad=false"]),
     ("api.cu", ["-fmad=false"]),
     ("state_json.cpp", []),
 ]

@@ -162,6 +162,25 @@ int hepem_step(const hepem_ctx* c, int64_t n, const hepem_track_state* in, hepem
   return HEPEM_OK;
 }
 
+int hepem_step_batched(const hepem_ctx* c, int64_t n, const hepem_track_state* in, hepem_track_state* out,
+                       const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res,
+                       hepem_step_counters* counters, void* stream) {
+  if (!c || n < 0 || nu < 0) return fail(HEPEM_BAD_ARG, "bad context or size");
+  if (n == 0) return HEPEM_OK;
+  if (!state_ok(in) || !state_ok(out) || !out_ok(res) || (nu > 0 && !uniforms))
+    return fail(HEPEM_BAD_ARG, "null array in track batch");
+  if (n > (int64_t)INT32_MAX) return fail(HEPEM_BAD_ARG, "batch too large");
+  cudaStream_t s = (cudaStream_t)stream;
+  void* ws = nullptr;
+  HEPEM_CUDA(cudaMallocAsync(&ws, hepem::batched_workspace_bytes(n), s));
+  cudaError_t e = hepem::launch_step_batched(c->tables, n, *in, *out, uniforms, nu, seed, *res, counters, ws, s,
+                                             c->sms);
+  cudaError_t f = cudaFreeAsync(ws, s);
+  if (e != cudaSuccess) return cuda_fail(e, "batched step launch");
+  if (f != cudaSuccess) return cuda_fail(f, "cudaFreeAsync");
+  return HEPEM_OK;
+}
+
 int hepem_step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem_track_state* out,
                     const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res,
                     hepem_step_counters* counters, void* stream) {
@@ -178,6 +197,7 @@ int hepem_step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in,
   for (size_t b : kStateSizes) need += al(b * n);
   for (size_t b : kOutSizes) need += al(b * n);
   need += al(sizeof(double) * (size_t)n * nu) + al(sizeof(hepem_step_counters));
+  need += al(hepem::batched_workspace_bytes(n));
   if (need > c->stageBytes) {
     if (c->stage) HEPEM_CUDA(cudaFree(c->stage));
     c->stage = nullptr;
@@ -193,6 +213,8 @@ int hepem_step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in,
   double* du = (double*)p;
   p += al(sizeof(double) * (size_t)n * nu);
   hepem_step_counters* dcnt = (hepem_step_counters*)p;
+  p += al(sizeof(hepem_step_counters));
+  void* dwork = p;
   hepem_track_state ds;
   hepem_step_out dr;
   static_assert(sizeof(hepem_track_state) == 20 * sizeof(void*), "state struct layout");
@@ -205,7 +227,8 @@ int hepem_step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in,
   for (int k = 0; k < 20; ++k) HEPEM_CUDA(cudaMemcpyAsync(dstate[k], hin[k], kStateSizes[k] * n, cudaMemcpyHostToDevice, s));
   if (nu > 0) HEPEM_CUDA(cudaMemcpyAsync(du, uniforms, sizeof(double) * (size_t)n * nu, cudaMemcpyHostToDevice, s));
   if (counters) HEPEM_CUDA(cudaMemsetAsync(dcnt, 0, sizeof(*dcnt), s));
-  HEPEM_CUDA(hepem::launch_step(c->tables, n, ds, ds, du, nu, seed, dr, counters ? dcnt : nullptr, s, c->sms));
+  HEPEM_CUDA(hepem::launch_step_batched(c->tables, n, ds, ds, du, nu, seed, dr, counters ? dcnt : nullptr,
+                                        dwork, s, c->sms));
   // the persistent per-track fields come back (type/imc/id/safety/boundary are inputs only)
   for (int k = 3; k < 20; ++k) {
     if (k == 11 || k == 12) continue;

@@ -24,6 +24,12 @@
 
 namespace hepem {
 
+// interaction queues of the batched form
+enum : int {
+  kQIoniEm = 0, kQIoniEp, kQBremSB, kQBremRB, kQAnnihFlight, kQAnnihRest, kQConversion, kQCompton,
+  kQPhotoelectric, kNumQueues
+};
+
 constexpr uint8_t kFlagRngOverflow = 1u;
 constexpr uint8_t kFlagLoopCap = 2u;
 constexpr uint8_t kFlagBadInput = 4u;
@@ -687,6 +693,58 @@ struct Physics {
       if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
     } while (el < 0. || el > twom);
     return el;
+  }
+
+  // Perform split at the discrete interaction: continuous part, the
+  // delta-interaction test, and the choice of the interaction to sample
+  // (G4HepEmElectronManager.icc:425-483).  Returns the queue of the pending
+  // interaction, or -1.
+  __device__ int el_perform_until_discrete() {
+    t.edep = 0;
+    t.pstep = t.gstep;
+    if (t.gstep <= 0.) return -1;
+    if (el_continuous()) return t.isEl ? -1 : kQAnnihRest;
+    const int ip = t.winner;
+    if (ip < 0 || t.onBoundary) return -1;
+    t.nia[ip] = -1.0;
+    const DevElData& d = eld();
+    const DevCouple c = couple();
+    const double e = t.e, le = t.logE();
+    const double mx = ip < 2 ? rest_macxs(d, t.imc, e, le, ip == 0)
+                     : (ip < 3 ? annih_macxs(e, ld(&T.mats[c.mat].elDensity)) : nuc_macxs(d, c.mat, e, le));
+    const double u = rng.flat();
+    if (mx <= 0.0 || u > mx * t.mfp[ip]) return -1;
+    switch (ip) {
+      case 0: return t.isEl ? kQIoniEm : kQIoniEp;
+      case 1: return e < T.bremModelLim ? kQBremSB : kQBremRB;
+      case 2: return kQAnnihFlight;
+      default: return -1;
+    }
+  }
+
+  // Gamma Perform up to the interaction (G4HepEmGammaManager.icc:54-81);
+  // returns the queue of the pending interaction or -1 (the tracking cut of
+  // :97-104 is then applied by the caller when no interaction is pending).
+  __device__ int gamma_perform_until_interaction() {
+    t.nia[0] -= t.gstep / t.mfp[0];
+    t.edep = 0.0;
+    if (t.onBoundary) return -1;
+    const int ip = t.winner;
+    if (ip >= 0 && ip < 4) t.nia[ip] = -1.0;
+    switch (ip) {
+      case 0: return kQConversion;
+      case 1: return kQCompton;
+      case 2: return kQPhotoelectric;
+      default: return -2;  // no interaction, tracking cut still applies
+    }
+  }
+
+  __device__ void gamma_tracking_cut() {
+    const double fe = t.e;
+    if (fe > 0.0 && fe <= T.gammaTrackingCut) {
+      t.setE(0.0);
+      t.edep += fe;
+    }
   }
 
   // G4HepEmElectronManager.icc:408-459

@@ -48,7 +48,7 @@ class StepCounters(C.Structure):
 
 
 EXPORTED = ["hepem_create", "hepem_create_from_file", "hepem_destroy", "hepem_info", "hepem_status_string",
-            "hepem_last_error", "hepem_electron_lookup", "hepem_step", "hepem_step_host", "hepem_philox_uniform",
+            "hepem_last_error", "hepem_electron_lookup", "hepem_step", "hepem_step_batched", "hepem_step_host", "hepem_philox_uniform",
             "hepem_fill_uniforms"]
 
 
@@ -79,6 +79,7 @@ def lib():
         L.hepem_step.argtypes = [_vp, C.c_int64, C.POINTER(TrackState), C.POINTER(TrackState), _vp, C.c_int32,
                                  C.c_uint64, C.POINTER(StepOut), _vp, _vp]
         L.hepem_step_host.argtypes = L.hepem_step.argtypes
+        L.hepem_step_batched.argtypes = L.hepem_step.argtypes
         L.hepem_philox_uniform.argtypes = [C.c_uint64, C.c_int32, C.c_int32]
         L.hepem_philox_uniform.restype = C.c_double
         L.hepem_fill_uniforms.argtypes = [C.c_int64, _vp, C.c_int32, C.c_uint64, _vp, _vp]
@@ -162,12 +163,13 @@ class Context:
         return out
 
     def step(self, state_in: dict, state_out: dict, uniforms, n_uniform: int, seed: int, res: dict,
-             counters=None, stream=None):
+             counters=None, stream=None, form="plain"):
+        """One step of every track; form: "plain" (hepem_step) or "batched" (hepem_step_batched)."""
         n = state_in["ekin"].numel()
         sin, sout, sres = make_state_struct(state_in), make_state_struct(state_out), make_out_struct(res)
-        check(lib().hepem_step(self.h, n, C.byref(sin), C.byref(sout), _ptr(uniforms), n_uniform, seed,
-                               C.byref(sres), _ptr(counters) if counters is not None else None,
-                               _stream_ptr(stream)))
+        fn = {"plain": lib().hepem_step, "batched": lib().hepem_step_batched}[form]
+        check(fn(self.h, n, C.byref(sin), C.byref(sout), _ptr(uniforms), n_uniform, seed, C.byref(sres),
+                 _ptr(counters) if counters is not None else None, _stream_ptr(stream)))
 
     # -- host-buffer entry point (numpy arrays) ----------------------------------
     def step_host(self, state_in: dict, state_out: dict, uniforms: np.ndarray, n_uniform: int, seed: int,

@@ -152,8 +152,22 @@ int  hepem_step(const hepem_ctx* ctx, int64_t n, const hepem_track_state* in,
                 uint64_t seed, hepem_step_out* res, hepem_step_counters* counters,
                 void* stream);
 
-/* Same with HOST buffers: copies the batch in, steps it, copies the results
- * back and synchronises.  Pinned host memory is fastest. */
+/* Batched form of hepem_step: same arguments, same results bit for bit.
+ * Tracks are sorted into per-particle lists and, after the continuous part of
+ * the step, into per-interaction queues, so that every warp executes one
+ * model at a time (no reference counterpart: a scheduling of the same
+ * G4HepEmElectronManager / G4HepEmGammaManager calls).  Uses a stream-ordered
+ * workspace of about 48 bytes per track (cudaMallocAsync on `stream`). */
+int  hepem_step_batched(const hepem_ctx* ctx, int64_t n, const hepem_track_state* in,
+                        hepem_track_state* out, const double* uniforms, int32_t n_uniform,
+                        uint64_t seed, hepem_step_out* res, hepem_step_counters* counters,
+                        void* stream);
+
+/* Same with HOST buffers: copies the batch in, steps it (batched form),
+ * copies the results back and synchronises.  Pinned host memory is fastest.
+ * Reference counterpart: the per-track G4HepEmElectronManager::HowFar/Perform
+ * and G4HepEmGammaManager::HowFar/SelectInteraction/Perform calls of
+ * apps/examples/TestEm3/src/G4HepEmProcess.cc:144-197 over a host batch. */
 int  hepem_step_host(const hepem_ctx* ctx, int64_t n, const hepem_track_state* in,
                      hepem_track_state* out, const double* uniforms,
                      int32_t n_uniform, uint64_t seed, hepem_step_out* res,
