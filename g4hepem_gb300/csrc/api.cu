@@ -1,6 +1,7 @@
 // api.cu -- the extern "C" boundary declared in include/g4hepem_gb300.h.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -18,10 +19,22 @@ struct hepem_ctx {
   void* arena = nullptr;
   size_t arenaBytes = 0;
   hepem::DevTables tables;
-  // staging area of hepem_step_host (grow-only, serialised by mu)
+  // copy/compute pipeline of hepem_step_host (grow-only buffers, serialised by mu)
+  static constexpr int kSlots = 3;
+  struct Slot {
+    cudaStream_t s = nullptr;
+    cudaEvent_t done = nullptr;
+    void* buf = nullptr;
+    size_t bytes = 0;
+  };
   std::mutex mu;
-  void* stage = nullptr;
-  size_t stageBytes = 0;
+  Slot slot[kSlots];
+  cudaEvent_t start = nullptr;
+  bool slotsReady = false;
+  // per-stage timing of the batched form (hepem_profile_stages)
+  bool profile = false;
+  bool stageEvReady = false;
+  cudaEvent_t stageEv[hepem::kNumStageEvents] = {};
 };
 
 namespace {
@@ -125,7 +138,15 @@ int hepem_destroy(hepem_ctx* c) {
   if (!c) return HEPEM_OK;
   cudaError_t e = cudaSuccess;
   if (c->arena) e = cudaFree(c->arena);
-  if (c->stage) cudaFree(c->stage);
+  for (auto& sl : c->slot) {
+    if (sl.s) cudaStreamSynchronize(sl.s);
+    if (sl.buf) cudaFree(sl.buf);
+    if (sl.done) cudaEventDestroy(sl.done);
+    if (sl.s) cudaStreamDestroy(sl.s);
+  }
+  if (c->start) cudaEventDestroy(c->start);
+  if (c->stageEvReady)
+    for (auto& e2 : c->stageEv) cudaEventDestroy(e2);
   delete c;
   return e == cudaSuccess ? HEPEM_OK : cuda_fail(e, "cudaFree");
 }
@@ -174,7 +195,7 @@ int hepem_step_batched(const hepem_ctx* c, int64_t n, const hepem_track_state* i
   void* ws = nullptr;
   HEPEM_CUDA(cudaMallocAsync(&ws, hepem::batched_workspace_bytes(n), s));
   cudaError_t e = hepem::launch_step_batched(c->tables, n, *in, *out, uniforms, nu, seed, *res, counters, ws, s,
-                                             c->sms);
+                                             c->sms, c->profile ? const_cast<cudaEvent_t*>(c->stageEv) : nullptr);
   cudaError_t f = cudaFreeAsync(ws, s);
   if (e != cudaSuccess) return cuda_fail(e, "batched step launch");
   if (f != cudaSuccess) return cuda_fail(f, "cudaFreeAsync");
@@ -189,57 +210,129 @@ int hepem_step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in,
   if (n == 0) return HEPEM_OK;
   if (!state_ok(in) || !state_ok(out) || !out_ok(res) || (nu > 0 && !uniforms))
     return fail(HEPEM_BAD_ARG, "null array in track batch");
+  if (n > (int64_t)INT32_MAX) return fail(HEPEM_BAD_ARG, "batch too large");
   std::lock_guard<std::mutex> lock(c->mu);
   cudaStream_t s = (cudaStream_t)stream;
-  // device staging: 20 state arrays, 14 result arrays, uniforms, counters
-  size_t need = 0;
+  // The batch is cut into chunks that cycle over kSlots streams, each with its
+  // own device buffers: the copy-in of one chunk, the step of the previous one
+  // and the copy-out of the one before overlap.
+  const int64_t m = std::min<int64_t>(n, std::max<int64_t>(1 << 16, ((n + 7) / 8 + 255) / 256 * 256));
+  const int nChunks = (int)((n + m - 1) / m);
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-  for (size_t b : kStateSizes) need += al(b * n);
-  for (size_t b : kOutSizes) need += al(b * n);
-  need += al(sizeof(double) * (size_t)n * nu) + al(sizeof(hepem_step_counters));
-  need += al(hepem::batched_workspace_bytes(n));
-  if (need > c->stageBytes) {
-    if (c->stage) HEPEM_CUDA(cudaFree(c->stage));
-    c->stage = nullptr;
-    c->stageBytes = 0;
-    HEPEM_CUDA(cudaMalloc(&c->stage, need));
-    c->stageBytes = need;
+  size_t need = 0;
+  for (size_t b : kStateSizes) need += al(b * m);
+  for (size_t b : kOutSizes) need += al(b * m);
+  need += al(sizeof(double) * (size_t)m * nu) + al(sizeof(hepem_step_counters)) + al(hepem::batched_workspace_bytes(m));
+  if (!c->slotsReady) {
+    for (int k = 0; k < hepem_ctx::kSlots; ++k) {
+      HEPEM_CUDA(cudaStreamCreateWithFlags(&c->slot[k].s, cudaStreamNonBlocking));
+      HEPEM_CUDA(cudaEventCreateWithFlags(&c->slot[k].done, cudaEventDisableTiming));
+    }
+    HEPEM_CUDA(cudaEventCreateWithFlags(&c->start, cudaEventDisableTiming));
+    c->slotsReady = true;
   }
-  uint8_t* p = (uint8_t*)c->stage;
-  void* dstate[20];
-  void* dout[14];
-  for (int k = 0; k < 20; ++k) { dstate[k] = p; p += al(kStateSizes[k] * n); }
-  for (int k = 0; k < 14; ++k) { dout[k] = p; p += al(kOutSizes[k] * n); }
-  double* du = (double*)p;
-  p += al(sizeof(double) * (size_t)n * nu);
-  hepem_step_counters* dcnt = (hepem_step_counters*)p;
-  p += al(sizeof(hepem_step_counters));
-  void* dwork = p;
-  hepem_track_state ds;
-  hepem_step_out dr;
-  static_assert(sizeof(hepem_track_state) == 20 * sizeof(void*), "state struct layout");
-  static_assert(sizeof(hepem_step_out) == 14 * sizeof(void*), "out struct layout");
-  memcpy(&ds, dstate, sizeof(ds));
-  memcpy(&dr, dout, sizeof(dr));
+  HEPEM_CUDA(cudaEventRecord(c->start, s));
+  for (int k = 0; k < hepem_ctx::kSlots; ++k) {
+    hepem_ctx::Slot& sl = c->slot[k];
+    if (need > sl.bytes) {
+      HEPEM_CUDA(cudaStreamSynchronize(sl.s));
+      if (sl.buf) HEPEM_CUDA(cudaFree(sl.buf));
+      sl.buf = nullptr;
+      sl.bytes = 0;
+      HEPEM_CUDA(cudaMalloc(&sl.buf, need));
+      sl.bytes = need;
+    }
+    HEPEM_CUDA(cudaStreamWaitEvent(sl.s, c->start, 0));
+  }
   void* const* hin = reinterpret_cast<void* const*>(in);
   void* const* hout = reinterpret_cast<void* const*>(out);
   void* const* hres = reinterpret_cast<void* const*>(res);
-  for (int k = 0; k < 20; ++k) HEPEM_CUDA(cudaMemcpyAsync(dstate[k], hin[k], kStateSizes[k] * n, cudaMemcpyHostToDevice, s));
-  if (nu > 0) HEPEM_CUDA(cudaMemcpyAsync(du, uniforms, sizeof(double) * (size_t)n * nu, cudaMemcpyHostToDevice, s));
-  if (counters) HEPEM_CUDA(cudaMemsetAsync(dcnt, 0, sizeof(*dcnt), s));
-  HEPEM_CUDA(hepem::launch_step_batched(c->tables, n, ds, ds, du, nu, seed, dr, counters ? dcnt : nullptr,
-                                        dwork, s, c->sms));
-  // the persistent per-track fields come back (type/imc/id/safety/boundary are inputs only)
-  for (int k = 3; k < 20; ++k) {
-    if (k == 11 || k == 12) continue;
-    HEPEM_CUDA(cudaMemcpyAsync(hout[k], dstate[k], kStateSizes[k] * n, cudaMemcpyDeviceToHost, s));
+  static_assert(sizeof(hepem_track_state) == 20 * sizeof(void*), "state struct layout");
+  static_assert(sizeof(hepem_step_out) == 14 * sizeof(void*), "out struct layout");
+  hepem_step_counters* dcnt[hepem_ctx::kSlots] = {};
+  for (int ch = 0; ch < nChunks; ++ch) {
+    const int64_t off = (int64_t)ch * m;
+    const int64_t mc = std::min<int64_t>(m, n - off);
+    hepem_ctx::Slot& sl = c->slot[ch % hepem_ctx::kSlots];
+    const cudaStream_t ss = sl.s;
+    uint8_t* p = (uint8_t*)sl.buf;
+    void* dstate[20];
+    void* dout[14];
+    for (int k = 0; k < 20; ++k) { dstate[k] = p; p += al(kStateSizes[k] * m); }
+    for (int k = 0; k < 14; ++k) { dout[k] = p; p += al(kOutSizes[k] * m); }
+    double* du = (double*)p;
+    p += al(sizeof(double) * (size_t)m * nu);
+    hepem_step_counters* cnt = (hepem_step_counters*)p;
+    p += al(sizeof(hepem_step_counters));
+    void* dwork = p;
+    if (counters && ch < hepem_ctx::kSlots) {
+      HEPEM_CUDA(cudaMemsetAsync(cnt, 0, sizeof(*cnt), ss));
+      dcnt[ch] = cnt;
+    }
+    hepem_track_state ds;
+    hepem_step_out dr;
+    memcpy(&ds, dstate, sizeof(ds));
+    memcpy(&dr, dout, sizeof(dr));
+    for (int k = 0; k < 20; ++k)
+      HEPEM_CUDA(cudaMemcpyAsync(dstate[k], (const uint8_t*)hin[k] + kStateSizes[k] * off, kStateSizes[k] * mc,
+                                 cudaMemcpyHostToDevice, ss));
+    if (nu > 0)
+      HEPEM_CUDA(cudaMemcpyAsync(du, uniforms + off * nu, sizeof(double) * (size_t)mc * nu, cudaMemcpyHostToDevice, ss));
+    HEPEM_CUDA(hepem::launch_step_batched(c->tables, mc, ds, ds, du, nu, seed, dr, counters ? cnt : nullptr, dwork,
+                                          ss, c->sms, nullptr));
+    // persistent per-track fields come back (type/imc/id/safety/boundary are inputs only)
+    for (int k = 3; k < 20; ++k) {
+      if (k == 11 || k == 12) continue;
+      HEPEM_CUDA(cudaMemcpyAsync((uint8_t*)hout[k] + kStateSizes[k] * off, dstate[k], kStateSizes[k] * mc,
+                                 cudaMemcpyDeviceToHost, ss));
+    }
+    for (int k = 0; k < 14; ++k)
+      HEPEM_CUDA(cudaMemcpyAsync((uint8_t*)hres[k] + kOutSizes[k] * off, dout[k], kOutSizes[k] * mc,
+                                 cudaMemcpyDeviceToHost, ss));
   }
   if (hout[0] != hin[0]) {
     for (int k : {0, 1, 2, 11, 12}) memcpy(hout[k], hin[k], kStateSizes[k] * n);
   }
-  for (int k = 0; k < 14; ++k) HEPEM_CUDA(cudaMemcpyAsync(hres[k], dout[k], kOutSizes[k] * n, cudaMemcpyDeviceToHost, s));
-  if (counters) HEPEM_CUDA(cudaMemcpyAsync(counters, dcnt, sizeof(*dcnt), cudaMemcpyDeviceToHost, s));
+  hepem_step_counters hc[hepem_ctx::kSlots];
+  for (int k = 0; k < hepem_ctx::kSlots; ++k) {
+    if (dcnt[k]) HEPEM_CUDA(cudaMemcpyAsync(&hc[k], dcnt[k], sizeof(hc[k]), cudaMemcpyDeviceToHost, c->slot[k].s));
+    HEPEM_CUDA(cudaEventRecord(c->slot[k].done, c->slot[k].s));
+    HEPEM_CUDA(cudaStreamWaitEvent(s, c->slot[k].done, 0));
+  }
   HEPEM_CUDA(cudaStreamSynchronize(s));
+  if (counters) {
+    memset(counters, 0, sizeof(*counters));
+    for (int k = 0; k < hepem_ctx::kSlots; ++k) {
+      if (!dcnt[k]) continue;
+      const uint64_t* a = reinterpret_cast<const uint64_t*>(&hc[k]);
+      uint64_t* b = reinterpret_cast<uint64_t*>(counters);
+      for (size_t j = 0; j < sizeof(hepem_step_counters) / 8; ++j) b[j] += a[j];
+    }
+  }
+  return HEPEM_OK;
+}
+
+int hepem_profile_stages(hepem_ctx* c, int enable) {
+  if (!c) return fail(HEPEM_BAD_ARG, "null context");
+  if (enable && !c->stageEvReady) {
+    for (int k = 0; k < hepem::kNumStageEvents; ++k) HEPEM_CUDA(cudaEventCreate(&c->stageEv[k]));
+    c->stageEvReady = true;
+  }
+  c->profile = enable != 0;
+  return HEPEM_OK;
+}
+
+int hepem_stage_times(hepem_ctx* c, float* ms, const char** names, int32_t max, int32_t* count) {
+  if (!c || !ms || max < 0) return fail(HEPEM_BAD_ARG, "bad argument");
+  if (!c->stageEvReady) return fail(HEPEM_BAD_ARG, "stage profiling was never enabled");
+  const int ns = hepem::kNumStageEvents - 1;
+  HEPEM_CUDA(cudaEventSynchronize(c->stageEv[ns]));
+  const int k = max < ns ? max : ns;
+  for (int i = 0; i < k; ++i) {
+    HEPEM_CUDA(cudaEventElapsedTime(&ms[i], c->stageEv[i], c->stageEv[i + 1]));
+    if (names) names[i] = hepem::stage_name(i);
+  }
+  if (count) *count = k;
   return HEPEM_OK;
 }
 

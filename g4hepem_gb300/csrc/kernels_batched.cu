@@ -34,6 +34,13 @@ struct Work {
   double* peXS;                   // parallel to queue[kQPhotoelectric]
 };
 
+const char* stage_name(int i) {
+  static const char* names[kNumStageEvents - 1] = {
+      "classify", "stage_a_charged", "stage_a_gamma", "ioni_e-", "ioni_e+", "brem_sb", "brem_rb",
+      "annihilation_in_flight", "annihilation_at_rest", "conversion", "compton", "photoelectric"};
+  return (i >= 0 && i < kNumStageEvents - 1) ? names[i] : "";
+}
+
 size_t batched_workspace_bytes(int64_t n) {
   const size_t al = 256;
   auto r = [&](size_t b) { return (b + al - 1) / al * al; };
@@ -243,7 +250,7 @@ static int grid_of(K kernel, int sms) {
 cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track_state& in,
                                 const hepem_track_state& out, const double* uniforms, int nu, uint64_t seed,
                                 const hepem_step_out& res, hepem_step_counters* counters, void* workspace,
-                                cudaStream_t s, int sms) {
+                                cudaStream_t s, int sms, cudaEvent_t* ev) {
   if (n <= 0) return cudaSuccess;
   static int gA = 0, gG = 0, gB[kNumQueues] = {};
   if (!gA) {
@@ -262,20 +269,37 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
   const Work w = carve(workspace, n);
   cudaError_t e = cudaMemsetAsync(w.counts, 0, 64 * sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
+  int k = 0;
+  auto mark = [&]() {
+    if (ev) cudaEventRecord(ev[k++], s);
+  };
   const int64_t blocks = (n + 255) / 256;
   const int gC = (int)(blocks < (int64_t)sms * 8 ? blocks : (int64_t)sms * 8);
+  mark();
   classify_kernel<<<gC, 256, 0, s>>>(T, n, in, out, res, w, counters);
+  mark();
   stage_a_charged_kernel<<<gA, 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+  mark();
   stage_a_gamma_kernel<<<gG, 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+  mark();
   stage_b_kernel<0><<<gB[0], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+  mark();
   stage_b_kernel<1><<<gB[1], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+  mark();
   stage_b_kernel<2><<<gB[2], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+  mark();
   stage_b_kernel<3><<<gB[3], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+  mark();
   stage_b_kernel<4><<<gB[4], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+  mark();
   stage_b_kernel<5><<<gB[5], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+  mark();
   stage_b_kernel<6><<<gB[6], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+  mark();
   stage_b_kernel<7><<<gB[7], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+  mark();
   stage_b_kernel<8><<<gB[8], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+  mark();
   return cudaGetLastError();
 }
 

@@ -1334,7 +1334,7 @@ struct Physics {
           const double r0 = rng.flat(), r1 = rng.flat();
           r2 = rng.flat();
           if (cond > r0) {
-            eps = 0.5 - epsRange * pow(r1, 1. / 3.);
+            eps = 0.5 - epsRange * cbrt(r1);  // reference: std::pow(u, 1./3.) of the host libm
             gr = (screen1(df / (eps * (1. - eps))) - FZ) * iF10;
           } else {
             eps = epsMin + epsRange * r1;
@@ -1349,7 +1349,7 @@ struct Physics {
           r2 = rng.flat();
           double xiS, gS, phiS, p1, p2;
           if (cond > r0) {
-            eps = 0.5 - epsRange * pow(r1, 1. / 3.);
+            eps = 0.5 - epsRange * cbrt(r1);  // reference: std::pow(u, 1./3.) of the host libm
             phi12(df / (eps * (1. - eps)), p1, p2);
             lpm_functions(xiS, gS, phiS, E, eps * E, lpmE, z23, il1, il1c, 0.0, -1.0);
             gr = xiS * ((2. * phiS + gS) * p1 - gS * p2 - phiS * FZ) * iF10;

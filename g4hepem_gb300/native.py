@@ -48,8 +48,8 @@ class StepCounters(C.Structure):
 
 
 EXPORTED = ["hepem_create", "hepem_create_from_file", "hepem_destroy", "hepem_info", "hepem_status_string",
-            "hepem_last_error", "hepem_electron_lookup", "hepem_step", "hepem_step_batched", "hepem_step_host", "hepem_philox_uniform",
-            "hepem_fill_uniforms"]
+            "hepem_last_error", "hepem_electron_lookup", "hepem_step", "hepem_step_batched", "hepem_step_host",
+            "hepem_philox_uniform", "hepem_fill_uniforms", "hepem_profile_stages", "hepem_stage_times"]
 
 
 class HepEmError(RuntimeError):
@@ -83,6 +83,9 @@ def lib():
         L.hepem_philox_uniform.argtypes = [C.c_uint64, C.c_int32, C.c_int32]
         L.hepem_philox_uniform.restype = C.c_double
         L.hepem_fill_uniforms.argtypes = [C.c_int64, _vp, C.c_int32, C.c_uint64, _vp, _vp]
+        L.hepem_profile_stages.argtypes = [_vp, C.c_int]
+        L.hepem_stage_times.argtypes = [_vp, C.POINTER(C.c_float), C.POINTER(C.c_char_p), C.c_int32,
+                                        C.POINTER(C.c_int32)]
         _LIB = L
     return _LIB
 

@@ -173,6 +173,16 @@ int  hepem_step_host(const hepem_ctx* ctx, int64_t n, const hepem_track_state* i
                      int32_t n_uniform, uint64_t seed, hepem_step_out* res,
                      hepem_step_counters* counters, void* stream);
 
+/* ---- stage timing (profiling aid; not thread-safe) ------------------------ */
+/* enable != 0: the following hepem_step_batched calls on this context record
+ * CUDA events around each of their stage kernels (no reference counterpart:
+ * the reference has no stage structure).  hepem_stage_times then returns the
+ * milliseconds of each stage of the last such call (it waits for it) and,
+ * if names is not NULL, static stage names. */
+int  hepem_profile_stages(hepem_ctx* ctx, int enable);
+int  hepem_stage_times(hepem_ctx* ctx, float* ms, const char** names, int32_t max,
+                       int32_t* count);
+
 /* ---- RNG stream helpers --------------------------------------------------- */
 /* Philox4x32-10 (Salmon et al., SC'11) uniform in (0,1): counter
  * (k>>1, id, 0, 0x48455045), key (seed lo, seed hi); 52 random bits. */
