@@ -38,7 +38,7 @@ N_TRACKS = 4194304
 NU = 64
 SEED = 20261203
 WORKLOAD_SEED = 7
-LAUNCHES_PER_STEP = 12  # classify, 2 stage-A kernels, 9 interaction kernels (plus one memset)
+LAUNCHES_PER_STEP = 14  # 3 sort kernels, 2 stage-A kernels, 9 interaction kernels (plus two memsets)
 METRIC = "mixed e±/γ physics steps/s (1 GB300) vs plain FP64 path; p50/p99 batch latency"
 UNIT = "steps/s"
 CONFIG = {"workload": "plain FP64 full step, 4,194,304 mixed tracks (45% gamma, 45% e-, 10% e+), "

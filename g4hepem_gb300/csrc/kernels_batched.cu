@@ -6,10 +6,12 @@
 // and different interaction models, and the FP64 pipe -- the scarce resource of
 // GB300 -- executes every branch for the whole warp.  Here the step is
 // re-scheduled so that warps are coherent:
-//   1. classify   : tracks are appended to per-particle lists (warp-aggregated
-//                   atomics); malformed tracks are flagged and finished here;
-//   2. stage A    : e+- lists: HowFar, continuous loss, MSC, fluctuations,
-//                   the delta-interaction test; gamma list: HowFar and the
+//   1. sort       : a counting sort (histogram, scan, warp-aggregated scatter)
+//                   orders the tracks by particle, couple and energy bin, so
+//                   that warps hold similar tracks; malformed tracks are
+//                   flagged and finished here;
+//   2. stage A    : e+- ranges: HowFar, continuous loss, MSC, fluctuations,
+//                   the delta-interaction test; gamma range: HowFar and the
 //                   interaction choice.  Each track that has a discrete
 //                   interaction left is appended to the queue of that model;
 //   3. stage B    : one kernel per interaction queue (Moller, Bhabha,
@@ -27,48 +29,127 @@
 
 namespace hepem {
 
+// Tracks are ordered by a sort key (particle, couple bin, energy bin) with a
+// counting sort, so that the warps of a stage hold tracks of one particle in
+// one material at similar energies and take the same branches.
+constexpr int kSortEBins = 32;      // log2(E) bins over 1 keV - 100 TeV
+constexpr int kSortCoupleBins = 64; // couples beyond 64 share bins (imc % 64)
+constexpr int kMaxSortKeys = 3 * kSortCoupleBins * kSortEBins;
+
 struct Work {
-  uint32_t* counts;               // [0..2] particle lists, [3..3+kNumQueues) queues
-  int32_t* list[3];
+  uint32_t* counts;               // [0..2] e-, e+, gamma tracks, [3..3+kNumQueues) queues
+  uint32_t* hist;                 // [kMaxSortKeys] tracks per sort key
+  uint32_t* cursor;               // [kMaxSortKeys] scatter cursors
+  int32_t* perm;                  // [n] valid tracks in sort-key order
   int32_t* queue[kNumQueues];
   double* peXS;                   // parallel to queue[kQPhotoelectric]
 };
 
 const char* stage_name(int i) {
   static const char* names[kNumStageEvents - 1] = {
-      "classify", "stage_a_charged", "stage_a_gamma", "ioni_e-", "ioni_e+", "brem_sb", "brem_rb",
+      "sort", "stage_a_charged", "stage_a_gamma", "ioni_e-", "ioni_e+", "brem_sb", "brem_rb",
       "annihilation_in_flight", "annihilation_at_rest", "conversion", "compton", "photoelectric"};
   return (i >= 0 && i < kNumStageEvents - 1) ? names[i] : "";
 }
 
+static size_t rnd(size_t b) { return (b + 255) / 256 * 256; }
+
 size_t batched_workspace_bytes(int64_t n) {
-  const size_t al = 256;
-  auto r = [&](size_t b) { return (b + al - 1) / al * al; };
-  return r(64 * sizeof(uint32_t)) + (3 + kNumQueues) * r(sizeof(int32_t) * (size_t)n) + r(sizeof(double) * (size_t)n);
+  return rnd(64 * sizeof(uint32_t)) + 2 * rnd(kMaxSortKeys * sizeof(uint32_t)) +
+         (1 + kNumQueues) * rnd(sizeof(int32_t) * (size_t)n) + rnd(sizeof(double) * (size_t)n);
 }
 
 static Work carve(void* ws, int64_t n) {
-  const size_t al = 256;
-  auto r = [&](size_t b) { return (b + al - 1) / al * al; };
   uint8_t* p = static_cast<uint8_t*>(ws);
   Work w;
   w.counts = reinterpret_cast<uint32_t*>(p);
-  p += r(64 * sizeof(uint32_t));
-  for (int k = 0; k < 3; ++k) { w.list[k] = reinterpret_cast<int32_t*>(p); p += r(sizeof(int32_t) * (size_t)n); }
+  p += rnd(64 * sizeof(uint32_t));
+  w.hist = reinterpret_cast<uint32_t*>(p);
+  p += rnd(kMaxSortKeys * sizeof(uint32_t));
+  w.cursor = reinterpret_cast<uint32_t*>(p);
+  p += rnd(kMaxSortKeys * sizeof(uint32_t));
+  w.perm = reinterpret_cast<int32_t*>(p);
+  p += rnd(sizeof(int32_t) * (size_t)n);
   for (int k = 0; k < kNumQueues; ++k) {
     w.queue[k] = reinterpret_cast<int32_t*>(p);
-    p += r(sizeof(int32_t) * (size_t)n);
+    p += rnd(sizeof(int32_t) * (size_t)n);
   }
   w.peXS = reinterpret_cast<double*>(p);
   return w;
 }
 
-// ---- 1. classify ------------------------------------------------------------------
-__global__ void __launch_bounds__(256) classify_kernel(const __grid_constant__ DevTables T, int64_t n,
-                                                       const hepem_track_state in, const hepem_track_state out,
-                                                       const hepem_step_out res, const Work w,
-                                                       hepem_step_counters* counters) {
+__device__ __forceinline__ int sort_key(int type, int imc, double e, int ncb) {
+  // log2(1 keV / MeV) = -9.9658, log2(100 TeV / 1 keV) = 36.5412
+  int eb = (int)((__log2f((float)e) + 9.965784f) * (kSortEBins / 36.541209f));
+  eb = eb < 0 ? 0 : (eb >= kSortEBins ? kSortEBins - 1 : eb);
+  return ((type * ncb) + (imc % ncb)) * kSortEBins + eb;
+}
+
+// ---- 1. sort: histogram, scan, scatter ----------------------------------------------
+__global__ void __launch_bounds__(256) sort_hist_kernel(const __grid_constant__ DevTables T, int64_t n,
+                                                        const hepem_track_state in, const hepem_track_state out,
+                                                        const hepem_step_out res, const Work w, int ncb,
+                                                        hepem_step_counters* counters) {
+  extern __shared__ uint32_t sh[];
+  const int nkeys = 3 * ncb * kSortEBins;
+  for (int k = threadIdx.x; k < nkeys; k += blockDim.x) sh[k] = 0;
+  __syncthreads();
   StepCount cnt = {};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int type = in.type[i];
+    const int imc = in.imc[i];
+    const double e = in.ekin[i];
+    if (track_input_bad(T, type, imc, e)) {
+      // pass the track through unchanged, flagged
+      Track t;
+      Rng rng;
+      load_track(in, i, t, rng, nullptr, 0, 0, 2);
+      t.flags = kFlagBadInput;
+      store_track(in, out, res, i, t, rng, 2, true);
+      res.n_sec[i] = 0;
+      cnt.steps += 1;
+    } else {
+      atomicAdd(&sh[sort_key(type, imc, e, ncb)], 1u);
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < nkeys; k += blockDim.x)
+    if (sh[k]) atomicAdd(&w.hist[k], sh[k]);
+  add_counters(cnt, counters);
+}
+
+// one block: exclusive scan of the histogram into the scatter cursors, and
+// the number of tracks of each particle type
+__global__ void __launch_bounds__(1024) sort_scan_kernel(const Work w, int ncb) {
+  __shared__ uint32_t partial[1024];
+  const int nkeys = 3 * ncb * kSortEBins;
+  const int per = (nkeys + blockDim.x - 1) / blockDim.x;
+  const int b = threadIdx.x * per;
+  uint32_t s = 0;
+  for (int k = b; k < b + per && k < nkeys; ++k) s += w.hist[k];
+  partial[threadIdx.x] = s;
+  __syncthreads();
+  for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+    const uint32_t v = threadIdx.x >= (unsigned)off ? partial[threadIdx.x - off] : 0u;
+    __syncthreads();
+    partial[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t run = partial[threadIdx.x] - s;
+  for (int k = b; k < b + per && k < nkeys; ++k) {
+    w.cursor[k] = run;
+    run += w.hist[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    uint32_t c = 0;
+    for (int k = threadIdx.x * ncb * kSortEBins; k < (threadIdx.x + 1) * ncb * kSortEBins; ++k) c += w.hist[k];
+    w.counts[threadIdx.x] = c;
+  }
+}
+
+__global__ void __launch_bounds__(256) sort_scatter_kernel(const __grid_constant__ DevTables T, int64_t n,
+                                                           const hepem_track_state in, const Work w, int ncb) {
   for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = base + threadIdx.x;
     int key = -1;
@@ -76,22 +157,17 @@ __global__ void __launch_bounds__(256) classify_kernel(const __grid_constant__ D
       const int type = in.type[i];
       const int imc = in.imc[i];
       const double e = in.ekin[i];
-      if (track_input_bad(T, type, imc, e)) {
-        // pass the track through unchanged, flagged
-        Track t;
-        Rng rng;
-        load_track(in, i, t, rng, nullptr, 0, 0, 2);
-        t.flags = kFlagBadInput;
-        store_track(in, out, res, i, t, rng, 2, true);
-        res.n_sec[i] = 0;
-        cnt.steps += 1;
-      } else {
-        key = type;
-      }
+      if (!track_input_bad(T, type, imc, e)) key = sort_key(type, imc, e, ncb);
     }
-    warp_push(key, (int32_t)i, w.list, w.counts);
+    // warp-aggregated: one atomic per distinct key in the warp
+    const unsigned same = __match_any_sync(0xFFFFFFFFu, key);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(same) - 1;
+    uint32_t base2 = 0;
+    if (key >= 0 && lane == leader) base2 = atomicAdd(&w.cursor[key], (uint32_t)__popc(same));
+    base2 = __shfl_sync(0xFFFFFFFFu, base2, leader);
+    if (key >= 0) w.perm[base2 + __popc(same & ((1u << lane) - 1u))] = (int32_t)i;
   }
-  add_counters(cnt, counters);
 }
 
 // ---- 2. stage A -----------------------------------------------------------------------
@@ -108,7 +184,7 @@ __global__ void __launch_bounds__(256) stage_a_charged_kernel(const __grid_const
     int key = -1;
     int32_t idx = 0;
     if (j < total) {
-      idx = j < nEm ? w.list[0][j] : w.list[1][j - nEm];
+      idx = w.perm[j];
       const int type = j < nEm ? 0 : 1;
       Track t;
       Rng rng;
@@ -142,7 +218,7 @@ __global__ void __launch_bounds__(256) stage_a_gamma_kernel(const __grid_constan
     int32_t idx = 0;
     double pe = 0.0;
     if (j < total) {
-      idx = w.list[2][j];
+      idx = w.perm[w.counts[0] + w.counts[1] + j];
       Track t;
       Rng rng;
       load_track(in, idx, t, rng, uniforms, nu, seed, 2);
@@ -267,7 +343,10 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
     gB[8] = grid_of(stage_b_kernel<8>, sms);
   }
   const Work w = carve(workspace, n);
+  const int ncb = T.nCouples < kSortCoupleBins ? T.nCouples : kSortCoupleBins;
+  const int nkeys = 3 * ncb * kSortEBins;
   cudaError_t e = cudaMemsetAsync(w.counts, 0, 64 * sizeof(uint32_t), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w.hist, 0, nkeys * sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
   int k = 0;
   auto mark = [&]() {
@@ -276,7 +355,9 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
   const int64_t blocks = (n + 255) / 256;
   const int gC = (int)(blocks < (int64_t)sms * 8 ? blocks : (int64_t)sms * 8);
   mark();
-  classify_kernel<<<gC, 256, 0, s>>>(T, n, in, out, res, w, counters);
+  sort_hist_kernel<<<gC, 256, nkeys * sizeof(uint32_t), s>>>(T, n, in, out, res, w, ncb, counters);
+  sort_scan_kernel<<<1, 1024, 0, s>>>(w, ncb);
+  sort_scatter_kernel<<<gC, 256, 0, s>>>(T, n, in, w, ncb);
   mark();
   stage_a_charged_kernel<<<gA, 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
   mark();

@@ -153,9 +153,9 @@ int  hepem_step(const hepem_ctx* ctx, int64_t n, const hepem_track_state* in,
                 void* stream);
 
 /* Batched form of hepem_step: same arguments, same results bit for bit.
- * Tracks are sorted into per-particle lists and, after the continuous part of
- * the step, into per-interaction queues, so that every warp executes one
- * model at a time (no reference counterpart: a scheduling of the same
+ * Tracks are sorted by particle, couple and energy and, after the continuous
+ * part of the step, into per-interaction queues, so that every warp executes
+ * one model at a time (no reference counterpart: a scheduling of the same
  * G4HepEmElectronManager / G4HepEmGammaManager calls).  Uses a stream-ordered
  * workspace of about 48 bytes per track (cudaMallocAsync on `stream`). */
 int  hepem_step_batched(const hepem_ctx* ctx, int64_t n, const hepem_track_state* in,
