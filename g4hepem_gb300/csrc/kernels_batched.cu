@@ -79,6 +79,9 @@ static Work carve(void* ws, int64_t n) {
 }
 
 __device__ __forceinline__ int sort_key(int type, int imc, double e, int ncb) {
+  // Gammas keep their batch order (one key): their stage is light on FP64 and
+  // latency bound, so coalesced loads matter more there than branch coherence.
+  if (type == 2) return 2 * ncb * kSortEBins;
   // log2(1 keV / MeV) = -9.9658, log2(100 TeV / 1 keV) = 36.5412
   int eb = (int)((__log2f((float)e) + 9.965784f) * (kSortEBins / 36.541209f));
   eb = eb < 0 ? 0 : (eb >= kSortEBins ? kSortEBins - 1 : eb);
