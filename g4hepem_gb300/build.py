@@ -24,6 +24,7 @@ UNITS = [
     ("kernels_fp64.cu", ["-fmad=false"]),
     ("kernels_batched.cu", ["-fmad=false"]),
     ("api.cu", ["-fmad=false"]),
+    ("noalloc.cu", []),
     ("state_json.cpp", []),
 ]
 

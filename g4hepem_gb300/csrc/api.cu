@@ -9,33 +9,10 @@
 #include <string>
 
 #include "g4hepem_gb300.h"
+#include "ctx.h"
 #include "kernels.h"
 #include "rng.cuh"
 #include "state_image.h"
-
-struct hepem_ctx {
-  int device = -1;
-  int sms = 0;
-  void* arena = nullptr;
-  size_t arenaBytes = 0;
-  hepem::DevTables tables;
-  // copy/compute pipeline of hepem_step_host (grow-only buffers, serialised by mu)
-  static constexpr int kSlots = 3;
-  struct Slot {
-    cudaStream_t s = nullptr;
-    cudaEvent_t done = nullptr;
-    void* buf = nullptr;
-    size_t bytes = 0;
-  };
-  std::mutex mu;
-  Slot slot[kSlots];
-  cudaEvent_t start = nullptr;
-  bool slotsReady = false;
-  // per-stage timing of the batched form (hepem_profile_stages)
-  bool profile = false;
-  bool stageEvReady = false;
-  cudaEvent_t stageEv[hepem::kNumStageEvents] = {};
-};
 
 namespace {
 
@@ -93,6 +70,12 @@ const size_t kStateSizes[20] = {1, 4, 4, 8, 8, 8, 8, 8, 8, 8, 8, 8, 1, 8, 8, 8, 
 const size_t kOutSizes[14] = {8, 8, 8, 1, 8, 8, 8, 1, 1, 2, 16, 16, 16, 16};  // secondaries: 2 slots
 
 }  // namespace
+
+namespace hepem {
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+bool valid_state(const hepem_track_state* s) { return state_ok(s); }
+bool valid_out(const hepem_step_out* r) { return out_ok(r); }
+}  // namespace hepem
 
 extern "C" {
 

@@ -1,0 +1,42 @@
+// ctx.h -- the context behind the opaque hepem_ctx handle of the C-ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+
+#include "g4hepem_gb300.h"
+#include "kernels.h"
+#include "tables.h"
+
+struct hepem_ctx {
+  int device = -1;
+  int sms = 0;
+  void* arena = nullptr;
+  size_t arenaBytes = 0;
+  hepem::DevTables tables;
+  // copy/compute pipeline of hepem_step_host (grow-only buffers, serialised by mu)
+  static constexpr int kSlots = 3;
+  struct Slot {
+    cudaStream_t s = nullptr;
+    cudaEvent_t done = nullptr;
+    void* buf = nullptr;
+    size_t bytes = 0;
+  };
+  std::mutex mu;
+  Slot slot[kSlots];
+  cudaEvent_t start = nullptr;
+  bool slotsReady = false;
+  // per-stage timing of the batched form (hepem_profile_stages)
+  bool profile = false;
+  bool stageEvReady = false;
+  cudaEvent_t stageEv[hepem::kNumStageEvents] = {};
+};
+
+namespace hepem {
+// record the calling thread's last error message (hepem_last_error) and return code
+int set_error(int code, const std::string& msg);
+bool valid_state(const hepem_track_state* s);
+bool valid_out(const hepem_step_out* r);
+}  // namespace hepem

@@ -32,6 +32,7 @@ OUT_FIELDS = [("edep", np.float64, 1), ("gstep", np.float64, 1), ("pstep", np.fl
 STATE_OUT_FIELDS = [f for f, _ in STATE_FIELDS if f not in ("type", "imc", "id", "safety", "on_boundary")]
 
 FLAG_RNG_OVERFLOW, FLAG_LOOP_CAP, FLAG_BAD_INPUT, FLAG_BAD_INDEX = 1, 2, 4, 8
+NOALLOC_MAX_TRACKS = 524288  # HEPEM_NOALLOC_MAX_TRACKS
 
 
 class TrackState(C.Structure):
@@ -48,7 +49,8 @@ class StepCounters(C.Structure):
 
 
 EXPORTED = ["hepem_create", "hepem_create_from_file", "hepem_destroy", "hepem_info", "hepem_status_string",
-            "hepem_last_error", "hepem_electron_lookup", "hepem_step", "hepem_step_batched", "hepem_step_host",
+            "hepem_last_error", "hepem_electron_lookup", "hepem_step", "hepem_step_batched",
+            "hepem_step_batched_noalloc", "hepem_step_host",
             "hepem_philox_uniform", "hepem_fill_uniforms", "hepem_profile_stages", "hepem_stage_times"]
 
 
@@ -80,6 +82,7 @@ def lib():
                                  C.c_uint64, C.POINTER(StepOut), _vp, _vp]
         L.hepem_step_host.argtypes = L.hepem_step.argtypes
         L.hepem_step_batched.argtypes = L.hepem_step.argtypes
+        L.hepem_step_batched_noalloc.argtypes = L.hepem_step.argtypes
         L.hepem_philox_uniform.argtypes = [C.c_uint64, C.c_int32, C.c_int32]
         L.hepem_philox_uniform.restype = C.c_double
         L.hepem_fill_uniforms.argtypes = [C.c_int64, _vp, C.c_int32, C.c_uint64, _vp, _vp]
@@ -167,10 +170,12 @@ class Context:
 
     def step(self, state_in: dict, state_out: dict, uniforms, n_uniform: int, seed: int, res: dict,
              counters=None, stream=None, form="plain"):
-        """One step of every track; form: "plain" (hepem_step) or "batched" (hepem_step_batched)."""
+        """One step of every track; form: "plain" (hepem_step), "batched" (hepem_step_batched) or
+        "noalloc" (hepem_step_batched_noalloc)."""
         n = state_in["ekin"].numel()
         sin, sout, sres = make_state_struct(state_in), make_state_struct(state_out), make_out_struct(res)
-        fn = {"plain": lib().hepem_step, "batched": lib().hepem_step_batched}[form]
+        fn = {"plain": lib().hepem_step, "batched": lib().hepem_step_batched,
+              "noalloc": lib().hepem_step_batched_noalloc}[form]
         check(fn(self.h, n, C.byref(sin), C.byref(sout), _ptr(uniforms), n_uniform, seed, C.byref(sres),
                  _ptr(counters) if counters is not None else None, _stream_ptr(stream)))
 

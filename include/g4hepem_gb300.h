@@ -163,6 +163,25 @@ int  hepem_step_batched(const hepem_ctx* ctx, int64_t n, const hepem_track_state
                         uint64_t seed, hepem_step_out* res, hepem_step_counters* counters,
                         void* stream);
 
+/* Same as hepem_step_batched, except that this library allocates no device
+ * memory for the call.  For callers that cannot let a library allocate:
+ * applications that give all device memory to their own pool allocator at
+ * start-up, serving loops that must not enter an allocator on their latency
+ * path, integrations that forbid hidden allocations in third-party libraries.
+ * The workspace is a fixed 32 MiB array in the library's device image, held
+ * by every GPU that loads the library until the process exits; batches are
+ * limited to HEPEM_NOALLOC_MAX_TRACKS tracks (larger ones: HEPEM_BAD_ARG).
+ * The first call on a device looks up the array's device address on the
+ * current device (make it before any stream capture); the current device must
+ * be the context's.  All calls share the array: calls that overlap on the GPU
+ * (other streams, other threads) race.  No counterpart in the reference (its
+ * host functions need no device workspace). */
+#define HEPEM_NOALLOC_MAX_TRACKS 524288
+int  hepem_step_batched_noalloc(const hepem_ctx* ctx, int64_t n, const hepem_track_state* in,
+                                hepem_track_state* out, const double* uniforms,
+                                int32_t n_uniform, uint64_t seed, hepem_step_out* res,
+                                hepem_step_counters* counters, void* stream);
+
 /* Same with HOST buffers: copies the batch in, steps it (batched form),
  * copies the results back and synchronises.  Pinned host memory is fastest.
  * Reference counterpart: the per-track G4HepEmElectronManager::HowFar/Perform
