@@ -148,6 +148,102 @@ def profile_summary(name):
         return None
 
 
+def c1_lookups(torch, N, ctx, stream, args, hbm):
+    """BASELINE configuration 1: 2^20 e- with energies log-uniform in
+    [1 keV, 100 TeV] over the 3 couples; restricted ionisation and brem cross
+    sections, dE/dx, range and inverse range at half the range per track
+    (hepem_electron_lookup).  Inputs 12 B + outputs 40 B per track; the
+    2^20-track batch (54.5 MB) fits L2, so each timed launch reads a fresh
+    batch slice of a 16x larger buffer (inputs larger than L2)."""
+    from g4hepem_gb300 import workload as W
+    n1, reps = 1 << 20, 16
+    e_np, i_np = W.electron_lookup_batch(n1 * reps, seed=11)
+    ekin = torch.from_numpy(e_np).cuda()
+    imc = torch.from_numpy(i_np).cuda()
+    outs = [{k: torch.empty(n1, dtype=torch.float64, device="cuda")
+             for k in ("xs_ioni", "xs_brem", "dedx", "range", "invrange_half")} for _ in range(2)]
+    for r in range(3):
+        ctx.electron_lookup(ekin[r * n1:(r + 1) * n1], imc[r * n1:(r + 1) * n1], out=outs[r % 2], stream=stream)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k = max(args.steps, reps)
+    ev0.record(stream)
+    for r in range(k):
+        s = (r % reps) * n1
+        ctx.electron_lookup(ekin[s:s + n1], imc[s:s + n1], out=outs[r % 2], stream=stream)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / k
+    alg = n1 * (8 + 4 + 5 * 8)
+    return {"workload": "2^20 e-, 1 keV-100 TeV log-uniform, 3 couples, 5 lookups per track",
+            "value": n1 / (ms / 1e3), "unit": "tracks/s", "ms_per_launch": ms, "launches": k,
+            "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                         "frac": alg / (ms / 1e3) / 1e9 / hbm, "algorithmic_bytes_per_launch": alg,
+                         "note": "FP64-issue bound like the step (VDT log, 4 splines, range bisection)"}}
+
+
+def c3_batching(torch, N, args):
+    """BASELINE configuration 3: 64 sub-batches of log-normal sizes (median 30k
+    before scaling, sigma 1.5, clipped to [1k, 1M], scaled to 16,777,216 tracks
+    in total), the configuration-2 particle and energy mix, 16 random couples
+    (1-4 elements, Z in 1..82, 1-12 g/cm3, cuts 0.1/0.7/1.0 mm).  Each
+    sub-batch is one call; timed: the plain form, the batched form, and the
+    batched form captured once in a CUDA graph and replayed."""
+    from g4hepem_gb300 import workload as W
+    table = os.path.join(REPO, "g4hepem_gb300", "data", "random16.json")
+    ctx = N.Context(table)
+    sizes = W.subbatch_sizes()
+    total = int(sizes.sum())
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    st = W.mixed_batch(total, n_couples=16, seed=17)
+    sin = N.state_to_torch(st)
+    sout = N.empty_state_torch(total)
+    res = N.alloc_out_torch(total)
+    u = N.fill_uniforms(sin["id"], NU, SEED)
+    slots = {f: k for f, _, k in N.OUT_FIELDS}
+
+    def one_pass(form):
+        for b in range(len(sizes)):
+            a, e = int(off[b]), int(off[b + 1])
+            ctx.step({k: v[a:e] for k, v in sin.items()}, {k: v[a:e] for k, v in sout.items()},
+                     u[a * NU:e * NU], NU, SEED, {k: v[a * slots[k]:e * slots[k]] for k, v in res.items()},
+                     form=form)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(reps):
+            fn()
+        ev1.record()
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / reps
+
+    reps = max(2, min(args.steps, 5))
+    ms_plain = timed(lambda: one_pass("plain"), 1)
+    ms_batched = timed(lambda: one_pass("batched"), reps)
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        one_pass("batched")
+    torch.cuda.current_stream().wait_stream(side)
+    with torch.cuda.graph(graph):
+        one_pass("batched")
+    ms_graph = timed(graph.replay, reps)
+    ctx.close()
+    return {"workload": "64 sub-batches (log-normal, median 30k, sigma 1.5, clipped [1k, 1M], scaled to "
+                        "16,777,216 tracks), 16 random couples, configuration-2 particle/energy mix",
+            "subbatch_min": int(sizes.min()), "subbatch_median": int(np.median(sizes)),
+            "subbatch_max": int(sizes.max()),
+            "plain": {"value": total / (ms_plain / 1e3), "unit": UNIT, "ms_per_pass": ms_plain},
+            "batched": {"value": total / (ms_batched / 1e3), "unit": UNIT, "ms_per_pass": ms_batched},
+            "batched_graph": {"value": total / (ms_graph / 1e3), "unit": UNIT, "ms_per_pass": ms_graph,
+                              "launches_per_pass": LAUNCHES_PER_STEP * len(sizes)},
+            "vs_plain": ms_plain / ms_graph}
+
+
 def cpu_port_rate(state, threads, n_sample, reps=1):
     from oracle import oracle as O
     O.build_port()
@@ -198,6 +294,7 @@ def main():
     ap.add_argument("--n", type=int, default=N_TRACKS)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-c3", action="store_true")
     args = ap.parse_args()
     ws, rank, lrank = dist_env()
     if args.impl == "reference":
@@ -303,6 +400,8 @@ def main():
     if rank != 0:
         return
     hbm, hbm_src = peaks()
+    c1 = c1_lookups(torch, N, ctx, stream, args, hbm)
+    c3 = None if args.no_c3 else c3_batching(torch, N, args)
     # per-stage device times of one more batched step: CUDA events recorded on
     # the launching stream around every stage kernel (hepem_profile_stages)
     import ctypes as C
@@ -357,7 +456,7 @@ def main():
             "plain_fp64": {"value": ws * n / (ms_plain / 1e3), "unit": UNIT, "ms_per_step": ms_plain,
                            "entry_point": "hepem_step"},
             "vs_plain_fp64": ms_plain / ms_step, "roofline": roof, "roofline_fp64": fp64,
-            "stage_ms": stages, "cpu_baseline": cpu, "clocks": clk,
+            "stage_ms": stages, "c1_lookup": c1, "c3_batching": c3, "cpu_baseline": cpu, "clocks": clk,
             "counters": {"uniforms_per_step": uniforms_consumed, "secondaries_per_step": secondaries,
                          "interactions": [int(x) for x in c[4:12]]}}
     print(json.dumps(line), flush=True)

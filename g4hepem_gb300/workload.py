@@ -114,3 +114,33 @@ def electron_lookup_batch(n: int, n_couples: int = 3, seed: int = 11, emin=1e-3,
     ekin = np.exp(np.log(emin) + (np.log(emax) - np.log(emin)) * rng.random(n))
     imc = rng.integers(0, n_couples, size=n).astype(np.int32)
     return ekin, imc
+
+
+def subbatch_sizes(total: int = 1 << 24, n_sub: int = 64, median: float = 30000.0, sigma: float = 1.5,
+                   lo: int = 1000, hi: int = 1 << 20, seed: int = 3) -> np.ndarray:
+    """Uneven sub-batch sizes of BASELINE configuration 3: log-normal with the
+    given median and sigma, scaled so that the clipped sizes sum to `total`
+    (the scale factor is found by bisection; the last size absorbs rounding)."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    base = median * np.exp(sigma * rng.standard_normal(n_sub))
+    f_lo, f_hi = 1e-6, 1e6
+    for _ in range(200):
+        f = np.sqrt(f_lo * f_hi)
+        s = np.clip(base * f, lo, hi).sum()
+        if s < total:
+            f_lo = f
+        else:
+            f_hi = f
+    sizes = np.clip(np.round(base * np.sqrt(f_lo * f_hi)), lo, hi).astype(np.int64)
+    diff = total - int(sizes.sum())
+    order = np.argsort(-sizes) if diff < 0 else np.argsort(sizes)
+    k = 0
+    while diff != 0:
+        j = order[k % n_sub]
+        step = int(np.clip(sizes[j] + diff, lo, hi)) - int(sizes[j])
+        sizes[j] += step
+        diff -= step
+        k += 1
+        if k > 10 * n_sub:
+            break
+    return sizes

@@ -260,6 +260,39 @@ def test_batched_equals_plain_bitwise(native, gpu_ctx, table, nc, emin, emax):
     assert np.array_equal(a_cnt, b_cnt), (a_cnt, b_cnt)
 
 
+def test_batched_step_replays_from_a_cuda_graph(native, gpu_ctx):
+    """The batched entry point is stream-capturable (its workspace is a
+    stream-ordered allocation): capture once, replay, same results."""
+    torch = _torch()
+    st = W.mixed_batch(100000, seed=71)
+    n = len(st["ekin"])
+    ctx = gpu_ctx(T3)
+    sin = native.state_to_torch(st)
+    u = native.fill_uniforms(sin["id"], 64, 9)
+    ref_out, ref_res = native.empty_state_torch(n), native.alloc_out_torch(n)
+    ctx.step(sin, ref_out, u, 64, 9, ref_res, form="batched")
+    g_out, g_res = native.empty_state_torch(n), native.alloc_out_torch(n)
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        ctx.step(sin, g_out, u, 64, 9, g_res, form="batched")
+    torch.cuda.current_stream().wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        ctx.step(sin, g_out, u, 64, 9, g_res, form="batched")
+    for v in list(g_out.values()) + list(g_res.values()):
+        v.zero_()
+    graph.replay()
+    graph.replay()
+    torch.cuda.synchronize()
+    a, b = native.to_numpy(ref_out), native.to_numpy(g_out)
+    for k in native.STATE_OUT_FIELDS:
+        assert np.array_equal(a[k], b[k], equal_nan=True), k
+    ra, rb = native.to_numpy(ref_res), native.to_numpy(g_res)
+    for k in ("edep", "gstep", "pstep", "winner", "n_sec", "flags"):
+        assert np.array_equal(ra[k], rb[k]), k
+
+
 def test_batched_in_place(native, gpu_ctx):
     st = W.mixed_batch(50000, seed=61)
     a = gpu_step(native, gpu_ctx(T3), st, 5, 64, form="batched")
