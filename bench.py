@@ -187,8 +187,10 @@ def c3_batching(torch, N, args):
     before scaling, sigma 1.5, clipped to [1k, 1M], scaled to 16,777,216 tracks
     in total), the configuration-2 particle and energy mix, 16 random couples
     (1-4 elements, Z in 1..82, 1-12 g/cm3, cuts 0.1/0.7/1.0 mm).  Each
-    sub-batch is one call; timed: the plain form, the batched form, and the
-    batched form captured once in a CUDA graph and replayed."""
+    sub-batch is one call; timed: the plain form, the batched form with the
+    default launch configuration, the batched form with the configuration
+    chosen by the autotuner, and the latter captured once in a CUDA graph and
+    replayed."""
     from g4hepem_gb300 import workload as W
     table = os.path.join(REPO, "g4hepem_gb300", "data", "random16.json")
     ctx = N.Context(table)
@@ -222,6 +224,10 @@ def c3_batching(torch, N, args):
 
     reps = max(2, min(args.steps, 5))
     ms_plain = timed(lambda: one_pass("plain"), 1)
+    ms_default = timed(lambda: one_pass("batched"), reps)
+    # launch configuration chosen by the autotuner on a 2^20-track sample of the workload
+    ns = 1 << 20
+    tuned = ctx.autotune({k: v[:ns] for k, v in sin.items()}, u[:ns * NU], NU, SEED, apply=True)
     ms_batched = timed(lambda: one_pass("batched"), reps)
     graph = torch.cuda.CUDAGraph()
     side = torch.cuda.Stream()
@@ -238,10 +244,108 @@ def c3_batching(torch, N, args):
             "subbatch_min": int(sizes.min()), "subbatch_median": int(np.median(sizes)),
             "subbatch_max": int(sizes.max()),
             "plain": {"value": total / (ms_plain / 1e3), "unit": UNIT, "ms_per_pass": ms_plain},
-            "batched": {"value": total / (ms_batched / 1e3), "unit": UNIT, "ms_per_pass": ms_batched},
+            "batched_default_launch": {"value": total / (ms_default / 1e3), "unit": UNIT, "ms_per_pass": ms_default},
+            "batched": {"value": total / (ms_batched / 1e3), "unit": UNIT, "ms_per_pass": ms_batched,
+                        "launch": "autotuned (hepem_autotune on 2^20 tracks)"},
+            "autotuned_config": tuned,
             "batched_graph": {"value": total / (ms_graph / 1e3), "unit": UNIT, "ms_per_pass": ms_graph,
                               "launches_per_pass": LAUNCHES_PER_STEP * len(sizes)},
             "vs_plain": ms_plain / ms_graph}
+
+
+def c4_serving(torch, N, args):
+    """BASELINE configuration 4: an event stream through the serving form
+    (hepem_server_*).  A request is one event's track batch, log-normal in size
+    (median 2k tracks, sigma 1.5, clipped to [1, 500k]), with the
+    configuration-2 particle / energy / couple mix; 256 distinct event batches
+    are drawn once and re-submitted with fresh seeds (new uniform streams).
+    Memory admission budget 16 GB; tracks stay resident until they fall below
+    1 keV or the request reaches 1000 steps.  First the sustained peak: a
+    closed loop with 512 requests in flight; then open-loop Poisson arrivals at
+    25/50/90% of that peak request rate.  Reported per level: steps/s, p50/p99 request
+    latency (submit to result) and p50/p99 batch latency (one server
+    iteration: one batched step over every resident track)."""
+    from g4hepem_gb300 import workload as W
+    ctx = N.Context(TABLE)
+    srv = N.Server(ctx, memory_budget_bytes=16 << 30, max_steps=1000, max_requests=4096, min_energy=1.0e-3)
+    rng = np.random.Generator(np.random.Philox(41))
+    sizes = np.clip(np.round(2000.0 * np.exp(1.5 * rng.standard_normal(256))), 1, 500000).astype(np.int64)
+    events = [W.mixed_batch(int(m), seed=1000 + k) for k, m in enumerate(sizes)]
+    seed_next = [1 << 40]
+
+    def submit(k):
+        seed_next[0] += 1
+        return srv.submit(events[k % len(events)], seed=seed_next[0])
+
+    def collect(ids):
+        return [srv.wait(i, timeout_s=300.0)[0] for i in ids]
+
+    def summary(res, t_first, st):
+        t_end = max(r["t_done"] for r in res)
+        window = t_end - t_first
+        lat = np.array([r["t_done"] - r["t_submit"] for r in res]) * 1e3
+        steps = sum(r["track_steps"] for r in res)
+        return {"requests": len(res), "tracks": int(sum(r["n_tracks"] for r in res)),
+                "track_steps": int(steps), "seconds": window, "steps_per_s": steps / window,
+                "requests_per_s": len(res) / window,
+                "request_ms_p50": float(np.percentile(lat, 50)), "request_ms_p99": float(np.percentile(lat, 99)),
+                "batch_ms_p50": st["batch_ms_p50"], "batch_ms_p99": st["batch_ms_p99"],
+                "iterations": st["iterations"], "mean_tracks_per_iteration": st["track_steps"] / max(1, st["iterations"])}
+
+    # warm-up, then the sustained peak: a closed loop that keeps 512 requests
+    # in flight for 3 s (each completion is replaced by a new request); the
+    # rates are read over the last 2 s from the server's own counters
+    collect([submit(k) for k in range(64)])
+    inflight, k = [], 0
+    for _ in range(512):
+        inflight.append(submit(k))
+        k += 1
+    t_start = time.monotonic()
+    measuring = False
+    done_in_window = []
+    while time.monotonic() - t_start < 3.0:
+        r = srv.wait(inflight.pop(0), timeout_s=300.0)[0]
+        if not measuring and time.monotonic() - t_start > 1.0:
+            srv.reset_stats()
+            measuring, t_win = True, time.monotonic()
+        elif measuring:
+            done_in_window.append(r)
+        inflight.append(submit(k))
+        k += 1
+    st = srv.stats()
+    win = time.monotonic() - t_win
+    collect(inflight)
+    lat = np.array([r["t_done"] - r["t_submit"] for r in done_in_window]) * 1e3
+    peak = {"mode": "closed loop, 512 requests in flight", "seconds": win, "requests": len(done_in_window),
+            "steps_per_s": st["track_steps"] / win, "requests_per_s": len(done_in_window) / win,
+            "request_ms_p50": float(np.percentile(lat, 50)), "request_ms_p99": float(np.percentile(lat, 99)),
+            "batch_ms_p50": st["batch_ms_p50"], "batch_ms_p99": st["batch_ms_p99"], "iterations": st["iterations"],
+            "mean_tracks_per_iteration": st["track_steps"] / max(1, st["iterations"])}
+    levels = {}
+    for frac in (0.25, 0.5, 0.9):
+        rate = frac * peak["requests_per_s"]
+        duration = 2.0
+        srv.reset_stats()
+        arr = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * duration * 1.5) + 16))
+        arr = arr[arr < duration]
+        ids = []
+        t0 = time.monotonic()
+        for k, ta in enumerate(arr):
+            d = ta - (time.monotonic() - t0)
+            if d > 0:
+                time.sleep(d)
+            ids.append(submit(k))
+        res = collect(ids)
+        s = summary(res, min(r["t_submit"] for r in res), srv.stats())
+        s["offered_requests_per_s"] = rate
+        levels[f"{int(frac * 100)}%"] = s
+    cap = srv.capacity
+    srv.close()
+    ctx.close()
+    return {"workload": "event stream: requests log-normal (median 2k tracks, sigma 1.5, clipped [1, 500k]), "
+                        "configuration-2 mix, 16 GB admission budget, resident until < 1 keV or 1000 steps",
+            "capacity_tracks": cap, "event_pool": len(events), "event_size_median": int(np.median(sizes)),
+            "event_size_max": int(sizes.max()), "peak": peak, "poisson": levels}
 
 
 def cpu_port_rate(state, threads, n_sample, reps=1):
@@ -295,6 +399,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-c3", action="store_true")
+    ap.add_argument("--no-c4", action="store_true")
     args = ap.parse_args()
     ws, rank, lrank = dist_env()
     if args.impl == "reference":
@@ -402,6 +507,7 @@ def main():
     hbm, hbm_src = peaks()
     c1 = c1_lookups(torch, N, ctx, stream, args, hbm)
     c3 = None if args.no_c3 else c3_batching(torch, N, args)
+    c4 = None if args.no_c4 else c4_serving(torch, N, args)
     # per-stage device times of one more batched step: CUDA events recorded on
     # the launching stream around every stage kernel (hepem_profile_stages)
     import ctypes as C
@@ -456,7 +562,7 @@ def main():
             "plain_fp64": {"value": ws * n / (ms_plain / 1e3), "unit": UNIT, "ms_per_step": ms_plain,
                            "entry_point": "hepem_step"},
             "vs_plain_fp64": ms_plain / ms_step, "roofline": roof, "roofline_fp64": fp64,
-            "stage_ms": stages, "c1_lookup": c1, "c3_batching": c3, "cpu_baseline": cpu, "clocks": clk,
+            "stage_ms": stages, "c1_lookup": c1, "c3_batching": c3, "c4_serving": c4, "cpu_baseline": cpu, "clocks": clk,
             "counters": {"uniforms_per_step": uniforms_consumed, "secondaries_per_step": secondaries,
                          "interactions": [int(x) for x in c[4:12]]}}
     print(json.dumps(line), flush=True)

@@ -25,6 +25,8 @@ UNITS = [
     ("kernels_batched.cu", ["-fmad=false"]),
     ("api.cu", ["-fmad=false"]),
     ("noalloc.cu", []),
+    ("server.cu", ["-fmad=false"]),
+    ("tune.cu", []),
     ("state_json.cpp", []),
 ]
 

@@ -89,6 +89,7 @@ const char* hepem_status_string(int s) {
     case HEPEM_TIMEOUT: return "bounded wait gave up";
     case HEPEM_OOM_ADMISSION: return "request exceeds the memory budget";
     case HEPEM_NO_DEVICE: return "no CUDA device";
+    case HEPEM_CANCELLED: return "request cancelled";
     default: return "unknown status";
   }
 }
@@ -177,8 +178,11 @@ int hepem_step_batched(const hepem_ctx* c, int64_t n, const hepem_track_state* i
   cudaStream_t s = (cudaStream_t)stream;
   void* ws = nullptr;
   HEPEM_CUDA(cudaMallocAsync(&ws, hepem::batched_workspace_bytes(n), s));
+  hepem::BatchOpts o;
+  o.ev = c->profile ? const_cast<cudaEvent_t*>(c->stageEv) : nullptr;
+  o.cfg = &c->launch;
   cudaError_t e = hepem::launch_step_batched(c->tables, n, *in, *out, uniforms, nu, seed, *res, counters, ws, s,
-                                             c->sms, c->profile ? const_cast<cudaEvent_t*>(c->stageEv) : nullptr);
+                                             c->sms, o);
   cudaError_t f = cudaFreeAsync(ws, s);
   if (e != cudaSuccess) return cuda_fail(e, "batched step launch");
   if (f != cudaSuccess) return cuda_fail(f, "cudaFreeAsync");
@@ -261,8 +265,10 @@ int hepem_step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in,
                                  cudaMemcpyHostToDevice, ss));
     if (nu > 0)
       HEPEM_CUDA(cudaMemcpyAsync(du, uniforms + off * nu, sizeof(double) * (size_t)mc * nu, cudaMemcpyHostToDevice, ss));
+    hepem::BatchOpts o;
+    o.cfg = &c->launch;
     HEPEM_CUDA(hepem::launch_step_batched(c->tables, mc, ds, ds, du, nu, seed, dr, counters ? cnt : nullptr, dwork,
-                                          ss, c->sms, nullptr));
+                                          ss, c->sms, o));
     // persistent per-track fields come back (type/imc/id/safety/boundary are inputs only)
     for (int k = 3; k < 20; ++k) {
       if (k == 11 || k == 12) continue;

@@ -16,6 +16,8 @@ struct hepem_ctx {
   void* arena = nullptr;
   size_t arenaBytes = 0;
   hepem::DevTables tables;
+  // launch configuration of the batched form (hepem_set_launch_config / hepem_autotune)
+  hepem::LaunchCfg launch = hepem::default_launch_cfg();
   // copy/compute pipeline of hepem_step_host (grow-only buffers, serialised by mu)
   static constexpr int kSlots = 3;
   struct Slot {

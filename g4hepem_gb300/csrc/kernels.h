@@ -17,12 +17,30 @@ cudaError_t launch_step(const DevTables& T, int64_t n, const hepem_track_state& 
                         const double* uniforms, int nu, uint64_t seed, const hepem_step_out& res,
                         hepem_step_counters* counters, cudaStream_t s, int sms);
 
-// batched form (kernels_batched.cu): workspace of batched_workspace_bytes(n)
+// batched form (kernels_batched.cu): workspace of batched_workspace_bytes(n).
 size_t batched_workspace_bytes(int64_t n);
+// the eleven stage kernels: e+- stage A, gamma stage A, nine interaction kernels
+constexpr int kNumStageKernels = 11;
+// launch configuration of the stage kernels (chosen by hepem_autotune)
+struct LaunchCfg {
+  int block[kNumStageKernels];      // threads per block: 128, 256 or 512
+  int ctasPerSM[kNumStageKernels];  // 0 (or above the occupancy) = as many as fit
+  int sortEBins;                    // energy bins of the sort key: 8, 16 or 32
+};
+LaunchCfg default_launch_cfg();
+bool valid_launch_cfg(const LaunchCfg& c);
+int stage_occupancy(int kernel, int block);
+// optional inputs of a batched step
+struct BatchOpts {
+  cudaEvent_t* ev = nullptr;         // stage timing: kNumStageEvents events
+  const int32_t* active = nullptr;   // step tracks active[0..n) of larger arrays (serving pool)
+  const uint64_t* seeds = nullptr;   // per-track RNG keys instead of one seed
+  const LaunchCfg* cfg = nullptr;    // null: the default configuration
+};
 cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track_state& in,
                                 const hepem_track_state& out, const double* uniforms, int nu, uint64_t seed,
                                 const hepem_step_out& res, hepem_step_counters* counters, void* workspace,
-                                cudaStream_t s, int sms, cudaEvent_t* stage_events);
+                                cudaStream_t s, int sms, const BatchOpts& opts);
 // stage timing: events recorded before the first and after every stage kernel
 constexpr int kNumStageEvents = 13;
 const char* stage_name(int i);

@@ -32,9 +32,9 @@ namespace hepem {
 // Tracks are ordered by a sort key (particle, couple bin, energy bin) with a
 // counting sort, so that the warps of a stage hold tracks of one particle in
 // one material at similar energies and take the same branches.
-constexpr int kSortEBins = 32;      // log2(E) bins over 1 keV - 100 TeV
+constexpr int kMaxSortEBins = 32;   // log2(E) bins over 1 keV - 100 TeV (the launch configuration picks 8..32)
 constexpr int kSortCoupleBins = 64; // couples beyond 64 share bins (imc % 64)
-constexpr int kMaxSortKeys = 3 * kSortCoupleBins * kSortEBins;
+constexpr int kMaxSortKeys = 3 * kSortCoupleBins * kMaxSortEBins;
 
 struct Work {
   uint32_t* counts;               // [0..2] e-, e+, gamma tracks, [3..3+kNumQueues) queues
@@ -43,7 +43,12 @@ struct Work {
   int32_t* perm;                  // [n] valid tracks in sort-key order
   int32_t* queue[kNumQueues];
   double* peXS;                   // parallel to queue[kQPhotoelectric]
+  const uint64_t* seeds;          // per-track RNG keys (serving), or null: one key per call
 };
+
+__device__ __forceinline__ uint64_t key_of(const Work& w, int64_t i, uint64_t seed) {
+  return w.seeds ? w.seeds[i] : seed;
+}
 
 const char* stage_name(int i) {
   static const char* names[kNumStageEvents - 1] = {
@@ -78,27 +83,29 @@ static Work carve(void* ws, int64_t n) {
   return w;
 }
 
-__device__ __forceinline__ int sort_key(int type, int imc, double e, int ncb) {
+__device__ __forceinline__ int sort_key(int type, int imc, double e, int ncb, int neb) {
   // Gammas keep their batch order (one key): their stage is light on FP64 and
   // latency bound, so coalesced loads matter more there than branch coherence.
-  if (type == 2) return 2 * ncb * kSortEBins;
+  if (type == 2) return 2 * ncb * neb;
   // log2(1 keV / MeV) = -9.9658, log2(100 TeV / 1 keV) = 36.5412
-  int eb = (int)((__log2f((float)e) + 9.965784f) * (kSortEBins / 36.541209f));
-  eb = eb < 0 ? 0 : (eb >= kSortEBins ? kSortEBins - 1 : eb);
-  return ((type * ncb) + (imc % ncb)) * kSortEBins + eb;
+  int eb = (int)((__log2f((float)e) + 9.965784f) * ((float)neb / 36.541209f));
+  eb = eb < 0 ? 0 : (eb >= neb ? neb - 1 : eb);
+  return ((type * ncb) + (imc % ncb)) * neb + eb;
 }
 
 // ---- 1. sort: histogram, scan, scatter ----------------------------------------------
 __global__ void __launch_bounds__(256) sort_hist_kernel(const __grid_constant__ DevTables T, int64_t n,
+                                                        const int32_t* __restrict__ active,
                                                         const hepem_track_state in, const hepem_track_state out,
                                                         const hepem_step_out res, const Work w, int ncb,
-                                                        hepem_step_counters* counters) {
+                                                        int neb, hepem_step_counters* counters) {
   extern __shared__ uint32_t sh[];
-  const int nkeys = 3 * ncb * kSortEBins;
+  const int nkeys = 3 * ncb * neb;
   for (int k = threadIdx.x; k < nkeys; k += blockDim.x) sh[k] = 0;
   __syncthreads();
   StepCount cnt = {};
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = active ? (int64_t)active[j] : j;
     const int type = in.type[i];
     const int imc = in.imc[i];
     const double e = in.ekin[i];
@@ -112,7 +119,7 @@ __global__ void __launch_bounds__(256) sort_hist_kernel(const __grid_constant__ 
       res.n_sec[i] = 0;
       cnt.steps += 1;
     } else {
-      atomicAdd(&sh[sort_key(type, imc, e, ncb)], 1u);
+      atomicAdd(&sh[sort_key(type, imc, e, ncb, neb)], 1u);
     }
   }
   __syncthreads();
@@ -123,9 +130,9 @@ __global__ void __launch_bounds__(256) sort_hist_kernel(const __grid_constant__ 
 
 // one block: exclusive scan of the histogram into the scatter cursors, and
 // the number of tracks of each particle type
-__global__ void __launch_bounds__(1024) sort_scan_kernel(const Work w, int ncb) {
+__global__ void __launch_bounds__(1024) sort_scan_kernel(const Work w, int ncb, int neb) {
   __shared__ uint32_t partial[1024];
-  const int nkeys = 3 * ncb * kSortEBins;
+  const int nkeys = 3 * ncb * neb;
   const int per = (nkeys + blockDim.x - 1) / blockDim.x;
   const int b = threadIdx.x * per;
   uint32_t s = 0;
@@ -146,21 +153,24 @@ __global__ void __launch_bounds__(1024) sort_scan_kernel(const Work w, int ncb) 
   __syncthreads();
   if (threadIdx.x < 3) {
     uint32_t c = 0;
-    for (int k = threadIdx.x * ncb * kSortEBins; k < (threadIdx.x + 1) * ncb * kSortEBins; ++k) c += w.hist[k];
+    for (int k = threadIdx.x * ncb * neb; k < (threadIdx.x + 1) * ncb * neb; ++k) c += w.hist[k];
     w.counts[threadIdx.x] = c;
   }
 }
 
 __global__ void __launch_bounds__(256) sort_scatter_kernel(const __grid_constant__ DevTables T, int64_t n,
-                                                           const hepem_track_state in, const Work w, int ncb) {
+                                                           const int32_t* __restrict__ active,
+                                                           const hepem_track_state in, const Work w, int ncb,
+                                                           int neb) {
   for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = base + threadIdx.x;
+    const int64_t j = base + threadIdx.x;
+    const int64_t i = (active && j < n) ? (int64_t)active[j] : j;
     int key = -1;
-    if (i < n) {
+    if (j < n) {
       const int type = in.type[i];
       const int imc = in.imc[i];
       const double e = in.ekin[i];
-      if (!track_input_bad(T, type, imc, e)) key = sort_key(type, imc, e, ncb);
+      if (!track_input_bad(T, type, imc, e)) key = sort_key(type, imc, e, ncb, neb);
     }
     // warp-aggregated: one atomic per distinct key in the warp
     const unsigned same = __match_any_sync(0xFFFFFFFFu, key);
@@ -174,7 +184,8 @@ __global__ void __launch_bounds__(256) sort_scatter_kernel(const __grid_constant
 }
 
 // ---- 2. stage A -----------------------------------------------------------------------
-__global__ void __launch_bounds__(256) stage_a_charged_kernel(const __grid_constant__ DevTables T,
+template <int BS>
+__global__ void __launch_bounds__(BS) stage_a_charged_kernel(const __grid_constant__ DevTables T,
                                                               const hepem_track_state in, const hepem_track_state out,
                                                               const double* __restrict__ uniforms, int nu,
                                                               uint64_t seed, const hepem_step_out res, const Work w,
@@ -191,7 +202,7 @@ __global__ void __launch_bounds__(256) stage_a_charged_kernel(const __grid_const
       const int type = j < nEm ? 0 : 1;
       Track t;
       Rng rng;
-      load_track(in, idx, t, rng, uniforms, nu, seed, type);
+      load_track(in, idx, t, rng, uniforms, nu, key_of(w, idx, seed), type);
       const int32_t c0 = rng.cursor;
       Physics P{T, rng, t};
       P.el_howfar();
@@ -208,7 +219,8 @@ __global__ void __launch_bounds__(256) stage_a_charged_kernel(const __grid_const
   add_counters(cnt, counters);
 }
 
-__global__ void __launch_bounds__(256) stage_a_gamma_kernel(const __grid_constant__ DevTables T,
+template <int BS>
+__global__ void __launch_bounds__(BS) stage_a_gamma_kernel(const __grid_constant__ DevTables T,
                                                             const hepem_track_state in, const hepem_track_state out,
                                                             const double* __restrict__ uniforms, int nu,
                                                             uint64_t seed, const hepem_step_out res, const Work w,
@@ -224,7 +236,7 @@ __global__ void __launch_bounds__(256) stage_a_gamma_kernel(const __grid_constan
       idx = w.perm[w.counts[0] + w.counts[1] + j];
       Track t;
       Rng rng;
-      load_track(in, idx, t, rng, uniforms, nu, seed, 2);
+      load_track(in, idx, t, rng, uniforms, nu, key_of(w, idx, seed), 2);
       const int32_t c0 = rng.cursor;
       Physics P{T, rng, t};
       t.isEl = false;
@@ -254,8 +266,8 @@ __global__ void __launch_bounds__(256) stage_a_gamma_kernel(const __grid_constan
 }
 
 // ---- 3. stage B: one interaction model per kernel ------------------------------------------
-template <int Q>
-__global__ void __launch_bounds__(256) stage_b_kernel(const __grid_constant__ DevTables T,
+template <int Q, int BS>
+__global__ void __launch_bounds__(BS) stage_b_kernel(const __grid_constant__ DevTables T,
                                                       const hepem_track_state in, const hepem_track_state out,
                                                       const double* __restrict__ uniforms, int nu, uint64_t seed,
                                                       const hepem_step_out res, const Work w,
@@ -280,7 +292,7 @@ __global__ void __launch_bounds__(256) stage_b_kernel(const __grid_constant__ De
     rng.cursor = out.rng_cursor[i];
     rng.id = in.id[i];
     rng.overflow = 0u;
-    rng.seed = seed;
+    rng.seed = key_of(w, i, seed);
     rng.gaussValid = out.gauss_valid[i] != 0;
     rng.gaussValue = out.gauss_value[i];
     const int32_t c0 = rng.cursor;
@@ -319,71 +331,109 @@ __global__ void __launch_bounds__(256) stage_b_kernel(const __grid_constant__ De
 }
 
 // ---- host side -------------------------------------------------------------------------------
-template <class K>
-static int grid_of(K kernel, int sms) {
-  int per = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 256, 0) != cudaSuccess || per < 1) per = 1;
-  return sms * per;
+// The eleven stage kernels share one signature; each exists for 128, 256 and
+// 512 threads per block, and the launch configuration picks one of them and
+// the number of CTAs per SM for every kernel.
+using StageFn = void (*)(DevTables, hepem_track_state, hepem_track_state, const double*, int, uint64_t,
+                         hepem_step_out, Work, hepem_step_counters*);
+constexpr int kBlockSizes[3] = {128, 256, 512};
+
+static int bs_index(int bs) { return bs == 128 ? 0 : (bs == 512 ? 2 : 1); }
+
+template <int BS>
+static void stage_table(StageFn* f) {
+  f[0] = stage_a_charged_kernel<BS>;
+  f[1] = stage_a_gamma_kernel<BS>;
+  f[2] = stage_b_kernel<0, BS>;
+  f[3] = stage_b_kernel<1, BS>;
+  f[4] = stage_b_kernel<2, BS>;
+  f[5] = stage_b_kernel<3, BS>;
+  f[6] = stage_b_kernel<4, BS>;
+  f[7] = stage_b_kernel<5, BS>;
+  f[8] = stage_b_kernel<6, BS>;
+  f[9] = stage_b_kernel<7, BS>;
+  f[10] = stage_b_kernel<8, BS>;
+}
+
+struct StageKernels {
+  StageFn fn[3][kNumStageKernels];
+  int occ[3][kNumStageKernels];  // resident CTAs per SM
+};
+
+// kernel table and occupancies (thread-safe one-time initialisation)
+static const StageKernels& stage_kernels() {
+  static const StageKernels K = [] {
+    StageKernels r;
+    stage_table<128>(r.fn[0]);
+    stage_table<256>(r.fn[1]);
+    stage_table<512>(r.fn[2]);
+    for (int b = 0; b < 3; ++b)
+      for (int k = 0; k < kNumStageKernels; ++k) {
+        int per = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, r.fn[b][k], kBlockSizes[b], 0) != cudaSuccess ||
+            per < 1)
+          per = 1;
+        r.occ[b][k] = per;
+      }
+    return r;
+  }();
+  return K;
+}
+
+int stage_occupancy(int kernel, int block) { return stage_kernels().occ[bs_index(block)][kernel]; }
+
+LaunchCfg default_launch_cfg() {
+  LaunchCfg c;
+  for (int k = 0; k < kNumStageKernels; ++k) {
+    c.block[k] = 256;
+    c.ctasPerSM[k] = 0;
+  }
+  c.sortEBins = kMaxSortEBins;
+  return c;
+}
+
+bool valid_launch_cfg(const LaunchCfg& c) {
+  for (int k = 0; k < kNumStageKernels; ++k) {
+    if (c.block[k] != 128 && c.block[k] != 256 && c.block[k] != 512) return false;
+    if (c.ctasPerSM[k] < 0 || c.ctasPerSM[k] > 64) return false;
+  }
+  return c.sortEBins == 8 || c.sortEBins == 16 || c.sortEBins == 32;
 }
 
 cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track_state& in,
                                 const hepem_track_state& out, const double* uniforms, int nu, uint64_t seed,
                                 const hepem_step_out& res, hepem_step_counters* counters, void* workspace,
-                                cudaStream_t s, int sms, cudaEvent_t* ev) {
+                                cudaStream_t s, int sms, const BatchOpts& o) {
   if (n <= 0) return cudaSuccess;
-  static int gA = 0, gG = 0, gB[kNumQueues] = {};
-  if (!gA) {
-    gA = grid_of(stage_a_charged_kernel, sms);
-    gG = grid_of(stage_a_gamma_kernel, sms);
-    gB[0] = grid_of(stage_b_kernel<0>, sms);
-    gB[1] = grid_of(stage_b_kernel<1>, sms);
-    gB[2] = grid_of(stage_b_kernel<2>, sms);
-    gB[3] = grid_of(stage_b_kernel<3>, sms);
-    gB[4] = grid_of(stage_b_kernel<4>, sms);
-    gB[5] = grid_of(stage_b_kernel<5>, sms);
-    gB[6] = grid_of(stage_b_kernel<6>, sms);
-    gB[7] = grid_of(stage_b_kernel<7>, sms);
-    gB[8] = grid_of(stage_b_kernel<8>, sms);
-  }
-  const Work w = carve(workspace, n);
+  const StageKernels& K = stage_kernels();
+  static const LaunchCfg kDefault = default_launch_cfg();
+  const LaunchCfg& cfg = o.cfg ? *o.cfg : kDefault;
+  Work w = carve(workspace, n);
+  w.seeds = o.seeds;
   const int ncb = T.nCouples < kSortCoupleBins ? T.nCouples : kSortCoupleBins;
-  const int nkeys = 3 * ncb * kSortEBins;
+  const int neb = cfg.sortEBins;
+  const int nkeys = 3 * ncb * neb;
   cudaError_t e = cudaMemsetAsync(w.counts, 0, 64 * sizeof(uint32_t), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(w.hist, 0, nkeys * sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
   int k = 0;
   auto mark = [&]() {
-    if (ev) cudaEventRecord(ev[k++], s);
+    if (o.ev) cudaEventRecord(o.ev[k++], s);
   };
   const int64_t blocks = (n + 255) / 256;
   const int gC = (int)(blocks < (int64_t)sms * 8 ? blocks : (int64_t)sms * 8);
   mark();
-  sort_hist_kernel<<<gC, 256, nkeys * sizeof(uint32_t), s>>>(T, n, in, out, res, w, ncb, counters);
-  sort_scan_kernel<<<1, 1024, 0, s>>>(w, ncb);
-  sort_scatter_kernel<<<gC, 256, 0, s>>>(T, n, in, w, ncb);
+  sort_hist_kernel<<<gC, 256, nkeys * sizeof(uint32_t), s>>>(T, n, o.active, in, out, res, w, ncb, neb, counters);
+  sort_scan_kernel<<<1, 1024, 0, s>>>(w, ncb, neb);
+  sort_scatter_kernel<<<gC, 256, 0, s>>>(T, n, o.active, in, w, ncb, neb);
   mark();
-  stage_a_charged_kernel<<<gA, 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
-  mark();
-  stage_a_gamma_kernel<<<gG, 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
-  mark();
-  stage_b_kernel<0><<<gB[0], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
-  mark();
-  stage_b_kernel<1><<<gB[1], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
-  mark();
-  stage_b_kernel<2><<<gB[2], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
-  mark();
-  stage_b_kernel<3><<<gB[3], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
-  mark();
-  stage_b_kernel<4><<<gB[4], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
-  mark();
-  stage_b_kernel<5><<<gB[5], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
-  mark();
-  stage_b_kernel<6><<<gB[6], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
-  mark();
-  stage_b_kernel<7><<<gB[7], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
-  mark();
-  stage_b_kernel<8><<<gB[8], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
-  mark();
+  for (int q = 0; q < kNumStageKernels; ++q) {
+    const int b = bs_index(cfg.block[q]);
+    const int occ = K.occ[b][q];
+    const int per = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < occ ? cfg.ctasPerSM[q] : occ;
+    K.fn[b][q]<<<sms * per, kBlockSizes[b], 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+    mark();
+  }
   return cudaGetLastError();
 }
 

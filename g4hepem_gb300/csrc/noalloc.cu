@@ -80,8 +80,10 @@ extern "C" int hepem_step_batched_noalloc(const hepem_ctx* c, int64_t n, const h
   void* ws = nullptr;
   const int rc = scratch_address(&ws);
   if (rc != HEPEM_OK) return rc;
+  hepem::BatchOpts o;
+  o.cfg = &c->launch;
   const cudaError_t e = hepem::launch_step_batched(c->tables, n, *in, *out, uniforms, nu, seed, *res, counters, ws,
-                                                   (cudaStream_t)stream, c->sms, nullptr);
+                                                   (cudaStream_t)stream, c->sms, o);
   if (e != cudaSuccess)
     return hepem::set_error(HEPEM_CUDA_ERROR, std::string("batched step launch: ") + cudaGetErrorString(e));
   return HEPEM_OK;

@@ -1,0 +1,617 @@
+// server.cu -- the serving form: continuous batching of event requests.
+//
+// A request is one event's batch of tracks.  The server keeps the tracks of
+// admitted requests resident in a device slot pool sized from a memory budget
+// and runs one loop on its own host thread and stream:
+//   admit   : waiting requests (FIFO) get a contiguous slot range if one is
+//             free (admission by memory budget), their tracks are copied in;
+//   collect : one kernel compacts the alive tracks (E >= min_energy) of all
+//             active requests into an index list and counts them per request;
+//   step    : one batched step (kernels_batched.cu) over that list: requests
+//             that arrived while others were running join the same launch;
+//   account : per-track sums of deposited energy and secondaries;
+//   retire  : requests with no alive track or at their step budget are
+//             reduced (one block per request, fixed order), copied out, and
+//             their slots are freed.
+// Each track's uniform stream is Philox keyed by its request's seed and
+// counted by its index in the request, and every per-request sum is reduced in
+// a fixed order, so a request's result is the same alone and in any mix.
+// Waits are bounded: hepem_server_wait gives up with HEPEM_TIMEOUT.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "ctx.h"
+#include "g4hepem_gb300.h"
+#include "kernels.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+double now_s() { return std::chrono::duration<double>(Clock::now().time_since_epoch()).count(); }
+
+const size_t kStateSizes[20] = {1, 4, 4, 8, 8, 8, 8, 8, 8, 8, 8, 8, 1, 8, 8, 8, 1, 1, 8, 4};
+const size_t kOutSizes[14] = {8, 8, 8, 1, 8, 8, 8, 1, 1, 2, 16, 16, 16, 16};
+
+// bytes of pool memory per resident track: state, results, RNG key, owner,
+// accumulators, active index and the batched-step workspace share
+size_t bytes_per_slot() {
+  size_t b = 0;
+  for (size_t x : kStateSizes) b += x;
+  for (size_t x : kOutSizes) b += x;
+  return b + 8 + 4 + 8 + 8 + 4 + 4 + 48;
+}
+
+struct Request {
+  int64_t id = 0;
+  int64_t n = 0;
+  uint64_t seed = 0;
+  int64_t slot0 = -1;
+  int32_t steps = 0;
+  int32_t status = HEPEM_OK;
+  bool done = false;
+  std::atomic<bool> cancelled{false};
+  double tSubmit = 0, tAdmit = 0, tDone = 0;
+  std::vector<uint8_t> host;       // 20 state arrays back to back (input, then final state)
+  hepem_request_result result{};
+};
+
+// ---- kernels -----------------------------------------------------------------------
+// alive tracks of active requests -> index list; per-request alive counts
+__global__ void collect_kernel(int64_t nreq, const int64_t* __restrict__ slot0, const int64_t* __restrict__ off, int64_t total, const double* __restrict__ ekin,
+                               double minE, int32_t* __restrict__ active, uint32_t* __restrict__ nActive,
+                               uint32_t* __restrict__ aliveReq) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+    // request r owns flat positions [off[r], off[r+1])
+    int64_t lo = 0, hi = nreq - 1;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi + 1) / 2;
+      if (off[mid] <= g) lo = mid; else hi = mid - 1;
+    }
+    const int64_t slot = slot0[lo] + (g - off[lo]);
+    if (ekin[slot] > minE) {
+      const uint32_t p = atomicAdd(nActive, 1u);
+      active[p] = (int32_t)slot;
+      atomicAdd(&aliveReq[lo], 1u);
+    }
+  }
+}
+
+// per-track sums of the step just taken
+__global__ void account_kernel(const int32_t* __restrict__ active, const uint32_t* __restrict__ nActive,
+                               const hepem_step_out res, double* __restrict__ edepSum,
+                               double* __restrict__ eSecSum, int32_t* __restrict__ nSecSum,
+                               int32_t* __restrict__ stepSum) {
+  const uint32_t n = *nActive;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int32_t i = active[j];
+    edepSum[i] += res.edep[i];
+    const int ns = res.n_sec[i];
+    double es = 0.0;
+    for (int k = 0; k < ns && k < 2; ++k) es += res.sec_ekin[2 * (int64_t)i + k];
+    eSecSum[i] += es;
+    nSecSum[i] += ns;
+    stepSum[i] += 1;
+  }
+}
+
+// fixed-order reduction of one request's slot range (one block per request)
+__global__ void reduce_kernel(const int64_t* __restrict__ slot0, const int64_t* __restrict__ cnt,
+                              const double* __restrict__ edepSum, const double* __restrict__ eSecSum,
+                              const int32_t* __restrict__ nSecSum, const int32_t* __restrict__ stepSum,
+                              double* __restrict__ outD, int64_t* __restrict__ outI) {
+  __shared__ double sd[256], se[256];
+  __shared__ long long sn[256], ss[256];
+  const int64_t a = slot0[blockIdx.x], m = cnt[blockIdx.x];
+  double d = 0.0, e = 0.0;
+  long long ns = 0, st = 0;
+  for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
+    d += edepSum[a + k];
+    e += eSecSum[a + k];
+    ns += nSecSum[a + k];
+    st += stepSum[a + k];
+  }
+  sd[threadIdx.x] = d; se[threadIdx.x] = e; sn[threadIdx.x] = ns; ss[threadIdx.x] = st;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      sd[threadIdx.x] += sd[threadIdx.x + w];
+      se[threadIdx.x] += se[threadIdx.x + w];
+      sn[threadIdx.x] += sn[threadIdx.x + w];
+      ss[threadIdx.x] += ss[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    outD[2 * blockIdx.x] = sd[0];
+    outD[2 * blockIdx.x + 1] = se[0];
+    outI[2 * blockIdx.x] = sn[0];
+    outI[2 * blockIdx.x + 1] = ss[0];
+  }
+}
+
+__global__ void fill_seed_kernel(uint64_t* __restrict__ seeds, int64_t a, int64_t m, uint64_t seed,
+                                 double* __restrict__ d0, double* __restrict__ d1, int32_t* __restrict__ i0,
+                                 int32_t* __restrict__ i1) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m; k += (int64_t)gridDim.x * blockDim.x) {
+    seeds[a + k] = seed;
+    d0[a + k] = 0.0;
+    d1[a + k] = 0.0;
+    i0[a + k] = 0;
+    i1[a + k] = 0;
+  }
+}
+
+}  // namespace
+
+struct hepem_server {
+  const hepem_ctx* ctx = nullptr;
+  hepem_server_config cfg{};
+  int64_t capacity = 0;
+  cudaStream_t stream = nullptr;
+  // pool
+  void* pool = nullptr;
+  hepem_track_state st{};
+  hepem_step_out res{};
+  uint64_t* seeds = nullptr;
+  double* edepSum = nullptr;
+  double* eSecSum = nullptr;
+  int32_t* nSecSum = nullptr;
+  int32_t* stepSum = nullptr;
+  int32_t* active = nullptr;
+  void* work = nullptr;
+  // per-iteration request tables (device + pinned host mirrors)
+  int64_t maxReq = 0;
+  size_t tableBytes = 0;
+  int64_t *dSlot0 = nullptr, *dCnt = nullptr, *dOff = nullptr, *dOutI = nullptr;
+  double* dOutD = nullptr;
+  uint32_t *dNActive = nullptr, *dAlive = nullptr;
+  int64_t *hSlot0 = nullptr, *hCnt = nullptr, *hOff = nullptr, *hOutI = nullptr;
+  double* hOutD = nullptr;
+  uint32_t *hNActive = nullptr, *hAlive = nullptr;
+  // free slot ranges: start -> length
+  std::map<int64_t, int64_t> freeRanges;
+  // requests
+  std::mutex mu;
+  std::condition_variable cv, cvDone;
+  std::deque<int64_t> waiting;
+  std::vector<int64_t> activeReq;
+  std::unordered_map<int64_t, std::unique_ptr<Request>> reqs;
+  int64_t nextId = 1;
+  std::atomic<bool> stop{false};
+  std::thread loop;
+  int32_t loopError = HEPEM_OK;
+  std::string loopErrorMsg;
+  // statistics
+  std::vector<double> batchMs;
+  int64_t iterations = 0, trackSteps = 0, completed = 0;
+
+  int64_t alloc_slots(int64_t n) {
+    for (auto it = freeRanges.begin(); it != freeRanges.end(); ++it) {
+      if (it->second >= n) {
+        const int64_t a = it->first, len = it->second;
+        freeRanges.erase(it);
+        if (len > n) freeRanges[a + n] = len - n;
+        return a;
+      }
+    }
+    return -1;
+  }
+  void free_slots(int64_t a, int64_t n) {
+    auto it = freeRanges.emplace(a, n).first;
+    auto nx = std::next(it);
+    if (nx != freeRanges.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      freeRanges.erase(nx);
+    }
+    if (it != freeRanges.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        freeRanges.erase(it);
+      }
+    }
+  }
+  void* state_ptr(int k, int64_t slot) const {
+    return (uint8_t*)(reinterpret_cast<void* const*>(&st)[k]) + kStateSizes[k] * slot;
+  }
+  void run();
+  cudaError_t iterate();
+};
+
+#define SRV_CUDA(call)                  \
+  do {                                  \
+    cudaError_t e_ = (call);            \
+    if (e_ != cudaSuccess) return e_;   \
+  } while (0)
+
+cudaError_t hepem_server::iterate() {
+  std::vector<Request*> admitted;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    while (!waiting.empty() && (int64_t)activeReq.size() < maxReq) {
+      Request* r = reqs[waiting.front()].get();
+      const int64_t a = alloc_slots(r->n);
+      if (a < 0) break;                        // wait for memory (FIFO: no overtaking)
+      waiting.pop_front();
+      r->slot0 = a;
+      r->tAdmit = now_s();
+      admitted.push_back(r);
+      activeReq.push_back(r->id);
+    }
+  }
+  for (Request* r : admitted) {
+    size_t o = 0;
+    for (int k = 0; k < 20; ++k) {
+      SRV_CUDA(cudaMemcpyAsync(state_ptr(k, r->slot0), r->host.data() + o, kStateSizes[k] * r->n,
+                               cudaMemcpyHostToDevice, stream));
+      o += kStateSizes[k] * r->n;
+    }
+    fill_seed_kernel<<<std::max<int64_t>(1, std::min<int64_t>((r->n + 255) / 256, 1024)), 256, 0, stream>>>(
+        seeds, r->slot0, r->n, r->seed, edepSum, eSecSum, nSecSum, stepSum);
+    SRV_CUDA(cudaGetLastError());
+  }
+  std::vector<Request*> act;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    for (int64_t id : activeReq) act.push_back(reqs[id].get());
+  }
+  if (act.empty()) return cudaSuccess;
+  const double t0 = now_s();
+  const int64_t nr = (int64_t)act.size();
+  int64_t total = 0;
+  for (int64_t k = 0; k < nr; ++k) {
+    hSlot0[k] = act[k]->slot0;
+    hCnt[k] = act[k]->n;
+    hOff[k] = total;
+    total += act[k]->n;
+  }
+  hOff[nr] = total;
+  SRV_CUDA(cudaMemcpyAsync(dSlot0, hSlot0, sizeof(int64_t) * nr, cudaMemcpyHostToDevice, stream));
+  SRV_CUDA(cudaMemcpyAsync(dCnt, hCnt, sizeof(int64_t) * nr, cudaMemcpyHostToDevice, stream));
+  SRV_CUDA(cudaMemcpyAsync(dOff, hOff, sizeof(int64_t) * (nr + 1), cudaMemcpyHostToDevice, stream));
+  SRV_CUDA(cudaMemsetAsync(dNActive, 0, sizeof(uint32_t), stream));
+  SRV_CUDA(cudaMemsetAsync(dAlive, 0, sizeof(uint32_t) * nr, stream));
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)ctx->sms * 16));
+  collect_kernel<<<g, 256, 0, stream>>>(nr, dSlot0, dOff, total, st.ekin, cfg.min_energy, active, dNActive,
+                                        dAlive);
+  SRV_CUDA(cudaGetLastError());
+  SRV_CUDA(cudaMemcpyAsync(hNActive, dNActive, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+  SRV_CUDA(cudaStreamSynchronize(stream));
+  const int64_t nAct = *hNActive;
+  if (nAct > 0) {
+    hepem::BatchOpts o;
+    o.active = active;
+    o.seeds = seeds;
+    o.cfg = &ctx->launch;
+    SRV_CUDA(hepem::launch_step_batched(ctx->tables, nAct, st, st, nullptr, 0, 0, res, nullptr, work, stream,
+                                        ctx->sms, o));
+    account_kernel<<<g, 256, 0, stream>>>(active, dNActive, res, edepSum, eSecSum, nSecSum, stepSum);
+    SRV_CUDA(cudaGetLastError());
+  }
+  SRV_CUDA(cudaMemcpyAsync(hAlive, dAlive, sizeof(uint32_t) * nr, cudaMemcpyDeviceToHost, stream));
+  SRV_CUDA(cudaStreamSynchronize(stream));
+  // retire: nothing alive before this step, or the step budget is used up
+  std::vector<int64_t> fin;
+  for (int64_t k = 0; k < nr; ++k) {
+    Request* r = act[k];
+    if (hAlive[k] > 0) r->steps += 1;
+    if (hAlive[k] == 0 || r->steps >= cfg.max_steps || r->cancelled) fin.push_back(k);
+  }
+  if (!fin.empty()) {
+    const int64_t nf = (int64_t)fin.size();
+    for (int64_t q = 0; q < nf; ++q) {
+      hSlot0[q] = act[fin[q]]->slot0;
+      hCnt[q] = act[fin[q]]->n;
+    }
+    SRV_CUDA(cudaMemcpyAsync(dSlot0, hSlot0, sizeof(int64_t) * nf, cudaMemcpyHostToDevice, stream));
+    SRV_CUDA(cudaMemcpyAsync(dCnt, hCnt, sizeof(int64_t) * nf, cudaMemcpyHostToDevice, stream));
+    reduce_kernel<<<(unsigned)nf, 256, 0, stream>>>(dSlot0, dCnt, edepSum, eSecSum, nSecSum, stepSum, dOutD, dOutI);
+    SRV_CUDA(cudaGetLastError());
+    SRV_CUDA(cudaMemcpyAsync(hOutD, dOutD, sizeof(double) * 2 * nf, cudaMemcpyDeviceToHost, stream));
+    SRV_CUDA(cudaMemcpyAsync(hOutI, dOutI, sizeof(int64_t) * 2 * nf, cudaMemcpyDeviceToHost, stream));
+    for (int64_t q = 0; q < nf; ++q) {
+      Request* r = act[fin[q]];
+      size_t o = 0;
+      for (int k = 0; k < 20; ++k) {
+        SRV_CUDA(cudaMemcpyAsync(r->host.data() + o, state_ptr(k, r->slot0), kStateSizes[k] * r->n,
+                                 cudaMemcpyDeviceToHost, stream));
+        o += kStateSizes[k] * r->n;
+      }
+    }
+    SRV_CUDA(cudaStreamSynchronize(stream));
+    const double t = now_s();
+    std::lock_guard<std::mutex> lock(mu);
+    for (int64_t q = 0; q < nf; ++q) {
+      Request* r = act[fin[q]];
+      r->result.n_tracks = r->n;
+      r->result.steps = r->steps;
+      r->result.status = r->cancelled ? HEPEM_CANCELLED : HEPEM_OK;
+      r->result.edep = hOutD[2 * q];
+      r->result.e_secondaries = hOutD[2 * q + 1];
+      r->result.n_secondaries = hOutI[2 * q];
+      r->result.track_steps = hOutI[2 * q + 1];
+      r->result.t_submit = r->tSubmit;
+      r->result.t_admit = r->tAdmit;
+      r->result.t_done = t;
+      r->done = true;
+      free_slots(r->slot0, r->n);
+      activeReq.erase(std::find(activeReq.begin(), activeReq.end(), r->id));
+      completed += 1;
+    }
+    cvDone.notify_all();
+  }
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (batchMs.size() >= (size_t)1 << 20) batchMs.erase(batchMs.begin(), batchMs.begin() + (1 << 19));
+    batchMs.push_back(1e3 * (now_s() - t0));
+    iterations += 1;
+    trackSteps += nAct;
+  }
+  return cudaSuccess;
+}
+
+void hepem_server::run() {
+  cudaSetDevice(ctx->device);
+  while (!stop.load()) {
+    bool idle;
+    {
+      std::unique_lock<std::mutex> lock(mu);
+      cv.wait_for(lock, std::chrono::milliseconds(5),
+                  [&] { return stop.load() || !waiting.empty() || !activeReq.empty(); });
+      idle = waiting.empty() && activeReq.empty();
+    }
+    if (idle) continue;
+    const cudaError_t e = iterate();
+    if (e != cudaSuccess) {
+      std::lock_guard<std::mutex> lock(mu);
+      loopError = HEPEM_CUDA_ERROR;
+      loopErrorMsg = cudaGetErrorString(e);
+      for (auto& kv : reqs) {
+        if (!kv.second->done) {
+          kv.second->done = true;
+          kv.second->result.status = HEPEM_CUDA_ERROR;
+        }
+      }
+      cvDone.notify_all();
+      return;
+    }
+  }
+}
+
+extern "C" {
+
+int hepem_server_create(const hepem_ctx* ctx, const hepem_server_config* cfg, hepem_server** out) {
+  if (!ctx || !cfg || !out || cfg->memory_budget_bytes <= 0 || cfg->max_steps <= 0 || cfg->max_requests <= 0)
+    return hepem::set_error(HEPEM_BAD_ARG, "bad server configuration");
+  *out = nullptr;
+  std::unique_ptr<hepem_server> s(new hepem_server());
+  s->ctx = ctx;
+  s->cfg = *cfg;
+  s->maxReq = cfg->max_requests;
+  const size_t per = bytes_per_slot();
+  const size_t fixed = hepem::batched_workspace_bytes(0) + 64 * 256;  // + rounding of ~45 arrays
+  if ((size_t)cfg->memory_budget_bytes <= fixed + per) return hepem::set_error(HEPEM_BAD_ARG, "budget too small");
+  s->capacity = (int64_t)(((size_t)cfg->memory_budget_bytes - fixed) / per);
+  if (s->capacity > (int64_t)INT32_MAX / 2) s->capacity = INT32_MAX / 2;
+  const int64_t C = s->capacity;
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  size_t bytes = 0;
+  for (size_t b : kStateSizes) bytes += al(b * C);
+  for (size_t b : kOutSizes) bytes += al(b * C);
+  bytes += al(8 * C) * 3 + al(4 * C) * 3 + al(hepem::batched_workspace_bytes(C));
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&s->pool, bytes);
+  if (e != cudaSuccess) {
+    if (s->stream) cudaStreamDestroy(s->stream);
+    return hepem::set_error(HEPEM_OOM_ADMISSION, std::string("server pool: ") + cudaGetErrorString(e));
+  }
+  uint8_t* p = (uint8_t*)s->pool;
+  void** sp = reinterpret_cast<void**>(&s->st);
+  for (int k = 0; k < 20; ++k) { sp[k] = p; p += al(kStateSizes[k] * C); }
+  void** rp = reinterpret_cast<void**>(&s->res);
+  for (int k = 0; k < 14; ++k) { rp[k] = p; p += al(kOutSizes[k] * C); }
+  s->seeds = (uint64_t*)p; p += al(8 * C);
+  s->edepSum = (double*)p; p += al(8 * C);
+  s->eSecSum = (double*)p; p += al(8 * C);
+  s->nSecSum = (int32_t*)p; p += al(4 * C);
+  s->stepSum = (int32_t*)p; p += al(4 * C);
+  s->active = (int32_t*)p; p += al(4 * C);
+  s->work = p;
+  // request tables, same layout on the device and in pinned host memory:
+  // slot0[R] cnt[R] off[R+1] outI[2R] outD[2R] nActive[1] alive[R]
+  const int64_t R = s->maxReq;
+  size_t tabOff[7];
+  {
+    const size_t sz[7] = {8 * (size_t)R, 8 * (size_t)R, 8 * (size_t)(R + 1), 16 * (size_t)R, 16 * (size_t)R, 4,
+                          4 * (size_t)R};
+    size_t o = 0;
+    for (int k = 0; k < 7; ++k) {
+      tabOff[k] = o;
+      o += al(sz[k]);
+    }
+    s->tableBytes = o;
+  }
+  uint8_t *dTab = nullptr, *hTab = nullptr;
+  e = cudaMalloc((void**)&dTab, s->tableBytes);
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&hTab, s->tableBytes);
+  if (e != cudaSuccess) {
+    cudaFree(s->pool);
+    if (dTab) cudaFree(dTab);
+    cudaStreamDestroy(s->stream);
+    return hepem::set_error(HEPEM_CUDA_ERROR, std::string("server tables: ") + cudaGetErrorString(e));
+  }
+  s->dSlot0 = (int64_t*)(dTab + tabOff[0]);
+  s->dCnt = (int64_t*)(dTab + tabOff[1]);
+  s->dOff = (int64_t*)(dTab + tabOff[2]);
+  s->dOutI = (int64_t*)(dTab + tabOff[3]);
+  s->dOutD = (double*)(dTab + tabOff[4]);
+  s->dNActive = (uint32_t*)(dTab + tabOff[5]);
+  s->dAlive = (uint32_t*)(dTab + tabOff[6]);
+  s->hSlot0 = (int64_t*)(hTab + tabOff[0]);
+  s->hCnt = (int64_t*)(hTab + tabOff[1]);
+  s->hOff = (int64_t*)(hTab + tabOff[2]);
+  s->hOutI = (int64_t*)(hTab + tabOff[3]);
+  s->hOutD = (double*)(hTab + tabOff[4]);
+  s->hNActive = (uint32_t*)(hTab + tabOff[5]);
+  s->hAlive = (uint32_t*)(hTab + tabOff[6]);
+  s->freeRanges[0] = C;
+  hepem_server* raw = s.release();
+  raw->loop = std::thread([raw] { raw->run(); });
+  *out = raw;
+  return HEPEM_OK;
+}
+
+int hepem_server_capacity(const hepem_server* s, int64_t* tracks) {
+  if (!s || !tracks) return hepem::set_error(HEPEM_BAD_ARG, "null argument");
+  *tracks = s->capacity;
+  return HEPEM_OK;
+}
+
+int hepem_server_submit(hepem_server* s, int64_t n, const hepem_track_state* tracks, uint64_t seed,
+                        int64_t* request_id) {
+  if (!s || !tracks || !request_id || n <= 0) return hepem::set_error(HEPEM_BAD_ARG, "bad request");
+  if (n > s->capacity)
+    return hepem::set_error(HEPEM_OOM_ADMISSION, "request larger than the server's memory budget");
+  if (!hepem::valid_state(tracks)) return hepem::set_error(HEPEM_BAD_ARG, "null array in track batch");
+  std::unique_ptr<Request> r(new Request());
+  r->n = n;
+  r->seed = seed;
+  size_t tot = 0;
+  for (size_t b : kStateSizes) tot += b * n;
+  r->host.resize(tot);
+  void* const* src = reinterpret_cast<void* const*>(tracks);
+  size_t o = 0;
+  for (int k = 0; k < 20; ++k) {
+    memcpy(r->host.data() + o, src[k], kStateSizes[k] * n);
+    o += kStateSizes[k] * n;
+  }
+  r->tSubmit = now_s();
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (s->loopError != HEPEM_OK) return hepem::set_error(s->loopError, "server loop stopped: " + s->loopErrorMsg);
+  r->id = s->nextId++;
+  *request_id = r->id;
+  s->waiting.push_back(r->id);
+  s->reqs[r->id] = std::move(r);
+  s->cv.notify_all();
+  return HEPEM_OK;
+}
+
+static int take_result(hepem_server* s, Request* r, hepem_request_result* result, hepem_track_state* final_tracks) {
+  if (result) *result = r->result;
+  if (final_tracks) {
+    void* const* dst = reinterpret_cast<void* const*>(final_tracks);
+    size_t o = 0;
+    for (int k = 0; k < 20; ++k) {
+      if (dst[k]) memcpy(dst[k], r->host.data() + o, kStateSizes[k] * r->n);
+      o += kStateSizes[k] * r->n;
+    }
+  }
+  const int st = r->result.status;
+  s->reqs.erase(r->id);
+  return st;
+}
+
+int hepem_server_poll(hepem_server* s, int64_t request_id, int32_t* done, hepem_request_result* result,
+                      hepem_track_state* final_tracks) {
+  if (!s || !done) return hepem::set_error(HEPEM_BAD_ARG, "null argument");
+  std::lock_guard<std::mutex> lock(s->mu);
+  auto it = s->reqs.find(request_id);
+  if (it == s->reqs.end()) return hepem::set_error(HEPEM_BAD_ARG, "unknown request id");
+  *done = it->second->done ? 1 : 0;
+  if (!it->second->done) return HEPEM_OK;
+  const int st = take_result(s, it->second.get(), result, final_tracks);
+  return st == HEPEM_OK ? HEPEM_OK : hepem::set_error(st, "request did not complete");
+}
+
+int hepem_server_wait(hepem_server* s, int64_t request_id, double timeout_s, hepem_request_result* result,
+                      hepem_track_state* final_tracks) {
+  if (!s) return hepem::set_error(HEPEM_BAD_ARG, "null server");
+  std::unique_lock<std::mutex> lock(s->mu);
+  auto it = s->reqs.find(request_id);
+  if (it == s->reqs.end()) return hepem::set_error(HEPEM_BAD_ARG, "unknown request id");
+  Request* r = it->second.get();
+  const bool ok = s->cvDone.wait_for(lock, std::chrono::duration<double>(timeout_s), [&] { return r->done; });
+  if (!ok) return hepem::set_error(HEPEM_TIMEOUT, "request not finished within the timeout");
+  const int st = take_result(s, r, result, final_tracks);
+  return st == HEPEM_OK ? HEPEM_OK : hepem::set_error(st, "request did not complete");
+}
+
+int hepem_server_cancel(hepem_server* s, int64_t request_id) {
+  if (!s) return hepem::set_error(HEPEM_BAD_ARG, "null server");
+  std::lock_guard<std::mutex> lock(s->mu);
+  auto it = s->reqs.find(request_id);
+  if (it == s->reqs.end()) return hepem::set_error(HEPEM_BAD_ARG, "unknown request id");
+  Request* r = it->second.get();
+  r->cancelled = true;
+  if (r->slot0 < 0 && !r->done) {          // still waiting: finish it now
+    s->waiting.erase(std::find(s->waiting.begin(), s->waiting.end(), request_id));
+    r->done = true;
+    r->result.n_tracks = r->n;
+    r->result.status = HEPEM_CANCELLED;
+    r->result.t_submit = r->tSubmit;
+    r->result.t_done = now_s();
+    s->cvDone.notify_all();
+  }
+  return HEPEM_OK;
+}
+
+int hepem_server_get_stats(hepem_server* s, hepem_server_stats* out) {
+  if (!s || !out) return hepem::set_error(HEPEM_BAD_ARG, "null argument");
+  std::lock_guard<std::mutex> lock(s->mu);
+  memset(out, 0, sizeof(*out));
+  out->iterations = s->iterations;
+  out->track_steps = s->trackSteps;
+  out->completed = s->completed;
+  out->waiting = (int64_t)s->waiting.size();
+  out->active = (int64_t)s->activeReq.size();
+  std::vector<double> b = s->batchMs;
+  if (!b.empty()) {
+    std::sort(b.begin(), b.end());
+    out->batch_ms_p50 = b[b.size() / 2];
+    out->batch_ms_p99 = b[std::min(b.size() - 1, (size_t)(0.99 * b.size()))];
+  }
+  int64_t freeSlots = 0;
+  for (auto& kv : s->freeRanges) freeSlots += kv.second;
+  out->free_slots = freeSlots;
+  return HEPEM_OK;
+}
+
+int hepem_server_reset_stats(hepem_server* s) {
+  if (!s) return hepem::set_error(HEPEM_BAD_ARG, "null server");
+  std::lock_guard<std::mutex> lock(s->mu);
+  s->batchMs.clear();
+  s->iterations = 0;
+  s->trackSteps = 0;
+  s->completed = 0;
+  return HEPEM_OK;
+}
+
+int hepem_server_destroy(hepem_server* s) {
+  if (!s) return HEPEM_OK;
+  s->stop.store(true);
+  s->cv.notify_all();
+  if (s->loop.joinable()) s->loop.join();
+  cudaStreamSynchronize(s->stream);
+  cudaFree(s->pool);
+  cudaFree(s->dSlot0);
+  cudaFreeHost(s->hSlot0);
+  cudaStreamDestroy(s->stream);
+  delete s;
+  return HEPEM_OK;
+}
+
+}  // extern "C"

@@ -48,10 +48,46 @@ class StepCounters(C.Structure):
                 ("secondaries", C.c_uint64), ("interactions", C.c_uint64 * 8)]
 
 
+class LaunchConfig(C.Structure):
+    _fields_ = [("block", C.c_int32 * 11), ("ctas_per_sm", C.c_int32 * 11), ("sort_energy_bins", C.c_int32),
+                ("ms", C.c_float * 11)]
+
+    def as_dict(self) -> dict:
+        return {"block": list(self.block), "ctas_per_sm": list(self.ctas_per_sm),
+                "sort_energy_bins": self.sort_energy_bins, "ms": [round(x, 4) for x in self.ms]}
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("memory_budget_bytes", C.c_int64), ("max_steps", C.c_int32), ("max_requests", C.c_int32),
+                ("min_energy", C.c_double)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("n_tracks", C.c_int64), ("steps", C.c_int32), ("status", C.c_int32), ("edep", C.c_double),
+                ("e_secondaries", C.c_double), ("n_secondaries", C.c_int64), ("track_steps", C.c_int64),
+                ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("iterations", C.c_int64), ("track_steps", C.c_int64), ("completed", C.c_int64),
+                ("waiting", C.c_int64), ("active", C.c_int64), ("free_slots", C.c_int64),
+                ("batch_ms_p50", C.c_double), ("batch_ms_p99", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 EXPORTED = ["hepem_create", "hepem_create_from_file", "hepem_destroy", "hepem_info", "hepem_status_string",
             "hepem_last_error", "hepem_electron_lookup", "hepem_step", "hepem_step_batched",
             "hepem_step_batched_noalloc", "hepem_step_host",
-            "hepem_philox_uniform", "hepem_fill_uniforms", "hepem_profile_stages", "hepem_stage_times"]
+            "hepem_philox_uniform", "hepem_fill_uniforms", "hepem_profile_stages", "hepem_stage_times",
+            "hepem_server_create", "hepem_server_capacity", "hepem_server_submit", "hepem_server_poll",
+            "hepem_server_wait", "hepem_server_cancel", "hepem_server_get_stats", "hepem_server_reset_stats",
+            "hepem_server_destroy", "hepem_get_launch_config", "hepem_set_launch_config", "hepem_autotune"]
+STATUS_CANCELLED, STATUS_TIMEOUT, STATUS_OOM_ADMISSION = 8, 5, 6
 
 
 class HepEmError(RuntimeError):
@@ -89,6 +125,21 @@ def lib():
         L.hepem_profile_stages.argtypes = [_vp, C.c_int]
         L.hepem_stage_times.argtypes = [_vp, C.POINTER(C.c_float), C.POINTER(C.c_char_p), C.c_int32,
                                         C.POINTER(C.c_int32)]
+        L.hepem_get_launch_config.argtypes = [_vp, C.POINTER(LaunchConfig)]
+        L.hepem_set_launch_config.argtypes = [_vp, C.POINTER(LaunchConfig)]
+        L.hepem_autotune.argtypes = [_vp, C.c_int64, C.POINTER(TrackState), _vp, C.c_int32, C.c_uint64, C.c_int,
+                                     C.POINTER(LaunchConfig), _vp]
+        L.hepem_server_create.argtypes = [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]
+        L.hepem_server_capacity.argtypes = [_vp, C.POINTER(C.c_int64)]
+        L.hepem_server_submit.argtypes = [_vp, C.c_int64, C.POINTER(TrackState), C.c_uint64, C.POINTER(C.c_int64)]
+        L.hepem_server_poll.argtypes = [_vp, C.c_int64, C.POINTER(C.c_int32), C.POINTER(RequestResult),
+                                        C.POINTER(TrackState)]
+        L.hepem_server_wait.argtypes = [_vp, C.c_int64, C.c_double, C.POINTER(RequestResult),
+                                        C.POINTER(TrackState)]
+        L.hepem_server_cancel.argtypes = [_vp, C.c_int64]
+        L.hepem_server_get_stats.argtypes = [_vp, C.POINTER(ServerStats)]
+        L.hepem_server_reset_stats.argtypes = [_vp]
+        L.hepem_server_destroy.argtypes = [_vp]
         _LIB = L
     return _LIB
 
@@ -180,6 +231,33 @@ class Context:
                  _ptr(counters) if counters is not None else None, _stream_ptr(stream)))
 
     # -- host-buffer entry point (numpy arrays) ----------------------------------
+    # -- launch configuration of the batched form ----------------------------------
+    def launch_config(self) -> dict:
+        c = LaunchConfig()
+        check(lib().hepem_get_launch_config(self.h, C.byref(c)))
+        return c.as_dict()
+
+    def set_launch_config(self, cfg: dict | None):
+        if cfg is None:
+            check(lib().hepem_set_launch_config(self.h, None))
+            return
+        c = LaunchConfig()
+        for k in range(11):
+            c.block[k] = cfg["block"][k]
+            c.ctas_per_sm[k] = cfg["ctas_per_sm"][k]
+        c.sort_energy_bins = cfg["sort_energy_bins"]
+        check(lib().hepem_set_launch_config(self.h, C.byref(c)))
+
+    def autotune(self, state_in: dict, uniforms, n_uniform: int, seed: int, apply=True, stream=None) -> dict:
+        """Times the batched step on this batch under every launch candidate;
+        returns the fastest configuration (and applies it if `apply`)."""
+        n = len(state_in["ekin"])
+        sin = make_state_struct(state_in)
+        c = LaunchConfig()
+        check(lib().hepem_autotune(self.h, n, C.byref(sin), _ptr(uniforms) if n_uniform else None, n_uniform, seed,
+                                   int(apply), C.byref(c), _stream_ptr(stream)))
+        return c.as_dict()
+
     def step_host(self, state_in: dict, state_out: dict, uniforms: np.ndarray, n_uniform: int, seed: int,
                   res: dict, stream=None):
         n = len(state_in["ekin"])
@@ -188,6 +266,88 @@ class Context:
         check(lib().hepem_step_host(self.h, n, C.byref(sin), C.byref(sout), _ptr(uniforms), n_uniform, seed,
                                     C.byref(sres), C.byref(cnt), _stream_ptr(stream)))
         return cnt
+
+
+class Server:
+    """Serving form: continuous batching of event requests (hepem_server_*).
+
+    Requests are host SoA track batches (numpy dicts of STATE_FIELDS); results
+    are RequestResult dicts, and optionally the final track state."""
+
+    def __init__(self, ctx: Context, memory_budget_bytes: int, max_steps: int = 1000, max_requests: int = 4096,
+                 min_energy: float = 1.0e-3):
+        self.ctx = ctx
+        cfg = ServerConfig(int(memory_budget_bytes), int(max_steps), int(max_requests), float(min_energy))
+        h = _vp()
+        check(lib().hepem_server_create(ctx.h, C.byref(cfg), C.byref(h)))
+        self.h = h
+        self._keep = {}
+
+    @property
+    def capacity(self) -> int:
+        c = C.c_int64()
+        check(lib().hepem_server_capacity(self.h, C.byref(c)))
+        return c.value
+
+    def submit(self, tracks: dict, seed: int) -> int:
+        n = len(tracks["ekin"])
+        arrs = {f: np.ascontiguousarray(tracks[f], dtype=dt) for f, dt in STATE_FIELDS}
+        st = make_state_struct(arrs)
+        rid = C.c_int64()
+        check(lib().hepem_server_submit(self.h, n, C.byref(st), seed, C.byref(rid)))
+        self._keep[rid.value] = n
+        return rid.value
+
+    def _final(self, rid, want_tracks):
+        if not want_tracks:
+            return None, None
+        n = self._keep[rid]
+        arrs = {f: np.zeros(n, dtype=dt) for f, dt in STATE_FIELDS}
+        return arrs, make_state_struct(arrs)
+
+    def poll(self, rid: int, want_tracks: bool = False):
+        """None while running, else (result dict, final tracks or None)."""
+        done = C.c_int32()
+        res = RequestResult()
+        arrs, st = self._final(rid, want_tracks)
+        rc = lib().hepem_server_poll(self.h, rid, C.byref(done), C.byref(res), C.byref(st) if st else None)
+        if rc not in (0, STATUS_CANCELLED):
+            check(rc)
+        if not done.value:
+            return None
+        self._keep.pop(rid, None)
+        return res.as_dict(), arrs
+
+    def wait(self, rid: int, timeout_s: float = 600.0, want_tracks: bool = False):
+        res = RequestResult()
+        arrs, st = self._final(rid, want_tracks)
+        rc = lib().hepem_server_wait(self.h, rid, timeout_s, C.byref(res), C.byref(st) if st else None)
+        if rc not in (0, STATUS_CANCELLED):
+            check(rc)
+        self._keep.pop(rid, None)
+        return res.as_dict(), arrs
+
+    def cancel(self, rid: int):
+        check(lib().hepem_server_cancel(self.h, rid))
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        check(lib().hepem_server_get_stats(self.h, C.byref(s)))
+        return s.as_dict()
+
+    def reset_stats(self):
+        check(lib().hepem_server_reset_stats(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().hepem_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def philox_uniform(seed: int, tid: int, k: int) -> float:

@@ -48,7 +48,8 @@ enum {
   HEPEM_RNG_EXHAUSTED = 4,  /* informational: some track read past n_uniform  */
   HEPEM_TIMEOUT       = 5,  /* a bounded wait gave up                          */
   HEPEM_OOM_ADMISSION = 6,  /* serving: request does not fit the memory budget */
-  HEPEM_NO_DEVICE     = 7   /* no CUDA device visible                         */
+  HEPEM_NO_DEVICE     = 7,  /* no CUDA device visible                         */
+  HEPEM_CANCELLED     = 8   /* serving: the request was cancelled             */
 };
 
 typedef struct hepem_ctx hepem_ctx;
@@ -202,6 +203,31 @@ int  hepem_profile_stages(hepem_ctx* ctx, int enable);
 int  hepem_stage_times(hepem_ctx* ctx, float* ms, const char** names, int32_t max,
                        int32_t* count);
 
+/* ---- launch configuration of the batched form and its autotuner ---------- */
+/* The batched form runs eleven stage kernels (index: 0 e+- stage A, 1 gamma
+ * stage A, 2..10 the interaction kernels in the order of hepem_stage_times).
+ * Each runs with 128, 256 or 512 threads per block and 1..occupancy CTAs per
+ * SM; e+- tracks are sorted into 8, 16 or 32 energy bins per couple.  Results
+ * do not depend on the configuration (bit-identical).  No reference
+ * counterpart: the reference has no batched form. */
+typedef struct hepem_launch_config {
+  int32_t block[11];          /* threads per block: 128, 256 or 512            */
+  int32_t ctas_per_sm[11];    /* 0 = as many as fit                            */
+  int32_t sort_energy_bins;   /* 8, 16 or 32                                   */
+  float   ms[11];             /* per-kernel time found by hepem_autotune       */
+} hepem_launch_config;
+int  hepem_get_launch_config(const hepem_ctx* ctx, hepem_launch_config* out);
+/* cfg NULL restores the default (256 threads, occupancy grid, 32 bins).  Set
+ * it before the context is shared between threads. */
+int  hepem_set_launch_config(hepem_ctx* ctx, const hepem_launch_config* cfg);
+/* Times the batched step on the caller's batch (device pointers; the batch is
+ * read, outputs go to scratch) under every candidate configuration and returns
+ * the fastest in `out`; apply != 0 also makes it the context's configuration.
+ * Synchronises the stream. */
+int  hepem_autotune(hepem_ctx* ctx, int64_t n, const hepem_track_state* in,
+                    const double* uniforms, int32_t n_uniform, uint64_t seed,
+                    int apply, hepem_launch_config* out, void* stream);
+
 /* ---- RNG stream helpers --------------------------------------------------- */
 /* Philox4x32-10 (Salmon et al., SC'11) uniform in (0,1): counter
  * (k>>1, id, 0, 0x48455045), key (seed lo, seed hi); 52 random bits. */
@@ -210,6 +236,66 @@ double hepem_philox_uniform(uint64_t seed, int32_t id, int32_t k);
  * device (ids: device pointer). */
 int  hepem_fill_uniforms(int64_t n, const int32_t* id, int32_t n_uniform,
                          uint64_t seed, double* uniforms, void* stream);
+
+/* ---- serving form: continuous batching of event requests ------------------- */
+/* A request is one event's track batch (host SoA).  The server keeps the
+ * tracks of admitted requests resident on the device, steps all of them in
+ * one batched step per iteration (requests that arrive while others run join
+ * the next iteration), and retires a request when none of its tracks is above
+ * min_energy or after max_steps iterations.  Admission is first-come
+ * first-served by the memory budget: a request waits until a contiguous slot
+ * range of its size is free.  Each track draws pure Philox uniforms keyed by
+ * the request's seed and the track's id, and every per-request sum is reduced
+ * in a fixed order, so a request's result does not depend on the mix.
+ * Reference counterpart: the per-event stepping loop of the TestEm3 tracking
+ * (apps/examples/TestEm3/src/G4HepEmProcess.cc:144-197 called per step by
+ * Geant4), here for many events at once; the reference has no server. */
+typedef struct hepem_server hepem_server;
+
+typedef struct hepem_server_config {
+  int64_t memory_budget_bytes;  /* device memory for resident tracks + workspace */
+  int32_t max_steps;            /* step budget of a request (iterations)         */
+  int32_t max_requests;         /* requests resident at once                     */
+  double  min_energy;           /* a track is alive while ekin > min_energy (MeV) */
+} hepem_server_config;
+
+typedef struct hepem_request_result {
+  int64_t n_tracks;
+  int32_t steps;                /* iterations the request took part in          */
+  int32_t status;               /* HEPEM_OK, HEPEM_CANCELLED or HEPEM_CUDA_ERROR */
+  double  edep;                 /* sum of deposited energy over tracks and steps */
+  double  e_secondaries;        /* sum of secondary kinetic energies             */
+  int64_t n_secondaries;
+  int64_t track_steps;          /* sum over tracks of the steps taken            */
+  double  t_submit, t_admit, t_done;  /* steady-clock seconds                    */
+} hepem_request_result;
+
+typedef struct hepem_server_stats {
+  int64_t iterations, track_steps, completed, waiting, active, free_slots;
+  double  batch_ms_p50, batch_ms_p99;  /* wall time of one iteration            */
+} hepem_server_stats;
+
+/* Starts the server thread; capacity (tracks) follows from the budget. */
+int  hepem_server_create(const hepem_ctx* ctx, const hepem_server_config* cfg,
+                         hepem_server** out);
+int  hepem_server_capacity(const hepem_server* s, int64_t* tracks);
+/* Copies the batch; HEPEM_OOM_ADMISSION if n exceeds the whole capacity. */
+int  hepem_server_submit(hepem_server* s, int64_t n, const hepem_track_state* tracks,
+                         uint64_t seed, int64_t* request_id);
+/* done = 1 when finished; then result (and, if not NULL, the final track
+ * state, host arrays of n) are filled and the request is forgotten. */
+int  hepem_server_poll(hepem_server* s, int64_t request_id, int32_t* done,
+                       hepem_request_result* result, hepem_track_state* final_tracks);
+/* Waits at most timeout_s seconds (HEPEM_TIMEOUT otherwise), then as poll. */
+int  hepem_server_wait(hepem_server* s, int64_t request_id, double timeout_s,
+                       hepem_request_result* result, hepem_track_state* final_tracks);
+/* A waiting request finishes at once; an admitted one at the next iteration;
+ * either way with status HEPEM_CANCELLED. */
+int  hepem_server_cancel(hepem_server* s, int64_t request_id);
+int  hepem_server_get_stats(hepem_server* s, hepem_server_stats* out);
+int  hepem_server_reset_stats(hepem_server* s);
+/* Stops the thread after the current iteration and frees the pool. */
+int  hepem_server_destroy(hepem_server* s);
 
 #ifdef __cplusplus
 }
