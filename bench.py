@@ -425,7 +425,7 @@ def main():
     sout = N.empty_state_torch(n)
     res = N.alloc_out_torch(n)
     u = N.fill_uniforms(sin["id"], NU, SEED)
-    cnt = torch.zeros(12, dtype=torch.int64, device="cuda")
+    cnt = torch.zeros(13, dtype=torch.int64, device="cuda")
     stream = torch.cuda.current_stream()
 
     def barrier():

@@ -154,6 +154,30 @@ int hepem_electron_lookup(const hepem_ctx* c, int64_t n, int is_positron, const 
   return HEPEM_OK;
 }
 
+int hepem_electron_lookup_mixed(const hepem_ctx* c, int64_t n, int is_positron, const double* ekin,
+                                const int32_t* imc, double* xi, double* xb, double* dedx, double* range,
+                                double* invr, void* stream) {
+  if (!c || n < 0) return fail(HEPEM_BAD_ARG, "bad context or size");
+  if (n == 0) return HEPEM_OK;
+  if (!ekin || !imc || !xi || !xb || !dedx || !range || !invr) return fail(HEPEM_BAD_ARG, "null array");
+  HEPEM_CUDA(hepem::launch_lookup_mixed(c->tables, n, is_positron ? 1 : 0, ekin, imc, xi, xb, dedx, range, invr,
+                                        (cudaStream_t)stream, c->sms));
+  return HEPEM_OK;
+}
+
+int hepem_sample_model(const hepem_ctx* c, int model, int precision, int64_t n, double ekin, int32_t imc,
+                       uint64_t seed, double* out, uint64_t* n_fallback, void* stream) {
+  if (!c || n < 0 || model < 0 || model > 5 || !(precision == 0 || precision == 1))
+    return fail(HEPEM_BAD_ARG, "bad context, size, model or precision");
+  if (!(imc >= 0 && imc < c->tables.nCouples) || !(ekin > 0.0 && ekin < 1.0e300))
+    return fail(HEPEM_BAD_ARG, "bad couple index or energy");
+  if (n == 0) return HEPEM_OK;
+  if (!out) return fail(HEPEM_BAD_ARG, "null output");
+  HEPEM_CUDA(hepem::launch_sample(c->tables, model, precision, n, ekin, imc, seed, out,
+                                  reinterpret_cast<unsigned long long*>(n_fallback), (cudaStream_t)stream, c->sms));
+  return HEPEM_OK;
+}
+
 int hepem_step(const hepem_ctx* c, int64_t n, const hepem_track_state* in, hepem_track_state* out,
                const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res,
                hepem_step_counters* counters, void* stream) {
@@ -167,26 +191,50 @@ int hepem_step(const hepem_ctx* c, int64_t n, const hepem_track_state* in, hepem
   return HEPEM_OK;
 }
 
-int hepem_step_batched(const hepem_ctx* c, int64_t n, const hepem_track_state* in, hepem_track_state* out,
-                       const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res,
-                       hepem_step_counters* counters, void* stream) {
+namespace {
+int step_batched(const hepem_ctx* c, int64_t n, const hepem_track_state* in, hepem_track_state* out,
+                 const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res,
+                 hepem_step_counters* counters, void* stream, bool mixed) {
   if (!c || n < 0 || nu < 0) return fail(HEPEM_BAD_ARG, "bad context or size");
   if (n == 0) return HEPEM_OK;
   if (!state_ok(in) || !state_ok(out) || !out_ok(res) || (nu > 0 && !uniforms))
     return fail(HEPEM_BAD_ARG, "null array in track batch");
   if (n > (int64_t)INT32_MAX) return fail(HEPEM_BAD_ARG, "batch too large");
   cudaStream_t s = (cudaStream_t)stream;
+  // an in-place precision-form step keeps a copy of the pre-step state of the
+  // e+- tracks that reach an FP32 interaction (their FP64 fallback restarts there)
+  const bool preCopy = mixed && in->ekin == out->ekin;
+  const size_t wsBytes = hepem::batched_workspace_bytes(n);
   void* ws = nullptr;
-  HEPEM_CUDA(cudaMallocAsync(&ws, hepem::batched_workspace_bytes(n), s));
+  HEPEM_CUDA(cudaMallocAsync(&ws, wsBytes + (preCopy ? hepem::mixed_pre_state_bytes(n) : 0), s));
   hepem::BatchOpts o;
   o.ev = c->profile ? const_cast<cudaEvent_t*>(c->stageEv) : nullptr;
   o.cfg = &c->launch;
+  o.mixed = mixed;
+  hepem_track_state pre;
+  if (preCopy) {
+    pre = hepem::carve_pre_state(static_cast<uint8_t*>(ws) + wsBytes, n, *in);
+    o.preState = &pre;
+  }
   cudaError_t e = hepem::launch_step_batched(c->tables, n, *in, *out, uniforms, nu, seed, *res, counters, ws, s,
                                              c->sms, o);
   cudaError_t f = cudaFreeAsync(ws, s);
   if (e != cudaSuccess) return cuda_fail(e, "batched step launch");
   if (f != cudaSuccess) return cuda_fail(f, "cudaFreeAsync");
   return HEPEM_OK;
+}
+}  // namespace
+
+int hepem_step_batched(const hepem_ctx* c, int64_t n, const hepem_track_state* in, hepem_track_state* out,
+                       const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res,
+                       hepem_step_counters* counters, void* stream) {
+  return step_batched(c, n, in, out, uniforms, nu, seed, res, counters, stream, false);
+}
+
+int hepem_step_mixed(const hepem_ctx* c, int64_t n, const hepem_track_state* in, hepem_track_state* out,
+                     const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res,
+                     hepem_step_counters* counters, void* stream) {
+  return step_batched(c, n, in, out, uniforms, nu, seed, res, counters, stream, true);
 }
 
 int hepem_step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem_track_state* out,

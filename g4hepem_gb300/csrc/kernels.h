@@ -13,6 +13,10 @@ namespace hepem {
 cudaError_t launch_lookup(const DevTables& T, int64_t n, int pos, const double* ekin, const int32_t* imc, double* xi,
                           double* xb, double* dedx, double* range, double* invr, cudaStream_t s, int sms);
 
+cudaError_t launch_lookup_mixed(const DevTables& T, int64_t n, int pos, const double* ekin, const int32_t* imc,
+                                double* xi, double* xb, double* dedx, double* range, double* invr, cudaStream_t s,
+                                int sms);
+
 cudaError_t launch_step(const DevTables& T, int64_t n, const hepem_track_state& in, const hepem_track_state& out,
                         const double* uniforms, int nu, uint64_t seed, const hepem_step_out& res,
                         hepem_step_counters* counters, cudaStream_t s, int sms);
@@ -36,11 +40,24 @@ struct BatchOpts {
   const int32_t* active = nullptr;   // step tracks active[0..n) of larger arrays (serving pool)
   const uint64_t* seeds = nullptr;   // per-track RNG keys instead of one seed
   const LaunchCfg* cfg = nullptr;    // null: the default configuration
+  bool mixed = false;                // precision form: e+- stage A in FP32 with FP64 fallback
+  // precision form, in-place steps (in == out): arrays for the pre-step state
+  // of the mutable fields (immutable fields pointing to the input), see
+  // mixed_pre_state_bytes; null for out-of-place steps
+  const hepem_track_state* preState = nullptr;
 };
+// bytes of the pre-step copy of an in-place precision-form step (n tracks)
+size_t mixed_pre_state_bytes(int64_t n);
+// carve the copy from `mem` (mixed_pre_state_bytes(n) bytes) around the batch `in`
+hepem_track_state carve_pre_state(void* mem, int64_t n, const hepem_track_state& in);
 cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track_state& in,
                                 const hepem_track_state& out, const double* uniforms, int nu, uint64_t seed,
                                 const hepem_step_out& res, hepem_step_counters* counters, void* workspace,
                                 cudaStream_t s, int sms, const BatchOpts& opts);
+// per-model sampling (hepem_sample_model): models
+enum { kSampleSB = 0, kSampleRB = 1, kSampleMoller = 2, kSampleBhabha = 3, kSampleCompton = 4, kSampleConversion = 5 };
+cudaError_t launch_sample(const DevTables& T, int model, int mixed, int64_t n, double ekin, int imc, uint64_t seed,
+                          double* out, unsigned long long* nFallback, cudaStream_t s, int sms);
 // stage timing: events recorded before the first and after every stage kernel
 constexpr int kNumStageEvents = 13;
 const char* stage_name(int i);

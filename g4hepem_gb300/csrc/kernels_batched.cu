@@ -25,9 +25,20 @@
 
 #include "g4hepem_gb300.h"
 #include "kernels.h"
+#include "physics_mixed.cuh"
 #include "step_io.cuh"
 
 namespace hepem {
+
+// Diagnostics build only (-DHEPEM_TRIP_SITES): count, per source line of
+// physics_mixed.cuh, the guards that sent a track of the precision form to
+// its FP64 fallback (read with hepem_debug_trip_sites).
+#ifdef HEPEM_TRIP_SITES
+__device__ unsigned long long g_tripSites[4096];
+#define HEPEM_COUNT_TRIP(line) atomicAdd(&g_tripSites[(line) & 4095], 1ull)
+#else
+#define HEPEM_COUNT_TRIP(line) ((void)0)
+#endif
 
 // Tracks are ordered by a sort key (particle, couple bin, energy bin) with a
 // counting sort, so that the warps of a stage hold tracks of one particle in
@@ -37,13 +48,17 @@ constexpr int kSortCoupleBins = 64; // couples beyond 64 share bins (imc % 64)
 constexpr int kMaxSortKeys = 3 * kSortCoupleBins * kMaxSortEBins;
 
 struct Work {
-  uint32_t* counts;               // [0..2] e-, e+, gamma tracks, [3..3+kNumQueues) queues
+  uint32_t* counts;               // [0..2] e-, e+, gamma tracks, [3..3+kNumQueues] queues + FP64 fallback
   uint32_t* hist;                 // [kMaxSortKeys] tracks per sort key
   uint32_t* cursor;               // [kMaxSortKeys] scatter cursors
   int32_t* perm;                  // [n] valid tracks in sort-key order
-  int32_t* queue[kNumQueues];
+  int32_t* queue[kNumQueues + 1];  // interaction queues; [kNumQueues]: tracks the precision form re-steps in FP64
   double* peXS;                   // parallel to queue[kQPhotoelectric]
   const uint64_t* seeds;          // per-track RNG keys (serving), or null: one key per call
+  // precision form: the pre-step state of the tracks (the input batch, or for
+  // in-place steps a copy that stage A takes of the e+- tracks it queues)
+  hepem_track_state pre;
+  bool preCopy;
 };
 
 __device__ __forceinline__ uint64_t key_of(const Work& w, int64_t i, uint64_t seed) {
@@ -61,7 +76,40 @@ static size_t rnd(size_t b) { return (b + 255) / 256 * 256; }
 
 size_t batched_workspace_bytes(int64_t n) {
   return rnd(64 * sizeof(uint32_t)) + 2 * rnd(kMaxSortKeys * sizeof(uint32_t)) +
-         (1 + kNumQueues) * rnd(sizeof(int32_t) * (size_t)n) + rnd(sizeof(double) * (size_t)n);
+         (2 + kNumQueues) * rnd(sizeof(int32_t) * (size_t)n) + rnd(sizeof(double) * (size_t)n);
+}
+
+size_t mixed_pre_state_bytes(int64_t n) {
+  // ekin, dir x3, nia x4, msc x3, gauss value: 12 doubles; cursor; first step, gauss valid
+  return 12 * rnd(sizeof(double) * (size_t)n) + rnd(sizeof(int32_t) * (size_t)n) + 2 * rnd((size_t)n);
+}
+
+hepem_track_state carve_pre_state(void* mem, int64_t n, const hepem_track_state& in) {
+  uint8_t* p = static_cast<uint8_t*>(mem);
+  auto dbl = [&]() {
+    double* r = reinterpret_cast<double*>(p);
+    p += rnd(sizeof(double) * (size_t)n);
+    return r;
+  };
+  hepem_track_state s = in;  // type, imc, id, safety, on_boundary: the input's
+  s.ekin = dbl();
+  s.dir_x = dbl();
+  s.dir_y = dbl();
+  s.dir_z = dbl();
+  s.nia0 = dbl();
+  s.nia1 = dbl();
+  s.nia2 = dbl();
+  s.nia3 = dbl();
+  s.msc_init_range = dbl();
+  s.msc_dyn_factor = dbl();
+  s.msc_tlimit_min = dbl();
+  s.gauss_value = dbl();
+  s.rng_cursor = reinterpret_cast<int32_t*>(p);
+  p += rnd(sizeof(int32_t) * (size_t)n);
+  s.msc_first_step = p;
+  p += rnd((size_t)n);
+  s.gauss_valid = p;
+  return s;
 }
 
 static Work carve(void* ws, int64_t n) {
@@ -75,7 +123,7 @@ static Work carve(void* ws, int64_t n) {
   p += rnd(kMaxSortKeys * sizeof(uint32_t));
   w.perm = reinterpret_cast<int32_t*>(p);
   p += rnd(sizeof(int32_t) * (size_t)n);
-  for (int k = 0; k < kNumQueues; ++k) {
+  for (int k = 0; k <= kNumQueues; ++k) {
     w.queue[k] = reinterpret_cast<int32_t*>(p);
     p += rnd(sizeof(int32_t) * (size_t)n);
   }
@@ -184,35 +232,76 @@ __global__ void __launch_bounds__(256) sort_scatter_kernel(const __grid_constant
 }
 
 // ---- 2. stage A -----------------------------------------------------------------------
-template <int BS>
+// copy of the mutable pre-step state of track i (precision form, in-place steps)
+__device__ __forceinline__ void save_pre(const hepem_track_state& in, const hepem_track_state& pre, int64_t i) {
+  pre.ekin[i] = in.ekin[i];
+  pre.dir_x[i] = in.dir_x[i];
+  pre.dir_y[i] = in.dir_y[i];
+  pre.dir_z[i] = in.dir_z[i];
+  pre.nia0[i] = in.nia0[i];
+  pre.nia1[i] = in.nia1[i];
+  pre.nia2[i] = in.nia2[i];
+  pre.nia3[i] = in.nia3[i];
+  pre.msc_init_range[i] = in.msc_init_range[i];
+  pre.msc_dyn_factor[i] = in.msc_dyn_factor[i];
+  pre.msc_tlimit_min[i] = in.msc_tlimit_min[i];
+  pre.msc_first_step[i] = in.msc_first_step[i];
+  pre.gauss_valid[i] = in.gauss_valid[i];
+  pre.gauss_value[i] = in.gauss_value[i];
+  pre.rng_cursor[i] = in.rng_cursor[i];
+}
+
+// MODE kStageFp64: the FP64 physics over the e+- tracks in sort order.
+// MODE kStageMixed: the precision form (physics_mixed.cuh) over the same
+//   tracks; a track whose FP32 pass tripped a guard is not stored but appended
+//   to the fallback list.
+// MODE kStageFallback: the FP64 physics over the fallback list (the tracks'
+//   input state is untouched: a tripped track was never stored).
+enum { kStageFp64 = 0, kStageMixed = 1, kStageFallback = 2 };
+
+template <int BS, int MODE>
 __global__ void __launch_bounds__(BS) stage_a_charged_kernel(const __grid_constant__ DevTables T,
                                                               const hepem_track_state in, const hepem_track_state out,
                                                               const double* __restrict__ uniforms, int nu,
                                                               uint64_t seed, const hepem_step_out res, const Work w,
                                                               hepem_step_counters* counters) {
   const uint32_t nEm = w.counts[0], nEp = w.counts[1];
-  const int64_t total = (int64_t)nEm + nEp;
+  const int64_t total = MODE == kStageFallback ? (int64_t)w.counts[3 + kNumQueues] : (int64_t)nEm + nEp;
   StepCount cnt = {};
   for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < total; base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = base + threadIdx.x;
     int key = -1;
     int32_t idx = 0;
     if (j < total) {
-      idx = w.perm[j];
-      const int type = j < nEm ? 0 : 1;
+      idx = MODE == kStageFallback ? w.queue[kNumQueues][j] : w.perm[j];
+      const int type = MODE == kStageFallback ? (int)in.type[idx] : (j < nEm ? 0 : 1);
       Track t;
       Rng rng;
       load_track(in, idx, t, rng, uniforms, nu, key_of(w, idx, seed), type);
       const int32_t c0 = rng.cursor;
-      Physics P{T, rng, t};
-      P.el_howfar();
-      key = P.el_perform_until_discrete();
-      store_track(in, out, res, idx, t, rng, type, false);
-      res.n_sec[idx] = 0;
-      cnt.steps += 1;
-      cnt.uniforms += (uint32_t)(rng.cursor - c0);
-      cnt.overflow += rng.overflow;
-      if (t.winner >= 0 && t.winner < 4) cnt.inter[t.winner] += 1;
+      bool tripped = false;
+      if (MODE == kStageMixed) {
+        MixedEl M{T, rng, t, false};
+        key = M.stage_a();
+        tripped = M.trip;
+        if (tripped) HEPEM_COUNT_TRIP(M.tripLine);
+      } else {
+        Physics P{T, rng, t};
+        P.el_howfar();
+        key = P.el_perform_until_discrete();
+      }
+      if (tripped) {
+        key = kNumQueues;
+      } else {
+        if (MODE != kStageFp64 && w.preCopy && key >= 0 && key != kQAnnihRest) save_pre(in, w.pre, idx);
+        store_track(in, out, res, idx, t, rng, type, false);
+        res.n_sec[idx] = 0;
+        cnt.steps += 1;
+        cnt.uniforms += (uint32_t)(rng.cursor - c0);
+        cnt.overflow += rng.overflow;
+        if (t.winner >= 0 && t.winner < 4) cnt.inter[t.winner] += 1;
+        if (MODE == kStageFallback) cnt.fallback += 1;
+      }
     }
     warp_push(key, idx, w.queue, w.counts + 3);
   }
@@ -266,66 +355,142 @@ __global__ void __launch_bounds__(BS) stage_a_gamma_kernel(const __grid_constant
 }
 
 // ---- 3. stage B: one interaction model per kernel ------------------------------------------
-template <int Q, int BS>
+// Models with an FP32 version in the precision form (physics_mixed.cuh).
+__host__ __device__ constexpr bool has_mixed(int q) {
+  return q == kQIoniEm || q == kQIoniEp || q == kQBremSB || q == kQBremRB || q == kQAnnihFlight ||
+         q == kQConversion || q == kQCompton;
+}
+// e+- models: their input energy carries the FP32 continuous loss
+__host__ __device__ constexpr bool charged_model(int q) {
+  return q == kQIoniEm || q == kQIoniEp || q == kQBremSB || q == kQBremRB || q == kQAnnihFlight;
+}
+
+// Precision form: an e+- track whose FP32 interaction tripped a guard is
+// stepped again from its pre-step state entirely in FP64 (stage A and the
+// interaction).  Its energy after the FP32 continuous step differs from the
+// FP64 one by ~1e-7, so the FP64 interaction alone would not give the FP64
+// path's outcome for the near-tie that tripped the guard.
+template <int Q>
+__device__ void charged_full_step(const DevTables& T, const hepem_track_state& in, const hepem_track_state& out,
+                                  const double* uniforms, int nu, uint64_t seed, const hepem_step_out& res,
+                                  const Work& w, int32_t i, StepCount& cnt) {
+  const int type = in.type[i];
+  Track t;
+  Rng rng;
+  load_track(w.pre, i, t, rng, uniforms, nu, key_of(w, i, seed), type);
+  Physics P{T, rng, t};
+  P.el_howfar();
+  const int key = P.el_perform_until_discrete();
+  const int32_t cA = rng.cursor;
+  const uint32_t ovA = rng.overflow;
+  if (key == Q) {  // always: the stage-A guards held for this track
+    if (Q == kQIoniEm || Q == kQIoniEp) P.ioni();
+    if (Q == kQBremSB) P.brem(true);
+    if (Q == kQBremRB) P.brem(false);
+    if (Q == kQAnnihFlight) P.annihilate_in_flight();
+  }
+  store_track(in, out, res, i, t, rng, type, false);
+  store_secondaries(res, i, t, 0);
+  cnt.uniforms += (uint32_t)(rng.cursor - cA);
+  cnt.overflow += (rng.overflow && !ovA) ? 1u : 0u;
+  cnt.secondaries += (uint32_t)(t.nsec > 2 ? 2 : t.nsec);
+  cnt.fallback += 1;
+}
+// counter of the FP64 fallback list of interaction queue q (precision form)
+constexpr int kFallbackCountB = 16;
+
+// MODE kStageFp64 / kStageMixed: the queue of model Q; kStageFallback: the
+// tracks of queue Q that the mixed kernel gave up on (the fallback list).
+template <int Q, int BS, int MODE>
 __global__ void __launch_bounds__(BS) stage_b_kernel(const __grid_constant__ DevTables T,
                                                       const hepem_track_state in, const hepem_track_state out,
                                                       const double* __restrict__ uniforms, int nu, uint64_t seed,
                                                       const hepem_step_out res, const Work w,
                                                       hepem_step_counters* counters) {
-  const int64_t total = w.counts[3 + Q];
-  const int32_t* q = w.queue[Q];
+  const int64_t total = MODE == kStageFallback ? w.counts[kFallbackCountB + Q] : w.counts[3 + Q];
+  const int32_t* q = MODE == kStageFallback ? w.queue[kNumQueues] : w.queue[Q];
   StepCount cnt = {};
-  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < total; j += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t i = q[j];
-    Track t;
-    Rng rng;
-    t.imc = in.imc[i];
-    t.setE(out.ekin[i]);
-    t.dir[0] = out.dir_x[i];
-    t.dir[1] = out.dir_y[i];
-    t.dir[2] = out.dir_z[i];
-    t.isEl = (Q == kQIoniEm) || ((Q == kQBremSB || Q == kQBremRB) && in.type[i] == 0);
-    t.flags = res.flags[i];
-    t.nsec = 0;
-    rng.u = uniforms + (int64_t)i * nu;
-    rng.n = nu;
-    rng.cursor = out.rng_cursor[i];
-    rng.id = in.id[i];
-    rng.overflow = 0u;
-    rng.seed = key_of(w, i, seed);
-    rng.gaussValid = out.gauss_valid[i] != 0;
-    rng.gaussValue = out.gauss_value[i];
-    const int32_t c0 = rng.cursor;
-    Physics P{T, rng, t};
-    if (Q == kQIoniEm || Q == kQIoniEp) P.ioni();
-    if (Q == kQBremSB) P.brem(true);
-    if (Q == kQBremRB) P.brem(false);
-    if (Q == kQAnnihFlight) P.annihilate_in_flight();
-    if (Q == kQAnnihRest) P.annihilate_at_rest();
-    if (Q >= kQConversion) {
-      t.edep = 0.0;
-      t.peXS = (Q == kQPhotoelectric) ? w.peXS[j] : 0.0;
-      if (Q == kQConversion) P.conversion();
-      if (Q == kQCompton) P.compton();
-      if (Q == kQPhotoelectric) P.photoelectric();
-      P.gamma_tracking_cut();
-      res.edep[i] = t.edep;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < total; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = base + threadIdx.x;
+    bool tripped = false;
+    int32_t i = 0;
+    if (j < total && MODE == kStageFallback && charged_model(Q)) {
+      charged_full_step<Q>(T, in, out, uniforms, nu, seed, res, w, q[j], cnt);
+    } else if (j < total) {
+      i = q[j];
+      Track t;
+      Rng rng;
+      t.imc = in.imc[i];
+      t.setE(out.ekin[i]);
+      t.dir[0] = out.dir_x[i];
+      t.dir[1] = out.dir_y[i];
+      t.dir[2] = out.dir_z[i];
+      t.isEl = (Q == kQIoniEm) || ((Q == kQBremSB || Q == kQBremRB) && in.type[i] == 0);
+      t.flags = res.flags[i];
+      t.nsec = 0;
+      rng.u = uniforms + (int64_t)i * nu;
+      rng.n = nu;
+      rng.cursor = out.rng_cursor[i];
+      rng.id = in.id[i];
+      rng.overflow = 0u;
+      rng.seed = key_of(w, i, seed);
+      rng.gaussValid = out.gauss_valid[i] != 0;
+      rng.gaussValue = out.gauss_value[i];
+      const int32_t c0 = rng.cursor;
+      if (MODE == kStageMixed) {
+        MixedB M{T, rng, t, false};
+        if (Q == kQIoniEm || Q == kQIoniEp) M.ioni();
+        if (Q == kQBremSB) M.brem(true);
+        if (Q == kQBremRB) M.brem(false);
+        if (Q == kQAnnihFlight) M.annihilate_in_flight();
+        if (Q >= kQConversion) {
+          t.edep = 0.0;
+          if (Q == kQConversion) M.conversion();
+          if (Q == kQCompton) M.compton();
+        }
+        tripped = M.trip;
+        if (tripped) HEPEM_COUNT_TRIP(M.tripLine);
+      } else {
+        Physics P{T, rng, t};
+        if (Q == kQIoniEm || Q == kQIoniEp) P.ioni();
+        if (Q == kQBremSB) P.brem(true);
+        if (Q == kQBremRB) P.brem(false);
+        if (Q == kQAnnihFlight) P.annihilate_in_flight();
+        if (Q == kQAnnihRest) P.annihilate_at_rest();
+        if (Q >= kQConversion) {
+          t.edep = 0.0;
+          t.peXS = (Q == kQPhotoelectric) ? w.peXS[j] : 0.0;
+          if (Q == kQConversion) P.conversion();
+          if (Q == kQCompton) P.compton();
+          if (Q == kQPhotoelectric) P.photoelectric();
+        }
+      }
+      if (!tripped) {
+        if (Q >= kQConversion) {
+          Physics P{T, rng, t};
+          P.gamma_tracking_cut();
+          res.edep[i] = t.edep;
+        }
+        out.ekin[i] = t.e;
+        if (Q != kQAnnihRest) {
+          out.dir_x[i] = t.dir[0];
+          out.dir_y[i] = t.dir[1];
+          out.dir_z[i] = t.dir[2];
+        }
+        out.gauss_valid[i] = rng.gaussValid ? 1 : 0;
+        out.gauss_value[i] = rng.gaussValue;
+        out.rng_cursor[i] = rng.cursor;
+        const bool firstOverflow = rng.overflow && !(t.flags & kFlagRngOverflow);
+        res.flags[i] = t.flags | (rng.overflow ? kFlagRngOverflow : 0);
+        store_secondaries(res, i, t, 0);
+        cnt.uniforms += (uint32_t)(rng.cursor - c0);
+        cnt.overflow += firstOverflow ? 1u : 0u;
+        cnt.secondaries += (uint32_t)(t.nsec > 2 ? 2 : t.nsec);
+        if (MODE == kStageFallback) cnt.fallback += 1;
+      }
     }
-    out.ekin[i] = t.e;
-    if (Q != kQAnnihRest) {
-      out.dir_x[i] = t.dir[0];
-      out.dir_y[i] = t.dir[1];
-      out.dir_z[i] = t.dir[2];
-    }
-    out.gauss_valid[i] = rng.gaussValid ? 1 : 0;
-    out.gauss_value[i] = rng.gaussValue;
-    out.rng_cursor[i] = rng.cursor;
-    const bool firstOverflow = rng.overflow && !(t.flags & kFlagRngOverflow);
-    res.flags[i] = t.flags | (rng.overflow ? kFlagRngOverflow : 0);
-    store_secondaries(res, i, t, 0);
-    cnt.uniforms += (uint32_t)(rng.cursor - c0);
-    cnt.overflow += firstOverflow ? 1u : 0u;
-    cnt.secondaries += (uint32_t)(t.nsec > 2 ? 2 : t.nsec);
+    if (MODE == kStageMixed)
+      warp_push(tripped ? (int)kNumQueues : -1, i, w.queue, w.counts + kFallbackCountB + Q - kNumQueues);
   }
   add_counters(cnt, counters);
 }
@@ -342,23 +507,53 @@ static int bs_index(int bs) { return bs == 128 ? 0 : (bs == 512 ? 2 : 1); }
 
 template <int BS>
 static void stage_table(StageFn* f) {
-  f[0] = stage_a_charged_kernel<BS>;
+  f[0] = stage_a_charged_kernel<BS, kStageFp64>;
   f[1] = stage_a_gamma_kernel<BS>;
-  f[2] = stage_b_kernel<0, BS>;
-  f[3] = stage_b_kernel<1, BS>;
-  f[4] = stage_b_kernel<2, BS>;
-  f[5] = stage_b_kernel<3, BS>;
-  f[6] = stage_b_kernel<4, BS>;
-  f[7] = stage_b_kernel<5, BS>;
-  f[8] = stage_b_kernel<6, BS>;
-  f[9] = stage_b_kernel<7, BS>;
-  f[10] = stage_b_kernel<8, BS>;
+  f[2] = stage_b_kernel<0, BS, kStageFp64>;
+  f[3] = stage_b_kernel<1, BS, kStageFp64>;
+  f[4] = stage_b_kernel<2, BS, kStageFp64>;
+  f[5] = stage_b_kernel<3, BS, kStageFp64>;
+  f[6] = stage_b_kernel<4, BS, kStageFp64>;
+  f[7] = stage_b_kernel<5, BS, kStageFp64>;
+  f[8] = stage_b_kernel<6, BS, kStageFp64>;
+  f[9] = stage_b_kernel<7, BS, kStageFp64>;
+  f[10] = stage_b_kernel<8, BS, kStageFp64>;
+}
+
+// precision form: [kernel index] -> FP32 kernel and its FP64 fallback (null: none)
+template <int BS>
+static void mixed_table(StageFn* m, StageFn* f) {
+  for (int k = 0; k < kNumStageKernels; ++k) m[k] = f[k] = nullptr;
+  m[0] = stage_a_charged_kernel<BS, kStageMixed>;
+  f[0] = stage_a_charged_kernel<BS, kStageFallback>;
+  m[2 + kQIoniEm] = stage_b_kernel<kQIoniEm, BS, kStageMixed>;
+  f[2 + kQIoniEm] = stage_b_kernel<kQIoniEm, BS, kStageFallback>;
+  m[2 + kQIoniEp] = stage_b_kernel<kQIoniEp, BS, kStageMixed>;
+  f[2 + kQIoniEp] = stage_b_kernel<kQIoniEp, BS, kStageFallback>;
+  m[2 + kQBremSB] = stage_b_kernel<kQBremSB, BS, kStageMixed>;
+  f[2 + kQBremSB] = stage_b_kernel<kQBremSB, BS, kStageFallback>;
+  m[2 + kQBremRB] = stage_b_kernel<kQBremRB, BS, kStageMixed>;
+  f[2 + kQBremRB] = stage_b_kernel<kQBremRB, BS, kStageFallback>;
+  m[2 + kQAnnihFlight] = stage_b_kernel<kQAnnihFlight, BS, kStageMixed>;
+  f[2 + kQAnnihFlight] = stage_b_kernel<kQAnnihFlight, BS, kStageFallback>;
+  m[2 + kQConversion] = stage_b_kernel<kQConversion, BS, kStageMixed>;
+  f[2 + kQConversion] = stage_b_kernel<kQConversion, BS, kStageFallback>;
+  m[2 + kQCompton] = stage_b_kernel<kQCompton, BS, kStageMixed>;
+  f[2 + kQCompton] = stage_b_kernel<kQCompton, BS, kStageFallback>;
 }
 
 struct StageKernels {
   StageFn fn[3][kNumStageKernels];
   int occ[3][kNumStageKernels];  // resident CTAs per SM
+  StageFn mixed[3][kNumStageKernels], fallback[3][kNumStageKernels];  // precision form (null: FP64 only)
+  int occMixed[3][kNumStageKernels], occFallback[3][kNumStageKernels];
 };
+
+static int occupancy_of(StageFn f, int bs) {
+  int per = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, bs, 0) != cudaSuccess || per < 1) per = 1;
+  return per;
+}
 
 // kernel table and occupancies (thread-safe one-time initialisation)
 static const StageKernels& stage_kernels() {
@@ -367,13 +562,14 @@ static const StageKernels& stage_kernels() {
     stage_table<128>(r.fn[0]);
     stage_table<256>(r.fn[1]);
     stage_table<512>(r.fn[2]);
+    mixed_table<128>(r.mixed[0], r.fallback[0]);
+    mixed_table<256>(r.mixed[1], r.fallback[1]);
+    mixed_table<512>(r.mixed[2], r.fallback[2]);
     for (int b = 0; b < 3; ++b)
       for (int k = 0; k < kNumStageKernels; ++k) {
-        int per = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, r.fn[b][k], kBlockSizes[b], 0) != cudaSuccess ||
-            per < 1)
-          per = 1;
-        r.occ[b][k] = per;
+        r.occ[b][k] = occupancy_of(r.fn[b][k], kBlockSizes[b]);
+        r.occMixed[b][k] = r.mixed[b][k] ? occupancy_of(r.mixed[b][k], kBlockSizes[b]) : 0;
+        r.occFallback[b][k] = r.fallback[b][k] ? occupancy_of(r.fallback[b][k], kBlockSizes[b]) : 0;
       }
     return r;
   }();
@@ -410,6 +606,12 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
   const LaunchCfg& cfg = o.cfg ? *o.cfg : kDefault;
   Work w = carve(workspace, n);
   w.seeds = o.seeds;
+  w.pre = in;
+  w.preCopy = false;
+  if (o.mixed && o.preState) {
+    w.pre = *o.preState;
+    w.preCopy = true;
+  }
   const int ncb = T.nCouples < kSortCoupleBins ? T.nCouples : kSortCoupleBins;
   const int neb = cfg.sortEBins;
   const int nkeys = 3 * ncb * neb;
@@ -429,6 +631,16 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
   mark();
   for (int q = 0; q < kNumStageKernels; ++q) {
     const int b = bs_index(cfg.block[q]);
+    if (o.mixed && K.mixed[b][q]) {
+      // precision form: the FP32 kernel, then the FP64 kernel over the tracks it gave up on
+      const int om = K.occMixed[b][q];
+      const int pm = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < om ? cfg.ctasPerSM[q] : om;
+      K.mixed[b][q]<<<sms * pm, kBlockSizes[b], 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+      K.fallback[b][q]<<<sms * K.occFallback[b][q], kBlockSizes[b], 0, s>>>(T, in, out, uniforms, nu, seed, res,
+                                                                             w, counters);
+      mark();
+      continue;
+    }
     const int occ = K.occ[b][q];
     const int per = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < occ ? cfg.ctasPerSM[q] : occ;
     K.fn[b][q]<<<sms * per, kBlockSizes[b], 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
@@ -437,4 +649,112 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
   return cudaGetLastError();
 }
 
+// ---- 4. per-model sampling (interaction unit tests and distribution checks) -------------
+// n independent draws of one interaction model at a fixed energy and couple:
+// draw i is a track with id i, direction +z and the pure Philox stream of
+// (seed, i).  MIXED: the FP32 model of the precision form, a draw that trips
+// a guard is redone by the FP64 model (counted in nFallback).
+__device__ __forceinline__ void sample_init(Track& t, Rng& rng, int model, double ekin, int imc, int64_t i,
+                                            uint64_t seed) {
+  t.imc = imc;
+  t.setE(ekin);
+  t.dir[0] = 0.0; t.dir[1] = 0.0; t.dir[2] = 1.0;
+  t.isEl = model != kSampleBhabha;
+  t.flags = 0;
+  t.nsec = 0;
+  t.edep = 0.0;
+  t.peXS = 0.0;
+  rng.u = nullptr;
+  rng.n = 0;
+  rng.cursor = 0;
+  rng.id = (int32_t)i;
+  rng.overflow = 0u;
+  rng.seed = seed;
+  rng.gaussValid = false;
+  rng.gaussValue = 0.0;
+}
+
+template <class M>
+__device__ __forceinline__ void sample_run(M& m, int model) {
+  switch (model) {
+    case kSampleSB: m.brem(true); break;
+    case kSampleRB: m.brem(false); break;
+    case kSampleMoller:
+    case kSampleBhabha: m.ioni(); break;
+    case kSampleCompton: m.compton(); break;
+    case kSampleConversion: m.conversion(); break;
+    default: break;
+  }
+}
+
+__device__ __forceinline__ double sample_value(const Track& t, int model) {
+  if (model == kSampleCompton) return t.e;            // scattered photon energy
+  return t.nsec > 0 ? t.sec[0].e : 0.0;               // photon, delta ray, or pair electron
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(256) sample_kernel(const __grid_constant__ DevTables T, int model, int64_t n,
+                                                     double ekin, int imc, uint64_t seed, double* __restrict__ out,
+                                                     unsigned long long* nFallback) {
+  uint32_t fb = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    Track t;
+    Rng rng;
+    sample_init(t, rng, model, ekin, imc, i, seed);
+    bool redo = !MIXED;
+    if (MIXED) {
+      MixedB mb{T, rng, t, false};
+      sample_run(mb, model);
+      if (mb.trip) {
+        redo = true;
+        ++fb;
+        sample_init(t, rng, model, ekin, imc, i, seed);
+      }
+    }
+    if (redo) {
+      Physics P{T, rng, t};
+      sample_run(P, model);
+    }
+    out[i] = sample_value(t, model);
+  }
+  if (MIXED && nFallback) {
+    const uint32_t w = __reduce_add_sync(0xFFFFFFFFu, fb);
+    if ((threadIdx.x & 31) == 0 && w) atomicAdd(nFallback, (unsigned long long)w);
+  }
+}
+
+cudaError_t launch_sample(const DevTables& T, int model, int mixed, int64_t n, double ekin, int imc, uint64_t seed,
+                          double* out, unsigned long long* nFallback, cudaStream_t s, int sms) {
+  if (n <= 0) return cudaSuccess;
+  const int64_t blocks = (n + 255) / 256;
+  const int g = (int)(blocks < (int64_t)sms * 16 ? blocks : (int64_t)sms * 16);
+  if (mixed)
+    sample_kernel<true><<<g, 256, 0, s>>>(T, model, n, ekin, imc, seed, out, nFallback);
+  else
+    sample_kernel<false><<<g, 256, 0, s>>>(T, model, n, ekin, imc, seed, out, nFallback);
+  return cudaGetLastError();
+}
+
 }  // namespace hepem
+
+#ifdef HEPEM_TRIP_SITES
+extern "C" int hepem_debug_trip_sites(unsigned long long* out, int reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, hepem::g_tripSites, sizeof(unsigned long long) * 4096);
+  if (e == cudaSuccess && reset) {
+    static const unsigned long long zero[4096] = {};
+    e = cudaMemcpyToSymbol(hepem::g_tripSites, zero, sizeof(zero));
+  }
+  return e == cudaSuccess ? 0 : 3;
+}
+#endif
+
+#ifdef HEPEM_TRACE
+extern "C" int hepem_debug_trace(int id, double* out128) {
+  if (id >= -1) {
+    static const double zero[128] = {};
+    if (cudaMemcpyToSymbol(hepem::g_trace, zero, sizeof(zero)) != cudaSuccess) return 3;
+    return cudaMemcpyToSymbol(hepem::g_traceId, &id, sizeof(int)) == cudaSuccess ? 0 : 3;
+  }
+  return cudaMemcpyFromSymbol(out128, hepem::g_trace, sizeof(double) * 128) == cudaSuccess ? 0 : 3;
+}
+#endif

@@ -12,6 +12,8 @@
 #include "g4hepem_gb300.h"
 #include "kernels.h"
 #include "physics.cuh"
+#include "physics_mixed.cuh"
+#include "step_io.cuh"
 
 namespace hepem {
 
@@ -43,30 +45,6 @@ __global__ void __launch_bounds__(256) lookup_kernel(const __grid_constant__ Dev
 }
 
 // ---------------------------------------------------------------------------
-// Block-level sum of the step counters: warp reduce, then one atomic per block.
-struct StepCount {
-  uint32_t steps, uniforms, overflow, secondaries, inter[8];
-};
-
-__device__ __forceinline__ void add_counters(StepCount& c, hepem_step_counters* g) {
-  __shared__ uint32_t s[12];
-  if (threadIdx.x < 12) s[threadIdx.x] = 0;
-  __syncthreads();
-  uint32_t v[12] = {c.steps, c.uniforms, c.overflow, c.secondaries, c.inter[0], c.inter[1], c.inter[2], c.inter[3],
-                    c.inter[4], c.inter[5], c.inter[6], c.inter[7]};
-#pragma unroll
-  for (int k = 0; k < 12; ++k) {
-    const uint32_t w = __reduce_add_sync(0xFFFFFFFFu, v[k]);
-    if ((threadIdx.x & 31) == 0 && w) atomicAdd(&s[k], w);
-  }
-  __syncthreads();
-  if (threadIdx.x < 12 && s[threadIdx.x]) {
-    unsigned long long* dst = threadIdx.x < 4 ? (unsigned long long*)&g->steps + threadIdx.x
-                                              : (unsigned long long*)&g->interactions[threadIdx.x - 4];
-    atomicAdd(dst, (unsigned long long)s[threadIdx.x]);
-  }
-}
-
 __device__ __forceinline__ void step_one(const DevTables& T, int64_t i, const hepem_track_state& in,
                                          const hepem_track_state& out, const double* uniforms, int nu,
                                          uint64_t seed, const hepem_step_out& res, StepCount& cnt) {
@@ -191,6 +169,35 @@ __global__ void __launch_bounds__(256) step_kernel(const __grid_constant__ DevTa
   if (counters) add_counters(cnt, counters);
 }
 
+// the same lookups from the FP32 tables of the precision form (FP32 arithmetic)
+__global__ void __launch_bounds__(256) lookup_mixed_kernel(const __grid_constant__ DevTables T, int64_t n, int pos,
+                                                           const double* __restrict__ ekin,
+                                                           const int32_t* __restrict__ imc, double* __restrict__ xi,
+                                                           double* __restrict__ xb, double* __restrict__ dedx,
+                                                           double* __restrict__ range, double* __restrict__ invr) {
+  const DevElData& d = T.el[pos ? 1 : 0];
+  const DevElData32& f = T.el32[pos ? 1 : 0];
+  const int nL = d.nLoss;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double e = ekin[i];
+    int c = imc[i];
+    const bool bad = !(c >= 0 && c < T.nCouples) || !(e > 0.0) || !(e < 1.0e300);
+    if (bad) c = 0;
+    const float ef = (float)e, le = logf(ef);
+    const float a = rest_macxs32(d, f, c, e, ef, le, true);
+    const float b = rest_macxs32(d, f, c, e, ef, le, false);
+    const float s = rest_dedx32(f, nL, c, ef, le);
+    const float r = rest_range32(f, nL, c, ef, le);
+    const float q = inv_range32(f, nL, c, 0.5f * r);
+    const double nan = __longlong_as_double(0x7FF8000000000000LL);
+    xi[i] = bad ? nan : (double)a;
+    xb[i] = bad ? nan : (double)b;
+    dedx[i] = bad ? nan : (double)s;
+    range[i] = bad ? nan : (double)r;
+    invr[i] = bad ? nan : (double)q;
+  }
+}
+
 __global__ void fill_uniforms_kernel(int64_t n, const int32_t* __restrict__ id, int nu, uint64_t seed,
                                      double* __restrict__ u) {
   const int64_t total = n * nu;
@@ -212,6 +219,14 @@ cudaError_t launch_lookup(const DevTables& T, int64_t n, int pos, const double* 
                           double* xb, double* dedx, double* range, double* invr, cudaStream_t s, int sms) {
   if (n <= 0) return cudaSuccess;
   lookup_kernel<<<grid_for(n, 256, sms), 256, 0, s>>>(T, n, pos, ekin, imc, xi, xb, dedx, range, invr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lookup_mixed(const DevTables& T, int64_t n, int pos, const double* ekin, const int32_t* imc,
+                                double* xi, double* xb, double* dedx, double* range, double* invr, cudaStream_t s,
+                                int sms) {
+  if (n <= 0) return cudaSuccess;
+  lookup_mixed_kernel<<<grid_for(n, 256, sms), 256, 0, s>>>(T, n, pos, ekin, imc, xi, xb, dedx, range, invr);
   return cudaGetLastError();
 }
 

@@ -47,6 +47,19 @@ constexpr double kMigdal = 5.2804955733859579e-30;
 constexpr double kLPM = 7.6843819381368661e+05;
 constexpr double kLarge = 1.0E+20;
 
+// Diagnostics build only (-DHEPEM_TRACE): intermediate values of one track
+// (id g_traceId) of the FP64 physics (row 0) and of the precision form (row 1).
+#ifdef HEPEM_TRACE
+static __device__ int g_traceId = -1;
+static __device__ double g_trace[2][64];
+#define HEPEM_TR(row, slot, v)                               \
+  do {                                                       \
+    if (rng.id == g_traceId) g_trace[row][slot] = (double)(v); \
+  } while (0)
+#else
+#define HEPEM_TR(row, slot, v) ((void)0)
+#endif
+
 template <class T>
 __device__ __forceinline__ T ld(const T* p) { return __ldg(p); }
 __device__ __forceinline__ double dmax_(double a, double b) { return a > b ? a : b; }
@@ -238,6 +251,8 @@ struct Physics {
     t.range = range;
     const double frange = ld(&reg.finalRange), drange = ld(&reg.dRoverRange);
     double pstep = range > frange ? range * drange + frange * (1.0 - drange) * (2.0 - frange / range) : range;
+    HEPEM_TR(0, 0, range);
+    HEPEM_TR(0, 1, pstep);
     int winner = -1;
     double mx[4];
     mx[0] = rest_macxs_stepping(d, imc, e, le, true);
@@ -254,6 +269,10 @@ struct Physics {
     t.pstep = pstep;
     t.winner = winner;
     t.gstep = pstep;
+    HEPEM_TR(0, 2, mx[0]);
+    HEPEM_TR(0, 3, mx[1]);
+    HEPEM_TR(0, 6, pstep);
+    HEPEM_TR(0, 7, winner);
     Msc& m = t.msc;
     m.trueStep = pstep;
     m.zPath = pstep;
@@ -264,7 +283,10 @@ struct Physics {
       m.active = true;
       m.lambtr1 = transport_mfp(d, c.mat, e, le);
       msc_step_limit(e, c.mat, range, reg);
+      HEPEM_TR(0, 8, m.lambtr1);
+      HEPEM_TR(0, 10, m.trueStep);
       true_to_geom(e, range, c.mat);
+      HEPEM_TR(0, 11, m.zPath);
       if (m.trueStep < pstep) {
         t.winner = -2;
         pstep = m.trueStep;
@@ -422,6 +444,7 @@ struct Physics {
       eloss = e - inv_range(d, t.imc, post);
     }
     eloss = dmax_(eloss, 0.0);
+    HEPEM_TR(0, 14, eloss);
     if (eloss >= e) {
       eloss = e;
       t.setE(0);
@@ -458,6 +481,7 @@ struct Physics {
   __device__ void msc_scatter(double pstep, double preE, double preMFP, double postE, double postMFP, int imat) {
     Msc& m = t.msc;
     const double cost = msc_cos_theta(pstep, preE, preMFP, postE, postMFP, m.tlimitMin, imat);
+    HEPEM_TR(0, 21, cost);
     if (fabs(cost) >= 1.0) {
       m.noScatter = true;
       return;
@@ -599,6 +623,7 @@ struct Physics {
       eloss = fluct(tcut, ld(&T.mats[c.mat].meanExc), eloss);
       eloss = dmax_(eloss, 0.0);
       finalE = preE - eloss;
+      HEPEM_TR(0, 15, eloss);
     }
     (void)pstep;
     if (finalE <= T.elTrackingCut) {
@@ -622,6 +647,7 @@ struct Physics {
     double a1 = 0.;
     double e1 = excE;
     double eloss = 0.0;
+    HEPEM_TR(0, 18, a3);
     if (tcut > excE) {
       const double a1t = meanLoss * (1. - rate) / excE;
       const double d0 = a1t < 42. ? .1 + (4. - .1) * sqrt(a1t / 42.) : 4.;
@@ -633,6 +659,7 @@ struct Physics {
         eloss = gauss_loss(em, em * e1);
       } else {
         const int p = poisson_capped(a1);
+        HEPEM_TR(0, 17, p);
         eloss = p > 0 ? ((p + 1) - 2. * rng.flat()) * e1 : 0.;
       }
     }
@@ -652,6 +679,8 @@ struct Physics {
       if (tcut > w3) {
         const double w = (tcut - w3) / tcut;
         int nnb = poisson_capped(p3);
+        HEPEM_TR(0, 19, p3);
+        HEPEM_TR(0, 20, nnb);
         if (nnb > kMaxIter) { nnb = kMaxIter; t.flags |= kFlagLoopCap; }
         for (int k = 0; k < nnb; ++k) eloss += w3 / (1. - w * rng.flat());
       }

@@ -1,0 +1,1364 @@
+// physics_mixed.cuh -- the e+- stage A (HowFar, continuous step, MSC, energy
+// loss fluctuations, delta-interaction test) of the precision form.
+//
+// The same algorithm as Physics::el_howfar + el_perform_until_discrete
+// (physics.cuh, G4HepEmElectronManager.icc:35-483, UMSC and fluctuation
+// models), with the table lookups and the sampling arithmetic in FP32 from
+// FP32 tables (DevElData32).  FP64 is kept for: the decisions on exact inputs
+// (energy against table thresholds), the range->energy inversion of the mean
+// energy loss, the polar-method acceptance of Gaussian samples, the sum of the
+// fluctuation terms, and the energy / deposit bookkeeping.
+//
+// Guarded decisions.  Every branch that changes a discrete outcome (the
+// winning process, whether MSC limits the step or scatters, Gaussian or
+// Poisson sampling, Poisson counts, rejection-loop acceptances, the
+// delta-interaction test, the tracking cut) compares FP32 values that carry a
+// relative error of ~1e-6.  A comparison whose operands are closer than
+// kGuardTol (relative) sets `trip`: the caller then discards the track's FP32
+// result and steps it again with the FP64 code (Physics), which gives the
+// FP64 outcome bit for bit.  So the discrete outcomes of the precision form
+// are those of the FP64 path; the tripped fraction is reported.
+#pragma once
+
+#include "physics.cuh"
+
+namespace hepem {
+
+constexpr float kGuardTol = 2.44140625e-4f;  // 2^-12
+constexpr float kLargeF = 1.0E+20f;
+
+__device__ __forceinline__ float fmx(float a, float b) { return a > b ? a : b; }
+__device__ __forceinline__ float fmn(float a, float b) { return a < b ? a : b; }
+
+// ---- FP32 interpolation (the formulas of G4HepEmRunUtils.icc:49-237) --------------
+__device__ __forceinline__ float spline32(float x1, float x2, float y1, float y2, float s1, float s2, float x) {
+  const float dl = x2 - x1;
+  const float b = fmx(0.f, fmn(1.f, (x - x1) / dl));
+  const float c0 = (2.0f - b) * s1;
+  const float c1 = (1.0f + b) * s2;
+  return y1 + b * (y2 - y1) + (b * (b - 1.0f)) * (c0 + c1) * (dl * dl * 0.16666667f);
+}
+__device__ __forceinline__ int bin32(float lx, float lxm, float ild, int nd) {
+  return (int)fmx(0.f, fmn((lx - lxm) * ild, (float)(nd - 2)));
+}
+__device__ __forceinline__ float spline_log_xy32(int nd, const float* xd, const float* yd, float x, float lx,
+                                                 float lxm, float ild) {
+  const float xv = fmx(ld(xd), fmn(ld(xd + nd - 1), x));
+  const int i = bin32(lx, lxm, ild, nd);
+  return spline32(ld(xd + i), ld(xd + i + 1), ld(yd + 2 * i), ld(yd + 2 * i + 2), ld(yd + 2 * i + 1),
+                  ld(yd + 2 * i + 3), xv);
+}
+__device__ __forceinline__ float spline_log_3_32(int nd, const float* d, float x, float lx, float lxm, float ild) {
+  const float xv = fmx(ld(d), fmn(ld(d + 3 * (nd - 1)), x));
+  const int i = 3 * bin32(lx, lxm, ild, nd);
+  return spline32(ld(d + i), ld(d + i + 3), ld(d + i + 1), ld(d + i + 4), ld(d + i + 2), ld(d + i + 5), xv);
+}
+__device__ __forceinline__ int lower_bin32(const float* xd, int num, float x, int step) {
+  int ml = -1, mu = num - 1;
+  while (abs(mu - ml) > 1) {
+    const int mav = (ml + mu) / 2;
+    if (x < ld(xd + step * mav)) mu = mav; else ml = mav;
+  }
+  return mu - 1;
+}
+__device__ __forceinline__ void rotate32(float* d, const float* r) {
+  float up = r[0] * r[0] + r[1] * r[1];
+  if (up > 0.f) {
+    up = sqrtf(up);
+    const float px = d[0], py = d[1], pz = d[2];
+    d[0] = (r[0] * r[2] * px - r[1] * py) / up + r[0] * pz;
+    d[1] = (r[1] * r[2] * px + r[0] * py) / up + r[1] * pz;
+    d[2] = -up * px + r[2] * pz;
+  } else if (r[2] < 0.f) {
+    d[0] = -d[0];
+    d[2] = -d[2];
+  }
+}
+// -ln(u) for u in (0,1) to FP32 accuracy, also for u close to 1
+__device__ __forceinline__ float neg_log_u(double u) {
+  return u > 0.5 ? -log1pf(-(float)(1.0 - u)) : -logf((float)u);
+}
+
+// ---- FP32 e+- table accessors (G4HepEmElectronManager.icc:486-599) -----------------
+__device__ __forceinline__ float rest_range32(const DevElData32& f, int nL, int imc, float e, float le) {
+  return fmx(0.f, spline_log_xy32(nL, f.lossGrid, f.loss + 5 * nL * imc, e, le, f.lossLogMin, f.lossILD));
+}
+__device__ __forceinline__ float rest_dedx32(const DevElData32& f, int nL, int imc, float e, float le) {
+  return fmx(0.f, spline_log_xy32(nL, f.lossGrid, f.loss + nL * (5 * imc + 2), e, le, f.lossLogMin, f.lossILD));
+}
+__device__ __forceinline__ float inv_range32(const DevElData32& f, int nL, int imc, float r) {
+  const float* R = f.loss + 5 * nL * imc;
+  const float rmin = ld(R);
+  if (r < rmin) {
+    const float q = r / rmin;
+    return fmx(0.f, ld(f.lossGrid) * q * q);
+  }
+  const int i = lower_bin32(R, nL, r, 2);
+  const float* S2 = R + 4 * nL;
+  return fmx(0.f, spline32(ld(R + 2 * i), ld(R + 2 * (i + 1)), ld(f.lossGrid + i), ld(f.lossGrid + i + 1),
+                           ld(S2 + i), ld(S2 + i + 1), r));
+}
+__device__ __forceinline__ float transport_mfp32(const DevElData32& f, int nL, int imat, float e, float le) {
+  const float v = fmx(0.f, spline_log_xy32(nL, f.lossGrid, f.tr1 + 2 * nL * imat, e, le, f.lossLogMin, f.lossILD));
+  return v > 0.f ? 1.f / v : kLargeF;
+}
+// restricted macroscopic cross section (at the energy e, FP64 threshold tests)
+__device__ __forceinline__ float rest_macxs32(const DevElData& d, const DevElData32& f, int imc, double e, float ef,
+                                              float le, bool ioni) {
+  const int i0 = ld(d.xsStart + imc);
+  const int st = ioni ? i0 : i0 + 3 * (int)ld(d.xs + i0) + 5;
+  const int nd = (int)ld(d.xs + st);
+  if (e < ld(d.xs + st + 5)) return 0.f;
+  return fmx(0.f, spline_log_3_32(nd, f.xs + st + 5, ef, le, ld(f.xs + st + 3), ld(f.xs + st + 4)));
+}
+__device__ __forceinline__ float rest_macxs_stepping32(const DevElData& d, const DevElData32& f, int imc, double e,
+                                                       float le, bool ioni) {
+  const int i0 = ld(d.xsStart + imc);
+  const int st = ioni ? i0 : i0 + 3 * (int)ld(d.xs + i0) + 5;
+  const int nd = (int)ld(d.xs + st);
+  const double minE = ld(d.xs + st + 5), maxE = ld(d.xs + st + 1);
+  double ee = e;
+  if (e > maxE) {
+    const double er = 0.8 * e;
+    if (er < maxE) return fmx(0.f, ld(f.xs + st + 2));
+    ee = er;
+    le += -0.22314355f;  // log(0.8)
+  }
+  if (ee < minE) return 0.f;
+  return fmx(0.f, spline_log_3_32(nd, f.xs + st + 5, (float)ee, le, ld(f.xs + st + 3), ld(f.xs + st + 4)));
+}
+__device__ __forceinline__ float nuc_macxs32(const DevElData& d, const DevElData32& f, int imat, double e, float ef,
+                                             float le) {
+  if (e < ld(d.nucGrid)) return 0.f;
+  const int n = d.nNuc;
+  return fmx(0.f, spline_log_xy32(n, f.nucGrid, f.nuc + imat * 2 * n, ef, le, f.nucLogMin, f.nucILD));
+}
+__device__ __forceinline__ float annih_macxs32(float e, float ne) {
+  const float tau = e * (float)kInvMec2;
+  const float gam = tau + 1.0f;
+  const float gam2 = gam * gam;
+  const float bg2 = tau * (tau + 2.0f);
+  const float bg = sqrtf(bg2);
+  return ne * (float)kPir02 * (((gam2 + 4.f * gam + 1.f) * logf(gam + bg) - (gam + 3.f) * bg) / (bg2 * (gam + 1.f)));
+}
+
+// ---- the e+- stage A in FP32 ------------------------------------------------------------
+struct MixedEl {
+  const DevTables& T;
+  Rng& rng;
+  Track& t;
+  bool trip;
+  int tripLine;  // source line of the first guard that tripped (diagnostics)
+
+  __device__ __forceinline__ void set_trip(int line = __builtin_LINE()) {
+    if (!trip) tripLine = line;
+    trip = true;
+  }
+
+  // guarded comparisons: a < b / a <= b with a trip when the operands are too close
+  __device__ __forceinline__ void near(float a, float b, int line = __builtin_LINE()) {
+    if (fabsf(a - b) <= kGuardTol * fmx(fabsf(a), fabsf(b))) set_trip(line);
+  }
+  __device__ __forceinline__ bool lt(float a, float b, int line = __builtin_LINE()) {
+    near(a, b, line);
+    return a < b;
+  }
+  __device__ __forceinline__ bool le(float a, float b, int line = __builtin_LINE()) {
+    near(a, b, line);
+    return a <= b;
+  }
+
+  __device__ __forceinline__ const DevElData& eld() const { return t.isEl ? T.el[0] : T.el[1]; }
+  __device__ __forceinline__ const DevElData32& elf() const { return t.isEl ? T.el32[0] : T.el32[1]; }
+
+  // Gaussian of the polar method with the cached second value (rng.cuh); the
+  // acceptance test is the FP64 one of the reference, the transform FP32
+  __device__ float gauss(float mean, float sd) {
+    if (rng.gaussValid) {
+      rng.gaussValid = false;
+      return (float)rng.gaussValue * sd + mean;
+    }
+    double r, v1, v2;
+    int it = 0;
+    do {
+      const double a = rng.flat(), b = rng.flat();
+      v1 = 2. * a - 1.;
+      v2 = 2. * b - 1.;
+      r = v1 * v1 + v2 * v2;
+      if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
+    } while (r > 1.);
+    const float rf = (float)r;
+    const float fac = sqrtf(-2.f * log1pf(-(float)(1.0 - r)) / rf);
+    rng.gaussValue = (double)((float)v1 * fac);
+    rng.gaussValid = true;
+    return (float)v2 * fac * sd + mean;
+  }
+
+  __device__ int poisson(float mean) {
+    int number = 0;
+    if (le(mean, 16.f)) {
+      const float position = (float)rng.flat();
+      float pv = expf(-mean);
+      float ps = pv;
+      while (le(ps, position)) {
+        ++number;
+        pv *= mean / number;
+        ps += pv;
+        if (number >= 4096) { t.flags |= kFlagLoopCap; break; }
+      }
+      return number;
+    }
+    const double a = rng.flat(), b = rng.flat();
+    float sb, cb;
+    sincosf((float)(k2Pi * b), &sb, &cb);
+    const float tt = sqrtf(2.f * neg_log_u(a)) * cb;
+    const float value = mean + tt * sqrtf(mean) + 0.5f;
+    // the integer part is a discrete outcome: guard the distance to the nearest integer
+    const float fl = floorf(value);
+    if (value - fl < kGuardTol * fmx(1.f, value) || fl + 1.f - value < kGuardTol * fmx(1.f, value)) set_trip();
+    return value < 0.f ? 0 : value >= 2.E+9f ? (int)2.E+9 : (int)value;
+  }
+
+  __device__ float gauss_loss(float me, float s2) {
+    const float twom = 2.f * me;
+    if (lt(me * me, 0.0625f * s2)) return twom * (float)rng.flat();
+    const float sig = sqrtf(s2);
+    float el;
+    int it = 0;
+    do {
+      el = gauss(me, sig);
+      if (fabsf(el) <= kGuardTol * sig) set_trip();
+      near(el, twom);
+      if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
+    } while (el < 0.f || el > twom);
+    return el;
+  }
+
+  // Urban fluctuation model (G4HepEmElectronEnergyLossFluctuation.icc:11-111);
+  // the sum of the sampled terms is accumulated in FP64
+  __device__ double fluct(float tcut, float excE, float meanE) {
+    const float scaling = fmn(1.f + 5.E-4f / tcut, 1.5f);
+    const float meanLoss = meanE / scaling;
+    const float rate = 0.56f, e0 = 1.E-5f, nmax = 8.f;
+    const float w1 = tcut / e0;
+    float a3 = meanLoss * (tcut - e0) / (e0 * tcut * logf(w1));
+    float a1 = 0.f;
+    float e1 = excE;
+    double eloss = 0.0;
+    HEPEM_TR(1, 18, a3);
+    if (lt(excE, tcut)) {
+      const float a1t = meanLoss * (1.f - rate) / excE;
+      const float d0 = a1t < 42.f ? .1f + (4.f - .1f) * sqrtf(a1t / 42.f) : 4.f;
+      a1 = a1t / d0;
+      e1 *= d0;
+      a3 *= rate;
+      if (lt(nmax, a1)) {
+        const float em = a1 * e1;
+        eloss = gauss_loss(em, em * e1);
+      } else {
+        const int p = poisson(a1);
+        HEPEM_TR(1, 17, p);
+        eloss = p > 0 ? (double)(((float)(p + 1) - 2.f * (float)rng.flat()) * e1) : 0.;
+      }
+    }
+    if (a3 > 0.f) {
+      // The reference's differences a3 - nam, alfa - 1 and tcut - w3 cancel for
+      // thick steps (a3 >> nmax); their closed forms are used here:
+      //   alfa - 1 = a3 (w1 - 1) / (w1 nmax + a3),  nam = a3^2 / (nmax + a3),
+      //   a3 - nam = a3 nmax / (nmax + a3),  (tcut - w3) / tcut = nmax (w1 - 1) / (w1 nmax + a3)
+      float p3 = a3;
+      float alfa = 1.f;
+      float w = (w1 - 1.f) / w1;
+      if (lt(nmax, a3)) {
+        const float den = w1 * nmax + a3;
+        alfa = w1 * (nmax + a3) / den;
+        const float am1 = a3 * (w1 - 1.f) / den;
+        const float alfa1 = alfa * logf(alfa) / am1;
+        const float nam = a3 * a3 / (nmax + a3);
+        const float em = nam * e0 * alfa1;
+        const float s2 = e0 * e0 * nam * (alfa - alfa1 * alfa1);
+        eloss += gauss_loss(em, s2);
+        p3 = a3 * nmax / (nmax + a3);
+        w = nmax * (w1 - 1.f) / den;
+      }
+      const float w3 = alfa * e0;
+      if (lt(w3, tcut)) {
+        int nnb = poisson(p3);
+        HEPEM_TR(1, 19, p3);
+        HEPEM_TR(1, 20, nnb);
+        if (nnb > kMaxIter) { nnb = kMaxIter; t.flags |= kFlagLoopCap; }
+        for (int k = 0; k < nnb; ++k) eloss += (double)(w3 / (1.f - w * (float)rng.flat()));
+      }
+    }
+    return eloss * (double)scaling;
+  }
+
+  // Urban MSC cos(theta) (G4HepEmElectronInteractionUMSC.icc:153-270); the
+  // result is assembled in FP64 so that 1 - cos keeps its precision
+  __device__ double simple_scatter(float xm, float x2m) {
+    const float d0 = 3.f * x2m - 1.f;
+    const float d1 = 2.f * xm - d0;
+    const float a = 1.f + 4.f * d0 / d1;
+    const float prob = (2.f + a) * xm / a;
+    const double r0 = rng.flat(), r1 = rng.flat();
+    return lt((float)r0, prob) ? -1. + 2. * (double)powf((float)r1, 1.f / (1.f + a)) : -1. + 2. * r1;
+  }
+
+  __device__ float theta0_of(float srl, float postE, float preE, const DevMat& md) {
+    const float me = (float)kMec2;
+    const float postInv = (postE + me) / (postE * (postE + 2.f * me));
+    const float inv = preE != postE ? sqrtf(postInv * (preE + me) / (preE * (preE + 2.f * me))) : postInv;
+    float y = srl;
+    if (!t.isEl && T.mscPosCor) y = srl * pos_correction32(preE * postE, (float)ld(&md.zeff));
+    return 13.6f * sqrtf(y) * inv * ((float)ld(&md.theta[0]) + (float)ld(&md.theta[1]) * logf(y));
+  }
+
+  __device__ static float pos_correction32(float eekin, float zeff) {
+    const float ff = 1.f + zeff * (1.84035E-4f * zeff - 1.86427E-2f) + 0.41125f;
+    const float a = 0.994f - 4.08E-3f * zeff;
+    const float b = 7.16f + (52.6f + 365.f / zeff) / zeff;
+    const float tu = sqrtf(eekin) * (float)kInvMec2;
+    const float x = sqrtf(tu * (tu + 2.f) / ((tu + 1.f) * (tu + 1.f)));
+    if (x < 0.6f) return ff * a * (1.f - expf(-b * x));
+    const float c = 1.00f - 4.47E-3f * zeff;
+    const float d = 1.21E-3f * zeff;
+    if (x > 0.9f) return ff * (c + d * expf(113.0f * (x - 1.f)));
+    const float yl = a * (1.f - expf(-b * 0.6f));
+    const float yh = c + d * expf(113.0f * (0.9f - 1.f));
+    const float y0 = (yh - yl) / (0.9f - 0.6f);
+    const float y1 = yl - y0 * 0.6f;
+    return ff * (y0 * x + y1);
+  }
+
+  bool exactCos;  // cos_theta returned an exact 1.0 of the reference's own shortcuts
+
+  __device__ double cos_theta(float pstep, float preE, float preMFP, float postE, float postMFP, float tlimMin,
+                              const DevMat& md, bool pIsTlm) {
+    exactCos = false;
+    const float iPre = 1.0f / preMFP;
+    const float dR = preMFP - postMFP;
+    const float tau = lt(0.01f * preMFP, fabsf(dR)) ? pstep * logf(preMFP / postMFP) / dR : pstep * iPre;
+    if (lt(8.0f, tau)) return 2.0 * rng.flat() - 1.0;
+    if (lt(tau, 1.0E-16f)) {
+      exactCos = true;
+      return 1.0;
+    }
+    float xm, x2m;
+    if (tau < 0.01f) {
+      xm = 1.0f - tau * (1.0f - 0.5f * tau);
+      x2m = 1.0f - tau * (5.0f - 6.25f * tau) * 0.333333f;
+    } else {
+      xm = expf(-tau);
+      x2m = (1.0f + 2.0f * expf(-2.5f * tau)) * 0.333333f;
+    }
+    if (lt(postE, 0.5f * preE)) return simple_scatter(xm, x2m);
+    const float radLen = (float)ld(&md.radLength);
+    const float tsmall = fmn(tlimMin, 1.0f);
+    // pstep == tlimitMin by construction when the MSC limit chose it
+    const bool notSmall = (pIsTlm && tlimMin <= 1.0f) ? false : lt(tsmall, pstep);
+    const float theta0 = notSmall ? theta0_of(pstep / radLen, postE, preE, md)
+                                  : theta0_of(tsmall / radLen, postE, preE, md) * sqrtf(pstep / tsmall);
+    if (lt((float)kPi * 0.166666f, theta0)) return simple_scatter(xm, x2m);
+    const float th2 = theta0 * theta0;
+    if (lt(th2, 1.0E-16f)) {
+      exactCos = true;
+      return 1.0;
+    }
+    const float dumtau = notSmall ? tau : tsmall * iPre;
+    const float u = powf(dumtau, 0.1666666f);
+    const float dumxsi = (float)ld(&md.tail[0]) + u * ((float)ld(&md.tail[1]) + u * (float)ld(&md.tail[2])) +
+                         (float)ld(&md.tail[3]) * logf(pstep / (tau * radLen));
+    const float xsi = fmx(dumxsi, 1.9f);
+    // the reference moves c off the poles of its formulas at 2 and 3
+    const bool pole3 = lt(fabsf(xsi - 3.f), 0.001f), pole2 = lt(fabsf(xsi - 2.f), 0.001f);
+    const float c = pole3 ? 3.001f : pole2 ? 2.001f : xsi;
+    const float c1 = c - 1.f;
+    const float ea = expf(-xsi);
+    const float eaa = 1.f / (1.f - ea);
+    float thex = th2 * (1.0f - th2 * 0.0833333f);
+    if (th2 > 0.01f) {
+      const float q = 2.0f * sinf(0.5f * theta0);
+      thex = q * q;
+    }
+    const float xmean1 = 1.f - (1.f - (1.f + xsi) * ea) * thex * eaa;
+    if (le(xmean1, 0.999f * xm)) return simple_scatter(xm, x2m);
+    const float x0 = 1.f - xsi * thex;
+    const float bx = c * thex;
+    const float b = bx + x0;
+    const float b1 = b + 1.f;
+    const float eb1 = powf(b1, c1);
+    const float ebx = powf(bx, c1);
+    const float dd = ebx / eb1;
+    const float xmean2 = (x0 + dd - (bx - b1 * dd) / (c - 2.f)) / (1.f - dd);
+    const float f1x0 = ea * eaa;
+    const float f2x0 = c1 / (c * (1.f - dd));
+    const float prob = f2x0 / (f1x0 + f2x0);
+    const float qprb = xm / (prob * xmean1 + (1.f - prob) * xmean2);
+    const double r0 = rng.flat(), r1 = rng.flat(), r2 = rng.flat();
+    if (lt((float)r0, qprb)) {
+      if (lt((float)r1, prob)) return 1. + (double)(logf(ea + (float)r2 / eaa) * thex);
+      const float var0 = (1.0f - dd) * (float)r2;
+      if (lt(var0, 0.01f * dd)) {
+        const float var = var0 / (dd * c1);
+        return -1.0 + (double)(var * (1.0f - var * 0.5f * c) * b1);
+      }
+      return 1.0 + (double)(thex * (c - xsi - c * powf(var0 + dd, -1.f / c1)));
+    }
+    return 2.0 * r1 - 1.0;
+  }
+
+  // ---- the stage: HowFar + Perform up to the pending discrete interaction ------------
+  // Returns the interaction queue of the pending interaction or -1 (as
+  // Physics::el_perform_until_discrete).  Valid only if !trip on return.
+  __device__ int stage_a() {
+    const DevElData& d = eld();
+    const DevElData32& f = elf();
+    const int nL = d.nLoss;
+    const int imc = t.imc;
+    const DevCouple c = T.couples[imc];
+    const DevRegion& reg = T.regions[c.region];
+    const DevMat& md = T.mats[c.mat];
+    // -- HowFar (G4HepEmElectronManager.icc:35-101)
+#pragma unroll
+    for (int ip = 0; ip < 4; ++ip)
+      if (t.nia[ip] <= 0.) t.nia[ip] = (double)neg_log_u(rng.flat());
+    const double e = t.e;
+    const float ef = (float)e, lef = logf(ef);
+    const float range = rest_range32(f, nL, imc, ef, lef);
+    const float frange = (float)ld(&reg.finalRange), drange = (float)ld(&reg.dRoverRange);
+    // The step function.  Some later comparisons of the reference meet values
+    // that are equal by construction (pstep == range, trueStep == pstep,
+    // trueStep == tlimitMin); their provenance is tracked here so that those
+    // comparisons are decided exactly and only the others are guarded.
+    const bool stepFn = lt(frange, range);
+    float pstep = stepFn ? range * drange + frange * (1.0f - drange) * (2.0f - frange / range) : range;
+    bool pIsRange = !stepFn;  // pstep == range
+    HEPEM_TR(1, 0, range);
+    HEPEM_TR(1, 1, pstep);
+    int winner = -1;
+    float mx[4], mfp[4], nia[4];
+    mx[0] = rest_macxs_stepping32(d, f, imc, e, lef, true);
+    mx[1] = rest_macxs_stepping32(d, f, imc, e, lef, false);
+    mx[2] = t.isEl ? 0.f : annih_macxs32(0.8f * ef, (float)ld(&md.elDensity));
+    mx[3] = nuc_macxs32(d, f, c.mat, e, ef, lef);
+#pragma unroll
+    for (int ip = 0; ip < 4; ++ip) {
+      nia[ip] = (float)t.nia[ip];
+      mfp[ip] = mx[ip] > 0.f ? 1.f / mx[ip] : kLargeF;
+      const float lim = mfp[ip] * nia[ip];
+      if (lt(lim, pstep)) { pstep = lim; winner = ip; pIsRange = false; }
+    }
+    HEPEM_TR(1, 2, mx[0]);
+    HEPEM_TR(1, 3, mx[1]);
+    HEPEM_TR(1, 6, pstep);
+    HEPEM_TR(1, 7, winner);
+    // MSC step limit and true -> geometrical length (UMSC.icc:19-126, Manager.icc:602-650)
+    float trueStep = pstep, zPath = pstep, lambtr1 = kLargeF;
+    float delta = 0.f;  // trueStep - zPath, kept without cancellation (lateral displacement)
+    float initRange = (float)t.msc.initRange, dynFactor = (float)t.msc.dynFactor;
+    float tlimitMin = (float)t.msc.tlimitMin;
+    bool firstStep = t.msc.firstStep;
+    bool active = false, displace = false;
+    bool tsIsP = true, tsIsTlm = false;  // trueStep == pstep / == tlimitMin
+    bool atRange = pIsRange;             // trueStep == range
+    float gstep = pstep;
+    if (lt(5.E-8f, pstep) && e > 1.0E-3) {
+      active = true;
+      lambtr1 = transport_mfp32(f, nL, c.mat, ef, lef);
+      // -- step limit
+      const float kTLimitMinfix = 1.0E-8f;
+      const float safety = (float)t.safety;
+      displace = true;
+      if (lt(trueStep, kTLimitMinfix) || lt(range * (float)ld(&md.umscPar), safety)) {
+        displace = false;
+      } else {
+        const float rf = (float)ld(&reg.mscRangeFactor), sf = (float)ld(&reg.mscSafetyFactor);
+        float tlimit;
+        bool tlimIsRange = false, tlimIsTlm = false;  // tlimit == range / == tlimitMin
+        if (!ld(&reg.mscMinimal)) {
+          if (firstStep || t.onBoundary) {
+            const float l1 = lambtr1;
+            initRange = fmx(range, l1);
+            dynFactor = l1 > 1.0f ? rf * (0.75f + 0.25f * l1) : rf;
+            const float stepMin = l1 * 1.0E-3f /
+                (2.0E-3f + ef * ((float)ld(&md.stepMin[0]) + ef * (float)ld(&md.stepMin[1])));
+            const float d0 = t.isEl ? 0.87f * (float)ld(&md.zeff23) : 0.70f * (float)ld(&md.zeffSqrt);
+            const float d1 = e > 5.0E-3 ? d0 * stepMin : d0 * stepMin * 0.5f * (1.0f + ef * 200.0f);
+            tlimitMin = fmx(d1, kTLimitMinfix);
+            firstStep = false;
+          }
+          float cand;
+          if (lt(safety, range)) {
+            cand = fmx(initRange * dynFactor, sf * safety);
+            tlimIsRange = false;
+          } else {
+            cand = range;
+            tlimIsRange = true;
+          }
+          near(cand, tlimitMin);
+          tlimIsTlm = !(cand > tlimitMin);
+          tlimIsRange = tlimIsRange && !tlimIsTlm;
+          tlimit = fmx(cand, tlimitMin);
+        } else {
+          if (t.onBoundary) {
+            const float tmp = range > lambtr1 ? rf * range : rf * lambtr1;
+            initRange = fmx(tmp, 10.f * kTLimitMinfix);
+          }
+          tlimit = initRange;
+        }
+        // reference: if (tlimit < trueStep) { d0 = tlimit > tlimitMin ? max(gauss, tlimitMin) : tlimitMin;
+        //                                     trueStep = min(d0, trueStep) }
+        const bool limits = (tlimIsRange && pIsRange) ? false : lt(tlimit, trueStep);
+        if (limits) {
+          float d0;
+          bool d0IsTlm;
+          if (!tlimIsTlm && lt(tlimitMin, tlimit)) {
+            const float gs = gauss(tlimit, 0.1f * (tlimit - tlimitMin));
+            near(gs, tlimitMin);
+            d0IsTlm = !(gs > tlimitMin);
+            d0 = fmx(gs, tlimitMin);
+          } else {
+            d0 = tlimitMin;
+            d0IsTlm = true;
+          }
+          near(d0, trueStep);
+          if (d0 < trueStep) {
+            trueStep = d0;
+            tsIsP = false;
+            tsIsTlm = d0IsTlm;
+          }
+        }
+      }
+      HEPEM_TR(1, 8, lambtr1);
+      HEPEM_TR(1, 10, trueStep);
+      // -- true -> geometrical.  trueStep <= pstep <= range: trueStep == range
+      // only by construction (the reference then takes its trueStep == range branch)
+      atRange = tsIsP && pIsRange;
+      if (!atRange) near(trueStep, range);
+      trueStep = fmn(trueStep, range);
+      zPath = trueStep;
+      if (!lt(trueStep, 1.0E-6f)) {
+        const float tau = trueStep / lambtr1;
+        if (lt(tau, 1.0e-16f)) {
+          zPath = fmn(trueStep, lambtr1);
+        } else if (lt(trueStep, range * 0.05f)) {
+          // zPath = lambda (1 - exp(-tau)); trueStep - zPath = lambda g(tau),
+          // g = exp(-tau) - 1 + tau, by its series where it cancels
+          const float g = tau < 0.1f
+              ? tau * tau * (0.5f - tau * (0.16666667f - tau * (0.041666668f - tau * (0.0083333338f - tau *
+                                                                                    0.0013888889f))))
+              : tau + expm1f(-tau);
+          delta = lambtr1 * g;
+          zPath = trueStep - delta;
+          // below ~1e-12 the reference's own rounding decides whether zPath < trueStep
+          if (tau < 1.0e-12f) set_trip();
+        } else {
+          // the range-based conversions: evaluated in FP64 from the FP32 inputs,
+          // so that trueStep - zPath (the displacement length) keeps the
+          // inputs' relative accuracy where zPath is close to trueStep
+          const double R = range, L = lambtr1, ts = trueStep;
+          double z;
+          if (e < kMec2 || atRange) {
+            const double par1 = 1. / R;
+            const double par3 = 1. + 1. / (par1 * L);
+            z = 1. / (par1 * par3);
+            if (!atRange) z *= -expm1(par3 * log1p(-ts / R));
+          } else {
+            const float rfin = fmx(range - trueStep, 0.01f * range);
+            const float t1 = inv_range32(f, nL, imc, rfin);
+            const double l1 = transport_mfp32(f, nL, c.mat, t1, logf(t1));
+            const double par1 = (L - l1) / (L * ts);
+            const double par3 = 1. + 1. / (par1 * L);
+            z = -expm1(par3 * log(l1 / L)) / (par1 * par3);
+          }
+          const double dz = ts - z;
+          // the reference displaces only when zPath < trueStep
+          if (dz < 1.0e-9 * ts) set_trip();
+          zPath = (float)z;
+          delta = (float)dz;
+        }
+        if (delta == 0.f) delta = trueStep - zPath;
+        if (zPath > lambtr1) {
+          zPath = lambtr1;
+          delta = trueStep - zPath;
+        }
+      }
+      HEPEM_TR(1, 11, zPath);
+      if (!tsIsP) {  // the MSC limit is below the proposed step
+        winner = -2;
+        pstep = trueStep;
+      }
+      gstep = fmn(zPath, pstep);
+      // the geometrical step equals zPath here (zPath <= true length <= pstep);
+      // the geometry-shortened case of the reference is left to the FP64 code
+      if (gstep < zPath) set_trip();
+    }
+    t.winner = winner;
+    t.gstep = (double)gstep;
+    t.msc.initRange = (double)initRange;
+    t.msc.dynFactor = (double)dynFactor;
+    t.msc.tlimitMin = (double)tlimitMin;
+    t.msc.firstStep = firstStep;
+    t.msc.disp[0] = t.msc.disp[1] = t.msc.disp[2] = 0.;
+#pragma unroll
+    for (int ip = 0; ip < 4; ++ip) t.mfp[ip] = (double)mfp[ip];
+
+    // -- Perform: continuous part (G4HepEmElectronManager.icc:375-405).  With
+    // no geometry the geometrical step is the one HowFar proposed, so the
+    // true length is the MSC true length.
+    t.edep = 0.0;
+    t.pstep = t.gstep;
+    if (!(gstep > 0.f)) return -1;
+    float p = gstep;
+    bool pAtRange = pIsRange && winner == -1;  // p == range
+    if (active) {
+      p = trueStep;
+      pAtRange = atRange;
+      if (le(p, 5.E-8f) || atRange) active = false;
+    }
+    t.pstep = (double)p;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) t.nia[i] = (double)(nia[i] - p / mfp[i]);
+    // mean energy loss (G4HepEmElectronManager.icc:216-259); the range->energy
+    // inversion in FP64
+    const double preE = e;
+    const float preEf = ef;
+    if (pAtRange || e <= T.minLossE) {
+      t.edep = e;
+      t.setE(0.0);
+      return t.isEl ? -1 : kQAnnihRest;
+    }
+    double eloss = (double)(p * rest_dedx32(f, nL, imc, ef, lef));
+    if (lt((float)((double)ld(&reg.linELossLimit) * e), (float)eloss)) {
+      const double le64 = vdt_log(e);
+      const double range64 = dmax_(0.0, spline_log_xy(nL, d.lossGrid, d.loss + 5 * nL * imc, e, le64, d.lossLogMin,
+                                                      d.lossILD));
+      eloss = e - inv_range(d, imc, range64 - (double)p);
+      // E(range - p) is ill-conditioned when p is close to the range: its
+      // relative error is that of p times range / (range - p); keep <= 8x
+      if (range - p < 0.125f * range) set_trip();
+    }
+    eloss = dmax_(eloss, 0.0);
+    HEPEM_TR(1, 14, eloss);
+    if (eloss >= e) {  // only after the inversion, where p close to the range has tripped
+      t.setE(0.0);
+      t.edep = e;
+      return t.isEl ? -1 : kQAnnihRest;
+    }
+    double postE = e - eloss;
+    t.setE(postE);
+    t.edep = eloss;
+    // MSC angular deflection and displacement (G4HepEmElectronManager.icc:261-322)
+    if (active && lt(fmx(1.0E-8f, 1.0e-16f * lambtr1), p)) {
+      float pE = preEf, pLE = lef;
+      if (lt(range * 0.01f, p)) {
+        pE = (float)postE;
+        pLE = logf(pE);
+      }
+      const float postMFP = transport_mfp32(f, nL, c.mat, pE, pLE);
+      const double cost = cos_theta(p, preEf, lambtr1, pE, postMFP, tlimitMin, md, tsIsTlm);
+      HEPEM_TR(1, 21, cost);
+      // the reference skips the deflection when cos(theta) rounds to +-1 in
+      // FP64: a computed value within a few ulp of that is undecidable here
+      if (!exactCos && 1.0 - fabs(cost) < 1.0E-15) set_trip();
+      if (fabs(cost) < 1.0) {
+        const double sth = sqrt((1.0 - cost) * (1.0 + cost));
+        const double uphi = rng.flat();
+        const float phi = (float)k2Pi * (float)uphi;
+        float sp, cp;
+        sincosf(phi, &sp, &cp);
+        float dir[3] = {(float)sth * cp, (float)sth * sp, (float)cost};
+        const float tdir[3] = {(float)t.dir[0], (float)t.dir[1], (float)t.dir[2]};
+        float disp[3] = {0.f, 0.f, 0.f};
+        bool dsp = displace && T.mscDisplacement;
+        if (dsp && delta > 0.f) {
+          const float r = 0.73f * sqrtf(delta * (p + zPath));
+          const float cbeta = 2.16f;
+          const float cbeta1 = -expm1f(-cbeta * (float)kPi);
+          const double r0 = rng.flat(), r1 = rng.flat();
+          const float psi = -log1pf(-(float)r0 * cbeta1) / cbeta;
+          const float ph = lt((float)r1, 0.5f) ? phi + psi : phi - psi;
+          float s2, c2;
+          sincosf(ph, &s2, &c2);
+          disp[0] = r * c2;
+          disp[1] = r * s2;
+          rotate32(disp, tdir);
+        } else {
+          dsp = false;
+        }
+        rotate32(dir, tdir);
+        // renormalise in FP64 so that repeated steps keep unit directions
+        const double nx = dir[0], ny = dir[1], nz = dir[2];
+        const double inv = 1.0 / sqrt(nx * nx + ny * ny + nz * nz);
+        t.dir[0] = nx * inv;
+        t.dir[1] = ny * inv;
+        t.dir[2] = nz * inv;
+        if (dsp) {
+          t.msc.disp[0] = disp[0];
+          t.msc.disp[1] = disp[1];
+          t.msc.disp[2] = disp[2];
+        }
+      }
+    }
+    // energy loss fluctuations (G4HepEmElectronManager.icc:324-368)
+    double finalE = postE;
+    if (ld(&T.regions[c.region].eLossFluct) && lt(1.E-5f, (float)eloss)) {
+      const float tmax = t.isEl ? 0.5f * preEf : preEf;
+      const float tcut = fmn((float)c.elCut, tmax);
+      eloss = dmax_(fluct(tcut, (float)ld(&md.meanExc), (float)eloss), 0.0);
+      finalE = preE - eloss;
+      HEPEM_TR(1, 15, eloss);
+      // the final energy inherits eloss's relative error times eloss / finalE
+      if (finalE < 0.125 * preE) set_trip();
+    }
+    if (le((float)finalE, (float)T.elTrackingCut)) {
+      t.setE(0.0);
+      t.edep = preE;
+      return t.isEl ? -1 : kQAnnihRest;
+    }
+    t.setE(finalE);
+    t.edep = eloss;
+    // the delta-interaction test (G4HepEmElectronManager.icc:408-423)
+    const int ip = t.winner;
+    if (ip < 0 || t.onBoundary) return -1;
+    t.nia[ip] = -1.0;
+    const float fe = (float)finalE, lfe = logf(fe);
+    const float mxp = ip < 2 ? rest_macxs32(d, f, imc, finalE, fe, lfe, ip == 0)
+                   : (ip < 3 ? annih_macxs32(fe, (float)ld(&md.elDensity)) : nuc_macxs32(d, f, c.mat, finalE, fe, lfe));
+    const double u = rng.flat();
+    if (mxp <= 0.f || !lt((float)u, mxp * mfp[ip])) return -1;
+    switch (ip) {
+      case 0: return t.isEl ? kQIoniEm : kQIoniEp;
+      case 1: near(fe, (float)T.bremModelLim); return finalE < T.bremModelLim ? kQBremSB : kQBremRB;
+      case 2: return kQAnnihFlight;
+      default: return -1;
+    }
+  }
+};
+
+// ---- stage B of the precision form: the costly interaction models ---------------------
+// Bethe-Heitler pair production, Seltzer-Berger and relativistic brem, the
+// modified-Tsai angles, Moller/Bhabha and Klein-Nishina Compton with their
+// rejection functions in FP32; FP64 is kept for the kinematic limits (e.g.
+// eps0 = m c^2 / E, the photon-energy sampling of the relativistic model near
+// the dielectric cut-off, the positron-correction velocities near the end
+// point), the target-element selection and the energy bookkeeping.  Guards as
+// in MixedEl: a tripped track is left to the FP64 interaction kernel.
+struct MixedB {
+  const DevTables& T;
+  Rng& rng;
+  Track& t;
+  bool trip;
+  int tripLine;  // source line of the first guard that tripped (diagnostics)
+
+  __device__ __forceinline__ void set_trip(int line = __builtin_LINE()) {
+    if (!trip) tripLine = line;
+    trip = true;
+  }
+
+  __device__ __forceinline__ void near(float a, float b, int line = __builtin_LINE()) {
+    if (fabsf(a - b) <= kGuardTol * fmx(fabsf(a), fabsf(b))) set_trip(line);
+  }
+  __device__ __forceinline__ void neard(double a, double b, int line = __builtin_LINE()) {
+    if (fabs(a - b) <= (double)kGuardTol * fmax(fabs(a), fabs(b))) set_trip(line);
+  }
+  __device__ __forceinline__ bool lt(float a, float b, int line = __builtin_LINE()) {
+    near(a, b, line);
+    return a < b;
+  }
+  __device__ __forceinline__ const DevElData& eld() const { return t.isEl ? T.el[0] : T.el[1]; }
+  __device__ __forceinline__ const DevCouple& couple() const { return T.couples[t.imc]; }
+
+  // modified-Tsai polar angle (G4HepEmInteractionUtils.icc:10-22); 1 - cos in FP32
+  __device__ double tsai_cost(double E) {
+    const float umax = 2.0f * (1.0f + (float)(E * kInvMec2));
+    float u;
+    int it = 0;
+    do {
+      const double r0 = rng.flat(), r1 = rng.flat(), r2 = rng.flat();
+      const float uu = neg_log_u(r0 * r1);
+      u = 0.25 > r2 ? uu * 1.6f : uu * 0.533333333f;
+      near(u, umax);
+      if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
+    } while (u > umax);
+    return 1.0 - (double)(2.0f * u * u / (umax * umax));
+  }
+
+  // the e+- target element of a brem model: the FP64 interpolation of the
+  // reference selector, guarded because E carries the FP32 continuous loss
+  __device__ int select_brem_target(double E, double le, double u, int which) {
+    const DevElData& d = eld();
+    const int st = ld(d.selStart[which] + t.imc);
+    const double* D = d.sel[which] + st;
+    const int nd = (int)ld(D);
+    const int ne = (int)ld(D + 1);
+    const double* x = D + 4;
+    const double xv = dmax_(ld(x), dmin_(ld(x + ne * (nd - 1)), E));
+    const double fi = dmax_(0.0, dmin_((le - ld(D + 2)) * ld(D + 3), nd - 2.0));
+    const int ie = (int)fi;
+    if (fi - ie < 1e-6 || fi - ie > 1.0 - 1e-6) set_trip();
+    int i0 = ie * ne, i1 = i0 + ne;
+    const double x1 = ld(x + i0++), x2 = ld(x + i1++);
+    const double b = dmax_(0., dmin_(1., (xv - x1) / (x2 - x1)));
+    int k = 0;
+    while (k < ne - 1) {
+      const double c = ld(x + i0 + k) + b * (ld(x + i1 + k) - ld(x + i0 + k));
+      neard(u, c);
+      if (!(u > c)) break;
+      ++k;
+    }
+    return k;
+  }
+
+  // ---- Moller / Bhabha (G4HepEmElectronInteractionIoni.icc:19-138) ------------------
+  __device__ void ioni() {
+    const double E = t.e;
+    const double cut = couple().elCut;
+    const double tmaxE = t.isEl ? 0.5 * E : E;
+    neard(tmaxE, cut);
+    if (tmaxE <= cut) return;
+    const float Ef = (float)E;
+    const float xmin = (float)(cut / E);
+    float x, omx = 1.f;
+    int it = 0;
+    if (t.isEl) {
+      const float xmax = 0.5f;
+      const float gam = Ef * (float)kInvMec2 + 1.0f;
+      const float g2 = gam * gam;
+      const float xmm = xmin * xmax;
+      const float gg = (2.0f * gam - 1.0f) / g2;
+      const float y = 1.f - xmax;
+      const float gf = 1.0f - gg * xmax + xmax * xmax * (1.0f - gg + (1.0f - gg * y) / (y * y));
+      float dum, g;
+      do {
+        const double r0 = rng.flat(), r1 = rng.flat();
+        x = xmm / (xmin * (float)(1.0 - r0) + xmax * (float)r0);
+        const float xx = 1.0f - x;
+        dum = 1.0f - gg * x + x * x * (1.0f - gg + (1.0f - gg * xx) / (xx * xx));
+        g = gf * (float)r1;
+        near(g, dum);
+        if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
+      } while (g > dum);
+    } else {
+      const float xmax = 1.0f;
+      const float gam = Ef * (float)kInvMec2 + 1.0f;
+      const float g2 = gam * gam;
+      const float b2 = 1.f - 1.f / g2;
+      const float xmm = xmin * xmax;
+      const float y = 1.0f / (1.0f + gam);
+      const float y2 = y * y;
+      const float y12 = 1.0f - 2.0f * y;
+      const float c1 = 2.0f - y2;
+      const float c2 = y12 * (3.0f + y2);
+      const float y122 = y12 * y12;
+      const float c4 = y122 * y12;
+      const float c3 = c4 + y122;
+      const float xmax2 = xmax * xmax;
+      const float gf = 1.0f + (xmax2 * c4 - xmin * xmin * xmin * c3 + xmax2 * c2 - xmin * c1) * b2;
+      float dum, g;
+      do {
+        const double r0 = rng.flat(), r1 = rng.flat();
+        const float den = xmin * (float)(1.0 - r0) + xmax * (float)r0;
+        x = xmm / den;
+        omx = (float)r0 * (1.f - xmin) / den;  // 1 - x, xmax = 1
+        const float xx = x * x;
+        dum = 1.0f + (xx * xx * c4 - x * xx * c3 + xx * c2 - x * c1) * b2;
+        g = gf * (float)r1;
+        near(g, dum);
+        if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
+      } while (g > dum);
+    }
+    const double dE = (double)x * E;
+    Sec& s = t.addSec(0);
+    // kinematics in FP64 (cos close to 1 at high energy)
+    const double eTot = E + kMec2;
+    const double pTot = sqrt(E * (eTot + kMec2));
+    const double dP = sqrt(dE * (dE + 2.0 * kMec2));
+    const double cost = dE * (eTot + kMec2) / (dP * pTot);
+    const double ct = dmax_(-1.0, dmin_(cost, 1.0));
+    const double st = sqrt((1.0 - ct) * (1.0 + ct));
+    float sp, cp;
+    sincosf((float)k2Pi * (float)rng.flat(), &sp, &cp);
+    s.dir[0] = st * cp;
+    s.dir[1] = st * sp;
+    s.dir[2] = ct;
+    rotate(s.dir, t.dir);
+    t.dir[0] = pTot * t.dir[0] - dP * s.dir[0];
+    t.dir[1] = pTot * t.dir[1] - dP * s.dir[1];
+    t.dir[2] = pTot * t.dir[2] - dP * s.dir[2];
+    const double nrm = 1.0 / sqrt(t.dir[0] * t.dir[0] + t.dir[1] * t.dir[1] + t.dir[2] * t.dir[2]);
+    t.dir[0] *= nrm; t.dir[1] *= nrm; t.dir[2] *= nrm;
+    t.setE(!t.isEl && omx < 0.5f ? E * (double)omx : E - dE);
+    s.e = dE;
+  }
+
+  // ---- bremsstrahlung (G4HepEmElectronInteractionBrem.icc:35-344) -------------------
+  // 1 - k/E of the last sample_sb, kept without cancellation (photon taking
+  // nearly all the energy); < 0: not set, the electron keeps E - k
+  double omk;
+
+  __device__ void brem(bool sbModel) {
+    const double E = t.e;
+    const double le = vdt_log(E);
+    neard(E, couple().gamCut);
+    if (E <= couple().gamCut) return;
+    omk = -1.0;
+    const double k = sbModel ? sample_sb(E, le) : sample_rb(E, le);
+    Sec& s = t.addSec(2);
+    const double cost = tsai_cost(E);
+    const double sint = sqrt((1.0 - cost) * (1.0 + cost));
+    float sp, cp;
+    sincosf((float)k2Pi * (float)rng.flat(), &sp, &cp);
+    s.dir[0] = sint * cp;
+    s.dir[1] = sint * sp;
+    s.dir[2] = cost;
+    rotate(s.dir, t.dir);
+    const double eTot = E + kMec2;
+    const double pTot = sqrt(E * (eTot + kMec2));
+    t.dir[0] = pTot * t.dir[0] - k * s.dir[0];
+    t.dir[1] = pTot * t.dir[1] - k * s.dir[1];
+    t.dir[2] = pTot * t.dir[2] - k * s.dir[2];
+    const double nrm = 1.0 / sqrt(t.dir[0] * t.dir[0] + t.dir[1] * t.dir[1] + t.dir[2] * t.dir[2]);
+    t.dir[0] *= nrm; t.dir[1] *= nrm; t.dir[2] *= nrm;
+    t.setE(omk >= 0.0 && omk < 0.5 ? E * omk : E - k);
+    s.e = k;
+  }
+
+  __device__ double sample_sb(double E, double le) {
+    const DevCouple c = couple();
+    const double gcut = c.gamCut, lgcut = c.logGamCut;
+    const DevMat& md = T.mats[c.mat];
+    const int nElem = ld(&md.nElem);
+    const int ei = nElem > 1 ? select_brem_target(E, le, rng.flat(), 1) : 0;
+    const int Z = ld(T.matElemZ + ld(&md.elemOff) + ei);
+    const DevSB& sb = T.sb;
+    const int st = ld(sb.startPerZ + Z);
+    const int gci = ld(sb.gcIdx + ld(sb.gcStart + t.imc) + ei);
+    bool corner = false, simple = false;
+    int ie = (int)ld(sb.data + st + 2);
+    neard(E, ld(sb.elE + ie));
+    if (E < ld(sb.elE + ie)) {
+      const double val = (le - sb.logMinE) * sb.ildE;
+      ie = (int)val;
+      double pH = val - ie;
+      if (pH < 1e-6 || pH > 1.0 - 1e-6) set_trip();
+      if (ie < 0 || ie > kNumElEnergySB - 2) { t.flags |= kFlagBadIndex; return E; }
+      if (ld(sb.elE + ie) <= gcut) {
+        pH = (le - lgcut) / (ld(sb.lelE + ie + 1) - lgcut);
+        corner = true;
+      }
+      const double u = rng.flat();
+      neard(u, pH);
+      if (u < pH) ++ie;
+      else if (corner) simple = true;
+    }
+    const int minIE = (int)ld(sb.data + st + 1);
+    const int maxIE = (int)ld(sb.data + st + 2);
+    if (ie < minIE || ie > maxIE) { t.flags |= kFlagBadIndex; return E; }
+    const int ncut = (int)ld(sb.data + st + 3);
+    const int size1 = ncut + 3 * kNumKappaSB;
+    const int tst = st + 4 + (ie - minIE) * size1;
+    const double minV = ld(sb.data + tst + gci);
+    const double* Tb = sb.data + tst + ncut;
+    const float lkt = (float)((lgcut - le) / (lgcut - ld(sb.lelE + ie)));
+    const float Ef = (float)E;
+    const float pe = Ef + (float)kMec2;
+    const float dsc = (float)ld(&md.densityCor) * pe * pe;
+    // positron correction: the velocity at E - gcut is fixed, the one at E - k
+    // is evaluated in FP64 (kinematic end point k -> E)
+    double ib1 = 0.0;
+    if (!t.isEl) {
+      const double e1 = E - gcut;
+      ib1 = (e1 + kMec2) / sqrt(e1 * (e1 + 2.0 * kMec2));
+    }
+    const float zfac = (float)(kAlpha * k2Pi * (double)Z);
+    double k = 0.0;
+    float sup = 1.0f;
+    double r1;
+    int it = 0;
+    do {
+      const double r0 = rng.flat();
+      r1 = rng.flat();
+      float kappa = 1.0f;
+      if (!simple) {
+        const double cum = r0 * (1.0 - minV) + minV;
+        int i3 = Physics::lin_search(Tb, kNumKappaSB, cum) - 3;
+        if (i3 > 3 * (kNumKappaSB - 2)) { i3 = 3 * (kNumKappaSB - 2); t.flags |= kFlagBadIndex; }
+        if (i3 < 0) { i3 = 0; t.flags |= kFlagBadIndex; }
+        const int i = i3 / 3;
+        const double cL = ld(Tb + i3), cH = ld(Tb + i3 + 3);
+        const float pA = (float)ld(Tb + i3 + 1), pB = (float)ld(Tb + i3 + 2);
+        const float lKL = (float)ld(sb.lkappa + i), lKH = (float)ld(sb.lkappa + i + 1);
+        const float m1 = (float)((cum - cL) / (cH - cL));
+        const float m2 = (1.0f + pA + pB) * m1;
+        const float m3 = 1.0f + m1 * (pA + pB * m1);
+        const float lk = lKL + m2 / m3 * (lKH - lKL);
+        kappa = expf(lk * lkt);
+        k = (double)kappa * E;
+        omk = (double)(-expm1f(lk * lkt));
+      } else {
+        const double om = r0 * (1.0 - gcut / E);
+        k = (1.0 - om) * E;
+        omk = om;
+      }
+      const float kf = (float)k;
+      const float ik = 1.0f / kf;
+      sup = 1.0f / (1.0f + dsc * ik * ik);
+      if (!t.isEl) {
+        const double e2 = omk >= 0.0 && omk < 0.5 ? E * omk : E - k;
+        const double ib2 = (e2 + kMec2) / sqrt(e2 * (e2 + 2.0 * kMec2));
+        const float dum = zfac * (float)(ib1 - ib2);
+        near(dum, -12.f);
+        sup = dum > -12.f ? sup * expf(dum) : 0.f;
+      }
+      near((float)r1, sup);
+      if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
+    } while ((float)r1 > sup);
+    return k;
+  }
+
+  __device__ static void lpm_functions32(float& xiS, float& gS, float& phiS, float eg, float et, float elpm,
+                                         float z23, float ilS1, float ilS1c, float dcor, float times) {
+    const float sqrt2 = 1.41421356f;
+    const float red = eg / et;
+    const float sP = sqrtf(0.125f * red * elpm / (times * (1.0f - red) * et));
+    const float s1 = z23 / (184.15f * 184.15f);
+    const float cond = sqrt2 * s1;
+    float xiSP = 2.0f;
+    if (sP > 1.0f) {
+      xiSP = 1.0f;
+    } else if (sP > cond) {
+      const float h = logf(sP) * ilS1c;
+      xiSP = 1.0f + h - 0.08f * (1.0f - h) * h * (2.0f - h) * ilS1c;
+    }
+    xiS = xiSP;
+    const float s = sP / sqrtf(xiSP);
+    float sh = s;
+    if (dcor != 0.0f) {
+      sh *= (1.0f + dcor / (eg * eg));
+      xiS = 2.0f;
+      if (sh > 1.0f) xiS = 1.0f;
+      else if (sh > s1) xiS = 1.0f + logf(sh) * ilS1;
+    }
+    if (sh < 2.0f) {
+      float val = sh * 20.0f;
+      int il = (int)val;
+      val -= il;
+      il *= 2;
+      il = il < 0 ? 0 : (il > 78 ? 78 : il);
+      const float f0 = (float)kFuncLPM[il], f1 = (float)kFuncLPM[il + 1];
+      gS = ((float)kFuncLPM[il + 2] - f0) * val + f0;
+      phiS = ((float)kFuncLPM[il + 3] - f1) * val + f1;
+    } else {
+      float ss = 1.0f / (sh * sh);
+      ss *= ss;
+      gS = 1.0f - 0.0230655f * ss;
+      phiS = 1.0f - 0.01190476f * ss;
+    }
+    if (xiS * phiS > 1.0f || sh > 0.57f) xiS = 1.0f / phiS;
+  }
+
+  __device__ double sample_rb(double E, double le) {
+    const DevCouple c = couple();
+    const double gcut = c.gamCut;
+    const DevMat& md = T.mats[c.mat];
+    const int nElem = ld(&md.nElem);
+    const int ei = nElem > 1 ? select_brem_target(E, le, rng.flat(), 2) : 0;
+    const int Z = ld(T.matElemZ + ld(&md.elemOff) + ei);
+    const float dZ = (float)Z;
+    const DevElem& el = T.elems[Z < kMaxZ ? Z : kMaxZ];
+    const double dens = kMigdal * ld(&md.elDensity);
+    const double lpmE = kLPM * ld(&md.radLength);
+    const double lpmLim = sqrt(dens) * lpmE;
+    const double pte = E + kMec2;
+    const double dcor = dens * pte * pte;
+    neard(pte, lpmLim);
+    const bool lpm = pte > lpmLim;
+    const float zf1 = (float)ld(&el.zFactor1);
+    const float zf2 = (1.f + 1.f / dZ) / 12.f;
+    const float fmax = zf1 + zf2;
+    // photon energy from the kinematic limits: FP64
+    const double xmin = vdt_log(gcut * gcut + dcor);
+    const double xr = vdt_log(E * E + dcor) - xmin;
+    const float ptef = (float)pte, lpmEf = (float)lpmE, dcorf = (float)dcor;
+    const float z23 = (float)ld(&el.Z23), ilS1 = (float)ld(&el.ilVarS1), ilS1c = (float)ld(&el.ilVarS1Cond);
+    const float z13 = (float)ld(&el.Z13), lz = (float)ld(&el.logZ), coul = (float)ld(&el.coulomb);
+    double k, r1;
+    float fv, g;
+    int it = 0;
+    do {
+      const double r0 = rng.flat();
+      r1 = rng.flat();
+      k = sqrt(dmax_(vdt_exp(xmin + r0 * xr) - dcor, 0.0));
+      const float kf = (float)k;
+      const float y = kf / ptef;
+      const float omy = 1.f - y;
+      const float d0 = 0.25f * y * y;
+      if (lpm) {
+        float xiS, gS, phiS;
+        lpm_functions32(xiS, gS, phiS, kf, ptef, lpmEf, z23, ilS1, ilS1c, dcorf, 1.0f);
+        const float t1 = xiS * (d0 * gS + (omy + 2.0f * d0) * phiS);
+        fv = t1 * zf1 + omy * zf2;
+      } else {
+        const float d1 = omy + 3.f * d0;
+        if (Z < 5) {
+          fv = d1 * zf1 + omy * zf2;
+        } else {
+          const float d2 = y / (float)(pte - k);
+          const float gam = d2 * 100.f * (float)kMec2 / z13;
+          const float eps = gam / z13;
+          const float g2 = gam * gam;
+          const float phi1 = 16.863f - 2.0f * log1pf(0.311877f * g2) + 2.4f * expf(-0.9f * gam) +
+                             1.6f * expf(-1.5f * gam);
+          const float phi2 = 2.0f / (3.0f + 19.5f * gam + 18.0f * g2);
+          const float e2 = eps * eps;
+          const float psi1 = 24.34f - 2.0f * log1pf(13.111641f * e2) + 2.8f * expf(-8.0f * eps) +
+                             1.2f * expf(-29.2f * eps);
+          const float psi2 = 2.0f / (3.0f + 120.0f * eps + 1200.0f * e2);
+          const float Fz = lz / 3.f + coul;
+          const float iz = 1.f / dZ;
+          fv = d1 * ((0.25f * phi1 - Fz) + (0.25f * psi1 - 2.f * lz / 3.f) * iz) + 0.125f * omy * (phi2 + psi2 * iz);
+        }
+      }
+      fv = fmx(0.0f, fv);
+      g = fmax * (float)r1;
+      near(fv, g);
+      if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
+    } while (fv < g);
+    return k;
+  }
+
+  // ---- annihilation in flight (G4HepEmPositronInteractionAnnihilation.icc) -----------
+  // the FP64 model (it is cheap) with its rejection test guarded
+  __device__ void annihilate_in_flight() {
+    const double E = t.e;
+    Sec& g1 = t.addSec(2);
+    Sec& g2 = t.addSec(2);
+    const double tau = E * kInvMec2;
+    const double gam = tau + 1.0;
+    const double tau2 = tau + 2.0;
+    const double sq = sqrt(tau / tau2) * 0.5;
+    const double emin = 0.5 - sq, emax = 0.5 + sq;
+    const double eq = emax / emin;
+    const double tau4 = tau2 * tau2;
+    double eps, rf, r1;
+    int it = 0;
+    do {
+      const double r0 = rng.flat();
+      r1 = rng.flat();
+      eps = emin * vdt_exp(vdt_log(eq) * r0);
+      rf = 1. - eps + (2. * gam * eps - 1.) / (eps * tau4);
+      neard(rf, r1);
+      if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
+    } while (rf < r1);
+    const double sqg = sqrt(tau * tau2);
+    const double cost = dmin_(1., dmax_(-1., (eps * tau2 - 1.) / (eps * sqg)));
+    const double sint = sqrt((1. + cost) * (1. - cost));
+    const double phi = k2Pi * rng.flat();
+    const double initE = E + 2. * kMec2;
+    const double e1 = eps * initE;
+    g1.e = e1;
+    double sp, cp;
+    sincos(phi, &sp, &cp);
+    g1.dir[0] = sint * cp;
+    g1.dir[1] = sint * sp;
+    g1.dir[2] = cost;
+    rotate(g1.dir, t.dir);
+    g2.e = initE - e1;
+    const double ip = sqrt(E * (E + 2 * kMec2));
+    const double px = ip * t.dir[0] - g1.dir[0] * e1;
+    const double py = ip * t.dir[1] - g1.dir[1] * e1;
+    const double pz = ip * t.dir[2] - g1.dir[2] * e1;
+    const double nrm = 1.0 / sqrt(px * px + py * py + pz * pz);
+    g2.dir[0] = px * nrm; g2.dir[1] = py * nrm; g2.dir[2] = pz * nrm;
+    t.setE(0.0);
+  }
+
+  // ---- pair production (G4HepEmGammaInteractionConversion.icc:19-274) ---------------
+  __device__ static float screen1(float d) {
+    return d > 1.4f ? 42.038f - 8.29f * logf(d + 0.958f) : 42.184f - d * (7.444f - 1.623f * d);
+  }
+  __device__ static float screen2(float d) {
+    return d > 1.4f ? 42.038f - 8.29f * logf(d + 0.958f) : 41.326f - d * (5.848f - 0.902f * d);
+  }
+  __device__ static void phi12(float d, float& p1, float& p2) {
+    if (d > 1.4f) {
+      p1 = 21.0190f - 4.145f * logf(d + 0.958f);
+      p2 = p1;
+    } else {
+      p1 = 20.806f - d * (3.190f - 0.5710f * d);
+      p2 = 20.234f - d * (2.126f - 0.0903f * d);
+    }
+  }
+
+  __device__ void conversion() {
+    const double E = t.e;
+    if (E < 2. * kMec2) return;
+    const double le = t.logE();
+    const int imat = couple().mat;
+    const DevMat& md = T.mats[imat];
+    const int nElem = ld(&md.nElem);
+    // the photon energy is exact here (gammas carry no FP32 continuous loss):
+    // the FP64 target selection is the reference's own
+    Physics P{T, rng, t};
+    const int ei = nElem > 1 ? P.conv_target(imat, E, le, rng.flat()) : 0;
+    const int Z = ld(T.matElemZ + ld(&md.elemOff) + ei);
+    const DevElem& el = T.elems[Z < kMaxZ ? Z : kMaxZ];
+    // kinematic limits in FP64
+    const double eps0 = kMec2 / E;
+    double eps = 0.0;
+    if (E < 2.0) {
+      eps = eps0 + (0.5 - eps0) * rng.flat();
+    } else {
+      const double df = eps0 * 136. / ld(&el.Z13);
+      const double dmn = 4. * df;
+      const double dmx = E < 50.0 ? ld(&el.deltaMaxLow) : ld(&el.deltaMaxHigh);
+      const double lz13 = 0.333333 * ld(&el.logZ);
+      const double FZ = E < 50.0 ? 8. * lz13 : 8. * (lz13 + ld(&el.coulomb));
+      const double epsp = 0.5 - 0.5 * sqrt(1. - dmn / dmx);
+      const double epsMin = dmax_(eps0, epsp);
+      const double epsRange = 0.5 - epsMin;
+      const float dmnf = (float)dmn, FZf = (float)FZ, dff = (float)df;
+      float F10, F20;
+      if (dmnf > 1.4f) {
+        F10 = 42.038f - 8.29f * logf(dmnf + 0.958f);
+        F20 = F10;
+      } else {
+        F10 = 42.184f - dmnf * (7.444f - 1.623f * dmnf);
+        F20 = 41.326f - dmnf * (5.848f - 0.902f * dmnf);
+      }
+      F10 -= FZf;
+      F20 -= FZf;
+      const float epsRf = (float)epsRange;
+      const float N1 = fmx(F10 * epsRf * epsRf, 0.f);
+      const float N2 = fmx(1.5f * F20, 0.f);
+      const float cond = N1 / (N1 + N2);
+      const float iF10 = 1.f / F10, iF20 = 1.f / F20;
+      double r2;
+      float gr;
+      int it = 0;
+      const bool lpmRegime = E >= 100000.0;
+      const float lpmEf = (float)(kLPM * ld(&md.radLength));
+      const float z23 = (float)ld(&el.Z23), il1 = (float)ld(&el.ilVarS1), il1c = (float)ld(&el.ilVarS1Cond);
+      const float Ef = (float)E;
+      do {
+        const double r0 = rng.flat(), r1 = rng.flat();
+        r2 = rng.flat();
+        const bool first = lt((float)r0, cond);
+        if (first) eps = 0.5 - epsRange * (double)cbrtf((float)r1);
+        else eps = epsMin + epsRange * r1;
+        const float ef = (float)eps;
+        const float dd = dff / (ef * (1.f - ef));
+        if (!lpmRegime) {
+          gr = first ? (screen1(dd) - FZf) * iF10 : (screen2(dd) - FZf) * iF20;
+        } else {
+          float xiS, gS, phiS, p1, p2;
+          phi12(dd, p1, p2);
+          lpm_functions32(xiS, gS, phiS, Ef, ef * Ef, lpmEf, z23, il1, il1c, 0.0f, -1.0f);
+          gr = first ? xiS * ((2.f * phiS + gS) * p1 - gS * p2 - phiS * FZf) * iF10
+                     : xiS * ((phiS + 0.5f * gS) * p1 + 0.5f * gS * p2 - 0.5f * (gS + phiS) * FZf) * iF20;
+        }
+        near(gr, (float)r2);
+        if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
+      } while (gr < (float)r2);
+    }
+    double eT, pT;
+    if (rng.flat() > 0.5) {
+      eT = (1. - eps) * E;
+      pT = eps * E;
+    } else {
+      pT = (1. - eps) * E;
+      eT = eps * E;
+    }
+    const double eK = dmax_(0., eT - kMec2);
+    const double pK = dmax_(0., pT - kMec2);
+    Sec& se = t.addSec(0);
+    Sec& sp = t.addSec(1);
+    float sph, cph;
+    sincosf((float)k2Pi * (float)rng.flat(), &sph, &cph);
+    const double ce = tsai_cost(eK);
+    const double st = sqrt((1.0 - ce) * (1.0 + ce));
+    se.dir[0] = st * cph; se.dir[1] = st * sph; se.dir[2] = ce;
+    rotate(se.dir, t.dir);
+    const double cpo = tsai_cost(pK);
+    const double stp = sqrt((1.0 - cpo) * (1.0 + cpo));
+    sp.dir[0] = -stp * cph; sp.dir[1] = -stp * sph; sp.dir[2] = cpo;
+    rotate(sp.dir, t.dir);
+    se.e = eK;
+    sp.e = pK;
+    t.setE(0.0);
+  }
+
+  // ---- Klein-Nishina Compton (G4HepEmGammaInteractionCompton.icc:17-103) ------------
+  __device__ void compton() {
+    const double E = t.e;
+    const double thr = 0.0001;
+    if (E < thr) return;
+    const double org[3] = {t.dir[0], t.dir[1], t.dir[2]};
+    const float kappa = (float)(E * kInvMec2);
+    const float eps0 = 1.f / (1.f + 2.f * kappa);
+    const float eps02 = eps0 * eps0;
+    const float al1 = log1pf(2.f * kappa);
+    const float al2 = al1 + 0.5f * (1.f - eps02);
+    float eps, ome, omc, s2, gf;
+    double r2;
+    int it = 0;
+    do {
+      const double r0 = rng.flat(), r1 = rng.flat();
+      r2 = rng.flat();
+      if (lt(al2 * (float)r0, al1)) {
+        eps = expf(-al1 * (float)r1);
+        ome = -expm1f(-al1 * (float)r1);
+      } else {
+        const float eps2 = eps02 + (1.f - eps02) * (float)r1;
+        eps = sqrtf(eps2);
+        ome = (1.f - eps02) * (float)(1.0 - r1) / (1.f + eps);
+      }
+      omc = ome / (eps * kappa);
+      s2 = omc * (2.f - omc);
+      gf = 1.f - eps * s2 / (1.f + eps * eps);
+      near(gf, (float)r2);
+      if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
+    } while (gf < (float)r2);
+    const double cost = 1.0 - (double)omc;
+    const double sint = sqrt((double)fmx(0.f, s2));
+    float sp, cp;
+    sincosf((float)k2Pi * (float)rng.flat(), &sp, &cp);
+    t.dir[0] = sint * cp;
+    t.dir[1] = sint * sp;
+    t.dir[2] = cost;
+    rotate(t.dir, org);
+    // energies: the smaller share is computed directly, the other by difference
+    double post, se;
+    if (eps < 0.5f) {
+      post = E * (double)eps;
+      se = E - post;
+    } else {
+      se = E * (double)ome;
+      post = E - se;
+    }
+    neard(se, thr);
+    neard(post, thr);
+    double dep = 0.0;
+    if (se > thr) {
+      Sec& s = t.addSec(0);
+      s.dir[0] = E * org[0] - post * t.dir[0];
+      s.dir[1] = E * org[1] - post * t.dir[1];
+      s.dir[2] = E * org[2] - post * t.dir[2];
+      const double nrm = 1.0 / sqrt(s.dir[0] * s.dir[0] + s.dir[1] * s.dir[1] + s.dir[2] * s.dir[2]);
+      s.dir[0] *= nrm; s.dir[1] *= nrm; s.dir[2] *= nrm;
+      s.e = se;
+    } else {
+      dep += se;
+    }
+    if (post > thr) {
+      t.setE(post);
+    } else {
+      dep += post;
+      t.setE(0.0);
+    }
+    t.edep = dep;
+  }
+};
+
+}  // namespace hepem

@@ -51,7 +51,7 @@ size_t bytes_per_slot() {
   size_t b = 0;
   for (size_t x : kStateSizes) b += x;
   for (size_t x : kOutSizes) b += x;
-  return b + 8 + 4 + 8 + 8 + 4 + 4 + 48;
+  return b + 8 + 4 + 8 + 8 + 4 + 4 + 52;
 }
 
 struct Request {

@@ -182,6 +182,12 @@ struct Builder {
     size_t off = append(v.data(), v.size() * sizeof(T));
     relocs.push_back({reinterpret_cast<const void**>(&field), off});
   }
+  // FP32 copy (round to nearest) of an FP64 table
+  void put32(const float*& field, const std::vector<double>& v) {
+    std::vector<float> f(v.size());
+    for (size_t i = 0; i < v.size(); ++i) f[i] = (float)v[i];
+    put(field, f);
+  }
 };
 
 struct ElSrc {
@@ -464,6 +470,17 @@ StateImage build_state_image(const char* text, size_t len) {
       B.put(d.selStart[k], es[p].selStart[k]);
       B.put(d.sel[k], es[p].sel[k]);
     }
+    DevElData32& f = T.el32[p];
+    f.lossLogMin = (float)d.lossLogMin;
+    f.lossILD = (float)d.lossILD;
+    f.nucLogMin = (float)d.nucLogMin;
+    f.nucILD = (float)d.nucILD;
+    B.put32(f.lossGrid, es[p].lossGrid);
+    B.put32(f.loss, es[p].loss);
+    B.put32(f.xs, es[p].xs);
+    B.put32(f.nucGrid, es[p].nucGrid);
+    B.put32(f.nuc, es[p].nuc);
+    B.put32(f.tr1, es[p].tr1);
   }
   B.put(T.sb.elE, elE);
   B.put(T.sb.lelE, lelE);

@@ -10,27 +10,28 @@
 namespace hepem {
 
 struct StepCount {
-  uint32_t steps, uniforms, overflow, secondaries, inter[8];
+  uint32_t steps, uniforms, overflow, secondaries, inter[8], fallback;
 };
 
 // Block-level sum of the step counters: warp reduce, then one atomic per block.
 // Every thread of the block must call it.
 __device__ __forceinline__ void add_counters(const StepCount& c, hepem_step_counters* g) {
   if (!g) return;
-  __shared__ uint32_t s[12];
-  if (threadIdx.x < 12) s[threadIdx.x] = 0;
+  __shared__ uint32_t s[13];
+  if (threadIdx.x < 13) s[threadIdx.x] = 0;
   __syncthreads();
-  const uint32_t v[12] = {c.steps, c.uniforms, c.overflow, c.secondaries, c.inter[0], c.inter[1], c.inter[2],
-                          c.inter[3], c.inter[4], c.inter[5], c.inter[6], c.inter[7]};
+  const uint32_t v[13] = {c.steps, c.uniforms, c.overflow, c.secondaries, c.inter[0], c.inter[1], c.inter[2],
+                          c.inter[3], c.inter[4], c.inter[5], c.inter[6], c.inter[7], c.fallback};
 #pragma unroll
-  for (int k = 0; k < 12; ++k) {
+  for (int k = 0; k < 13; ++k) {
     const uint32_t w = __reduce_add_sync(0xFFFFFFFFu, v[k]);
     if ((threadIdx.x & 31) == 0 && w) atomicAdd(&s[k], w);
   }
   __syncthreads();
-  if (threadIdx.x < 12 && s[threadIdx.x]) {
-    unsigned long long* dst = threadIdx.x < 4 ? (unsigned long long*)&g->steps + threadIdx.x
-                                              : (unsigned long long*)&g->interactions[threadIdx.x - 4];
+  if (threadIdx.x < 13 && s[threadIdx.x]) {
+    unsigned long long* dst = threadIdx.x < 4    ? (unsigned long long*)&g->steps + threadIdx.x
+                              : threadIdx.x < 12 ? (unsigned long long*)&g->interactions[threadIdx.x - 4]
+                                                 : (unsigned long long*)&g->fp64_fallback;
     atomicAdd(dst, (unsigned long long)s[threadIdx.x]);
   }
 }

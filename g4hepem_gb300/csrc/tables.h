@@ -77,6 +77,18 @@ struct DevGamma {                   // G4HepEmGammaData (G4HepEmGammaData.hh:15-
   const double* conv;
 };
 
+// FP32 copies of the e+- spline tables for the precision form: same layouts
+// and index arithmetic as the FP64 arrays they are rounded from.
+struct DevElData32 {
+  float lossLogMin, lossILD, nucLogMin, nucILD;
+  const float* lossGrid;            // [nLoss]
+  const float* loss;                // [5*nLoss*nCouples]
+  const float* xs;                  // same layout as DevElData::xs
+  const float* nucGrid;             // [nNuc]
+  const float* nuc;                 // [2*nNuc*nMats]
+  const float* tr1;                 // [2*nLoss*nMats]
+};
+
 struct DevTables {
   // G4HepEmParameters (G4HepEmParameters.hh:48-93)
   double elTrackingCut, gammaTrackingCut, minLossE, bremModelLim;
@@ -93,6 +105,7 @@ struct DevTables {
   DevElData el[2];                  // [0] e-, [1] e+
   DevSB sb;
   DevGamma gm;
+  DevElData32 el32[2];              // FP32 copies (precision form)
 };
 
 }  // namespace hepem

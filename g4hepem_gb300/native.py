@@ -45,7 +45,7 @@ class StepOut(C.Structure):
 
 class StepCounters(C.Structure):
     _fields_ = [("steps", C.c_uint64), ("uniforms", C.c_uint64), ("rng_overflow", C.c_uint64),
-                ("secondaries", C.c_uint64), ("interactions", C.c_uint64 * 8)]
+                ("secondaries", C.c_uint64), ("interactions", C.c_uint64 * 8), ("fp64_fallback", C.c_uint64)]
 
 
 class LaunchConfig(C.Structure):
@@ -81,12 +81,12 @@ class ServerStats(C.Structure):
 
 
 EXPORTED = ["hepem_create", "hepem_create_from_file", "hepem_destroy", "hepem_info", "hepem_status_string",
-            "hepem_last_error", "hepem_electron_lookup", "hepem_step", "hepem_step_batched",
-            "hepem_step_batched_noalloc", "hepem_step_host",
+            "hepem_last_error", "hepem_electron_lookup", "hepem_electron_lookup_mixed", "hepem_step", "hepem_step_batched",
+            "hepem_step_batched_noalloc", "hepem_step_mixed", "hepem_step_host",
             "hepem_philox_uniform", "hepem_fill_uniforms", "hepem_profile_stages", "hepem_stage_times",
             "hepem_server_create", "hepem_server_capacity", "hepem_server_submit", "hepem_server_poll",
             "hepem_server_wait", "hepem_server_cancel", "hepem_server_get_stats", "hepem_server_reset_stats",
-            "hepem_server_destroy", "hepem_get_launch_config", "hepem_set_launch_config", "hepem_autotune"]
+            "hepem_server_destroy", "hepem_sample_model", "hepem_get_launch_config", "hepem_set_launch_config", "hepem_autotune"]
 STATUS_CANCELLED, STATUS_TIMEOUT, STATUS_OOM_ADMISSION = 8, 5, 6
 
 
@@ -114,11 +114,15 @@ def lib():
         L.hepem_status_string.restype = C.c_char_p
         L.hepem_last_error.restype = C.c_char_p
         L.hepem_electron_lookup.argtypes = [_vp, C.c_int64, C.c_int] + [_vp] * 7 + [_vp]
+        L.hepem_electron_lookup_mixed.argtypes = L.hepem_electron_lookup.argtypes
         L.hepem_step.argtypes = [_vp, C.c_int64, C.POINTER(TrackState), C.POINTER(TrackState), _vp, C.c_int32,
                                  C.c_uint64, C.POINTER(StepOut), _vp, _vp]
         L.hepem_step_host.argtypes = L.hepem_step.argtypes
         L.hepem_step_batched.argtypes = L.hepem_step.argtypes
         L.hepem_step_batched_noalloc.argtypes = L.hepem_step.argtypes
+        L.hepem_step_mixed.argtypes = L.hepem_step.argtypes
+        L.hepem_sample_model.argtypes = [_vp, C.c_int, C.c_int, C.c_int64, C.c_double, C.c_int32, C.c_uint64, _vp,
+                                         _vp, _vp]
         L.hepem_philox_uniform.argtypes = [C.c_uint64, C.c_int32, C.c_int32]
         L.hepem_philox_uniform.restype = C.c_double
         L.hepem_fill_uniforms.argtypes = [C.c_int64, _vp, C.c_int32, C.c_uint64, _vp, _vp]
@@ -208,29 +212,45 @@ class Context:
         return dict(n_couples=nc.value, n_materials=nm.value, n_regions=nr.value, arena_bytes=nb.value)
 
     # -- device-pointer entry points (torch CUDA tensors) ----------------------
-    def electron_lookup(self, ekin, imc, positron=False, out=None, stream=None):
+    def electron_lookup(self, ekin, imc, positron=False, out=None, stream=None, mixed=False):
+        """hepem_electron_lookup (FP64), or with mixed=True hepem_electron_lookup_mixed (FP32 tables)."""
         import torch
         n = ekin.numel()
         if out is None:
             out = {k: torch.empty(n, dtype=torch.float64, device=ekin.device)
                    for k in ("xs_ioni", "xs_brem", "dedx", "range", "invrange_half")}
-        check(lib().hepem_electron_lookup(self.h, n, int(positron), _ptr(ekin), _ptr(imc), _ptr(out["xs_ioni"]),
+        fn = lib().hepem_electron_lookup_mixed if mixed else lib().hepem_electron_lookup
+        check(fn(self.h, n, int(positron), _ptr(ekin), _ptr(imc), _ptr(out["xs_ioni"]),
                                           _ptr(out["xs_brem"]), _ptr(out["dedx"]), _ptr(out["range"]),
                                           _ptr(out["invrange_half"]), _stream_ptr(stream)))
         return out
 
     def step(self, state_in: dict, state_out: dict, uniforms, n_uniform: int, seed: int, res: dict,
              counters=None, stream=None, form="plain"):
-        """One step of every track; form: "plain" (hepem_step), "batched" (hepem_step_batched) or
-        "noalloc" (hepem_step_batched_noalloc)."""
+        """One step of every track; form: "plain" (hepem_step), "batched" (hepem_step_batched),
+        "mixed" (hepem_step_mixed, the precision form) or "noalloc" (hepem_step_batched_noalloc)."""
         n = state_in["ekin"].numel()
         sin, sout, sres = make_state_struct(state_in), make_state_struct(state_out), make_out_struct(res)
-        fn = {"plain": lib().hepem_step, "batched": lib().hepem_step_batched,
+        fn = {"plain": lib().hepem_step, "batched": lib().hepem_step_batched, "mixed": lib().hepem_step_mixed,
               "noalloc": lib().hepem_step_batched_noalloc}[form]
         check(fn(self.h, n, C.byref(sin), C.byref(sout), _ptr(uniforms), n_uniform, seed, C.byref(sres),
                  _ptr(counters) if counters is not None else None, _stream_ptr(stream)))
 
     # -- host-buffer entry point (numpy arrays) ----------------------------------
+    # -- per-model sampling -------------------------------------------------------
+    SAMPLE_MODELS = {"sb": 0, "rb": 1, "moller": 2, "bhabha": 3, "compton": 4, "conversion": 5}
+
+    def sample_model(self, model: str, n: int, ekin: float, imc: int, seed: int, mixed=False, out=None,
+                     stream=None):
+        """n draws of one interaction model (hepem_sample_model); returns (energies, fallback count)."""
+        import torch
+        if out is None:
+            out = torch.empty(n, dtype=torch.float64, device="cuda")
+        fb = torch.zeros(1, dtype=torch.int64, device="cuda")
+        check(lib().hepem_sample_model(self.h, self.SAMPLE_MODELS[model], int(mixed), n, ekin, imc, seed,
+                                       _ptr(out), _ptr(fb), _stream_ptr(stream)))
+        return out, fb
+
     # -- launch configuration of the batched form ----------------------------------
     def launch_config(self) -> dict:
         c = LaunchConfig()

@@ -109,6 +109,7 @@ typedef struct hepem_step_counters {
   uint64_t rng_overflow;   /* tracks that read past n_uniform                 */
   uint64_t secondaries;    /* secondaries produced                            */
   uint64_t interactions[8];/* e+- winner 0..3, gamma winner 0..3              */
+  uint64_t fp64_fallback;  /* precision form: tracks re-stepped in FP64       */
 } hepem_step_counters;
 
 /* ---- context ------------------------------------------------------------ */
@@ -138,6 +139,12 @@ int  hepem_electron_lookup(const hepem_ctx* ctx, int64_t n, int is_positron,
                            const double* ekin, const int32_t* imc,
                            double* xs_ioni, double* xs_brem, double* dedx,
                            double* range, double* invrange_half, void* stream);
+/* The same five quantities from the FP32 tables of the precision form in FP32
+ * arithmetic (outputs widened to double): what hepem_step_mixed looks up. */
+int  hepem_electron_lookup_mixed(const hepem_ctx* ctx, int64_t n, int is_positron,
+                                 const double* ekin, const int32_t* imc,
+                                 double* xs_ioni, double* xs_brem, double* dedx,
+                                 double* range, double* invrange_half, void* stream);
 
 /* ---- one physics step (device pointers) ---------------------------------- */
 /* e+-: G4HepEmElectronManager::HowFar then ::Perform
@@ -183,6 +190,22 @@ int  hepem_step_batched_noalloc(const hepem_ctx* ctx, int64_t n, const hepem_tra
                                 int32_t n_uniform, uint64_t seed, hepem_step_out* res,
                                 hepem_step_counters* counters, void* stream);
 
+/* Precision form of hepem_step_batched: the e+- HowFar and continuous step
+ * (step limits, MSC, energy loss and its fluctuations, the delta-interaction
+ * test) run from FP32 copies of the tables in FP32 arithmetic; FP64 is kept
+ * for the range->energy inversion of the mean loss, the energy and deposit
+ * bookkeeping and decisions on exact inputs.  Every discrete decision taken
+ * on FP32 values is guarded: a track whose FP32 operands of any decision are
+ * closer than 2^-12 relative is re-stepped by the FP64 code
+ * (counters->fp64_fallback), so discrete outcomes (interaction, rejection
+ * acceptances, sampled counts) equal the FP64 path's, and continuous outputs
+ * agree with it to ~1e-6 relative.  No reference counterpart (the reference
+ * has FP64 only). */
+int  hepem_step_mixed(const hepem_ctx* ctx, int64_t n, const hepem_track_state* in,
+                      hepem_track_state* out, const double* uniforms,
+                      int32_t n_uniform, uint64_t seed, hepem_step_out* res,
+                      hepem_step_counters* counters, void* stream);
+
 /* Same with HOST buffers: copies the batch in, steps it (batched form),
  * copies the results back and synchronises.  Pinned host memory is fastest.
  * Reference counterpart: the per-track G4HepEmElectronManager::HowFar/Perform
@@ -202,6 +225,24 @@ int  hepem_step_host(const hepem_ctx* ctx, int64_t n, const hepem_track_state* i
 int  hepem_profile_stages(hepem_ctx* ctx, int enable);
 int  hepem_stage_times(hepem_ctx* ctx, float* ms, const char** names, int32_t max,
                        int32_t* count);
+
+/* ---- per-model sampling ---------------------------------------------------- */
+/* n independent draws of one interaction model for a particle of kinetic
+ * energy ekin in couple imc (direction +z; draw i uses the pure Philox stream
+ * of (seed, id = i)).  out[i] = the sampled energy: model 0 Seltzer-Berger and
+ * 1 relativistic brem (e-): the photon energy; 2 Moller (e-) and 3 Bhabha (e+):
+ * the delta-ray energy; 4 Klein-Nishina Compton: the scattered photon energy;
+ * 5 Bethe-Heitler pair production: the electron kinetic energy (0 when the
+ * model produces nothing, e.g. below its threshold).  precision 0: the FP64
+ * models of hepem_step; 1: the FP32 models of hepem_step_mixed, where a draw
+ * that trips a guard is redone in FP64 (*n_fallback, a device counter, may
+ * be NULL).  Replaces the direct calls of the reference's unit tests, e.g.
+ * G4HepEmElectronInteractionBrem::SampleETransferSB
+ * (G4HepEm/G4HepEmRun/include/G4HepEmElectronInteractionBrem.hh) as called
+ * from testElectronInteractionBrem/src/Implementation.cc:268-272. */
+int  hepem_sample_model(const hepem_ctx* ctx, int model, int precision, int64_t n,
+                        double ekin, int32_t imc, uint64_t seed, double* out,
+                        uint64_t* n_fallback, void* stream);
 
 /* ---- launch configuration of the batched form and its autotuner ---------- */
 /* The batched form runs eleven stage kernels (index: 0 e+- stage A, 1 gamma

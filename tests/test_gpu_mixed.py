@@ -1,0 +1,124 @@
+"""Precision form (hepem_step_mixed) against the FP64 path.
+
+The FP64 batched path is bit-identical to the reference (test_gpu_parity);
+here the precision form must give the same discrete outcomes on every track
+(interaction, number and type of secondaries, flags, uniforms consumed, Gauss
+cache state, which tracks stop) and continuous outputs within 1e-5 relative:
+  energies, deposits, step lengths, MSC range data   |d| <= 1e-5 |x|
+  unit directions (track and secondaries)            |d| <= 1e-5
+  lateral displacement                               |d| <= 1e-5 max(|disp|, 1e-3 pstep)
+  number of interaction lengths left                 |d| <= 1e-5 max(|nia|, 1)
+  cached Gaussian value                              |d| <= 1e-5
+"""
+import numpy as np
+import pytest
+
+from conftest import T3, T16
+from g4hepem_gb300 import workload as W
+
+pytestmark = pytest.mark.gpu
+
+NU = 64
+SEED = 777
+TOL = 1e-5
+
+
+def run(native, ctx, st, form):
+    import torch
+    n = len(st["ekin"])
+    sin = native.state_to_torch(st)
+    sout = native.empty_state_torch(n)
+    res = native.alloc_out_torch(n)
+    u = native.fill_uniforms(sin["id"], NU, SEED)
+    cnt = torch.zeros(13, dtype=torch.int64, device="cuda")
+    ctx.step(sin, sout, u, NU, SEED, res, counters=cnt, form=form)
+    torch.cuda.synchronize()
+    return native.to_numpy(sout), native.to_numpy(res), cnt.cpu().numpy()
+
+
+def rel_err(a, b, floor=0.0):
+    den = np.maximum(np.abs(b), floor)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        r = np.where(den > 0, np.abs(a - b) / np.where(den > 0, den, 1.0), np.abs(a - b))
+    return r
+
+
+def compare(st, ref, mix):
+    """Asserts the contract above; returns {quantity: (max, rms)} of the errors."""
+    (s64, r64, c64), (s32, r32, c32) = ref, mix
+    charged = st["type"] != 2
+    # discrete outcomes
+    for f in ("winner", "n_sec", "flags"):
+        np.testing.assert_array_equal(r32[f], r64[f], err_msg=f)
+    for f in ("rng_cursor", "gauss_valid", "msc_first_step"):
+        np.testing.assert_array_equal(s32[f], s64[f], err_msg=f)
+    np.testing.assert_array_equal(s32["ekin"] == 0, s64["ekin"] == 0, err_msg="stopped tracks")
+    ns = r64["n_sec"].astype(int)
+    valid = np.stack([ns > 0, ns > 1], axis=1).reshape(-1)
+    np.testing.assert_array_equal(r32["sec_type"][valid], r64["sec_type"][valid], err_msg="sec_type")
+    np.testing.assert_array_equal(c32[:12], c64[:12], err_msg="counters")
+    errs = {}
+
+    def check(name, e, mask=None):
+        e = e if mask is None else e[mask]
+        if e.size == 0:
+            return
+        errs[name] = (float(e.max()), float(np.sqrt(np.mean(e * e))))
+        assert e.max() <= TOL, (name, float(e.max()))
+
+    check("ekin", rel_err(s32["ekin"], s64["ekin"]))
+    check("edep", rel_err(r32["edep"], r64["edep"]))
+    check("gstep", rel_err(r32["gstep"], r64["gstep"]))
+    check("pstep", rel_err(r32["pstep"], r64["pstep"]))
+    for k in ("msc_init_range", "msc_dyn_factor", "msc_tlimit_min"):
+        check(k, rel_err(s32[k], s64[k]), charged)
+    check("dir", np.max([np.abs(s32[k] - s64[k]) for k in ("dir_x", "dir_y", "dir_z")], axis=0))
+    dnorm = np.sqrt(sum(r64[k] ** 2 for k in ("disp_x", "disp_y", "disp_z")))
+    dd = np.sqrt(sum((r32[k] - r64[k]) ** 2 for k in ("disp_x", "disp_y", "disp_z")))
+    check("disp", dd / np.maximum(np.maximum(dnorm, 1e-3 * r64["pstep"]), 1e-300))
+    check("nia", np.max([rel_err(s32[k], s64[k], 1.0) for k in ("nia0", "nia1", "nia2", "nia3")], axis=0), charged)
+    check("gauss_value", np.abs(s32["gauss_value"] - s64["gauss_value"]), s64["gauss_valid"] == 1)
+    check("sec_ekin", rel_err(r32["sec_ekin"], r64["sec_ekin"]), valid)
+    check("sec_dir", np.max([np.abs(r32[k] - r64[k]) for k in ("sec_dir_x", "sec_dir_y", "sec_dir_z")], axis=0),
+          valid)
+    return errs
+
+
+@pytest.mark.parametrize("table,nc,n", [(T3, 3, 1 << 20), (T16, 16, 1 << 19)])
+def test_mixed_matches_fp64(native, gpu_ctx, table, nc, n):
+    ctx = gpu_ctx(table)
+    st = W.mixed_batch(n, n_couples=nc, seed=31)
+    ref = run(native, ctx, st, "batched")
+    mix = run(native, ctx, st, "mixed")
+    errs = compare(st, ref, mix)
+    charged = int((st["type"] != 2).sum())
+    frac = mix[2][12] / charged
+    print(f"\nfp64 fallback {mix[2][12]} of {charged} e+- tracks ({frac:.2e});",
+          {k: f"{v[0]:.2e}/{v[1]:.2e}" for k, v in errs.items()})
+    assert frac < 0.02
+
+
+def test_mixed_wide_energy_range(native, gpu_ctx):
+    # 1 keV .. 100 TeV: table edges, LPM / relativistic brem, e-nuclear
+    ctx = gpu_ctx(T3)
+    st = W.mixed_batch(1 << 18, n_couples=3, seed=9, emin=1e-3, emax=1e8)
+    compare(st, run(native, ctx, st, "batched"), run(native, ctx, st, "mixed"))
+
+
+def test_mixed_in_place_and_deterministic(native, gpu_ctx):
+    import torch
+    ctx = gpu_ctx(T16)
+    n = 1 << 17
+    st = W.mixed_batch(n, n_couples=16, seed=12)
+    a = run(native, ctx, st, "mixed")
+    sin = native.state_to_torch(st)
+    res = native.alloc_out_torch(n)
+    u = native.fill_uniforms(sin["id"], NU, SEED)
+    ctx.step(sin, sin, u, NU, SEED, res, form="mixed")
+    torch.cuda.synchronize()
+    b = native.to_numpy(sin)
+    for k in a[0]:
+        assert np.array_equal(a[0][k], b[k]), k
+    rb = native.to_numpy(res)
+    for k in ("edep", "winner", "gstep"):
+        assert np.array_equal(a[1][k], rb[k]), k

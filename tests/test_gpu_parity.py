@@ -29,7 +29,7 @@ def gpu_step(native, ctx, st_np, seed, nu, uniforms_np=None, in_place=False, for
         u = native.fill_uniforms(sin["id"], nu, seed)
     else:
         u = torch.from_numpy(np.ascontiguousarray(uniforms_np).reshape(-1)).cuda()
-    cnt = torch.zeros(12, dtype=torch.int64, device="cuda")
+    cnt = torch.zeros(13, dtype=torch.int64, device="cuda")
     ctx.step(sin, sout, u, nu, seed, res, counters=cnt, form=form)
     torch.cuda.synchronize()
     out = native.to_numpy(sout)

@@ -21,7 +21,7 @@ def _batched(native, ctx, sin, u, n):
     import torch
     sout = native.empty_state_torch(n)
     res = native.alloc_out_torch(n)
-    cnt = torch.zeros(12, dtype=torch.int64, device="cuda")
+    cnt = torch.zeros(13, dtype=torch.int64, device="cuda")
     ctx.step(sin, sout, u, NU, SEED, res, counters=cnt, form="batched")
     torch.cuda.synchronize()
     return native.to_numpy(sout), native.to_numpy(res), cnt.cpu().numpy()

@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol(native):
 
 def test_status_strings(native):
     L = native.lib()
-    for code in range(8):
+    for code in range(9):
         assert len(L.hepem_status_string(code)) > 0
 
 

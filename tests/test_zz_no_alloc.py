@@ -26,7 +26,7 @@ def _run(native, ctx, st_np, seed, nu, form):
     sout = native.empty_state_torch(n)
     res = native.alloc_out_torch(n)
     u = native.fill_uniforms(sin["id"], nu, seed)
-    cnt = torch.zeros(12, dtype=torch.int64, device="cuda")
+    cnt = torch.zeros(13, dtype=torch.int64, device="cuda")
     ctx.step(sin, sout, u, nu, seed, res, counters=cnt, form=form)
     torch.cuda.synchronize()
     out = native.to_numpy(sout)
