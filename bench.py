@@ -348,6 +348,124 @@ def c4_serving(torch, N, args):
             "event_size_max": int(sizes.max()), "peak": peak, "poisson": levels}
 
 
+def c5_precision(torch, N, args, n_tracks=1 << 24):
+    """BASELINE configuration 5: the precision form (hepem_step_mixed) on a
+    16,777,216-track batch with the configuration-2 mix, against the FP64
+    batched form on identical uniforms: steps/s of both, the FP64 fallback
+    fraction, discrete mismatches (must be 0) and per-quantity max / RMS
+    relative errors; the configuration-1 lookups from the FP32 tables against
+    the FP64 ones; and chi2 of 1e8 Seltzer-Berger brem draws at 999 MeV in G4_Pb
+    (just below the 1 GeV switch to the relativistic model) and 1e8
+    Klein-Nishina draws at 1 MeV in G4_lAr, FP32 models against FP64 models."""
+    from g4hepem_gb300 import workload as W
+    ctx = N.Context(TABLE)
+    n = n_tracks
+    st = W.mixed_batch(n, n_couples=3, seed=WORKLOAD_SEED + 1)
+    sin = N.state_to_torch(st)
+    del st
+    u = N.fill_uniforms(sin["id"], NU, SEED)
+    outs, ress, cnts, ms = {}, {}, {}, {}
+    for form in ("batched", "mixed"):
+        sout = N.empty_state_torch(n)
+        res = N.alloc_out_torch(n)
+        cnt = torch.zeros(13, dtype=torch.int64, device="cuda")
+        for _ in range(max(3, args.warmup)):
+            ctx.step(sin, sout, u, NU, SEED, res, form=form)
+        torch.cuda.synchronize()
+        reps = max(3, min(args.steps, 8))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            ctx.step(sin, sout, u, NU, SEED, res, form=form)
+        e1.record()
+        torch.cuda.synchronize()
+        ms[form] = e0.elapsed_time(e1) / reps
+        ctx.step(sin, sout, u, NU, SEED, res, counters=cnt, form=form)
+        torch.cuda.synchronize()
+        outs[form], ress[form], cnts[form] = sout, res, cnt
+    a_s, b_s, a_r, b_r = outs["batched"], outs["mixed"], ress["batched"], ress["mixed"]
+    charged = sin["type"] != 2
+    mism = {f: int((a_r[f] != b_r[f]).sum()) for f in ("winner", "n_sec", "flags")}
+    mism.update({f: int((a_s[f] != b_s[f]).sum()) for f in ("rng_cursor", "gauss_valid")})
+    mism["stopped"] = int(((a_s["ekin"] == 0) != (b_s["ekin"] == 0)).sum())
+
+    def rel(x, y, mask=None):
+        d = (x - y).abs() / y.abs().clamp_min(1e-300)
+        d = torch.where(y == 0, (x - y).abs(), d)
+        if mask is not None:
+            d = d[mask]
+        if d.numel() == 0:
+            return None
+        return {"max": float(d.max()), "rms": float(d.pow(2).mean().sqrt())}
+
+    ns = a_r["n_sec"].long()
+    valid = torch.stack([ns > 0, ns > 1], dim=1).reshape(-1)
+    errs = {"ekin": rel(b_s["ekin"], a_s["ekin"]), "edep": rel(b_r["edep"], a_r["edep"]),
+            "gstep": rel(b_r["gstep"], a_r["gstep"]), "pstep": rel(b_r["pstep"], a_r["pstep"]),
+            "secondary_ekin": rel(b_r["sec_ekin"], a_r["sec_ekin"], valid),
+            "msc_tlimit_min": rel(b_s["msc_tlimit_min"], a_s["msc_tlimit_min"], charged),
+            "dir_abs_max": float(max((b_s[k] - a_s[k]).abs().max() for k in ("dir_x", "dir_y", "dir_z")))}
+    del outs, ress, a_s, b_s, a_r, b_r
+    torch.cuda.empty_cache()
+    # configuration-1 lookups, FP32 tables against FP64
+    e_np, i_np = W.electron_lookup_batch(1 << 20, seed=11)
+    ekin = torch.from_numpy(e_np).cuda()
+    imc = torch.from_numpy(i_np).cuda()
+    l64 = ctx.electron_lookup(ekin, imc)
+    l32 = ctx.electron_lookup(ekin, imc, mixed=True)
+    torch.cuda.synchronize()
+    lookups = {k: rel(l32[k], l64[k]) for k in l64}
+    # chi2 of the sampled energies, 1e8 draws per model and precision
+    import math
+    chi = {}
+    for name, model, e_mev, imc_c, lo, hi, logb in (("sb_999MeV_G4_Pb", "sb", 999.0, 2, None, None, True),
+                                                   ("compton_1MeV_G4_lAr", "compton", 1.0, 1, 0.0, 1.0, False)):
+        draws, chunk, nb = 10 ** 8, 10 ** 7, 100
+        h = {False: torch.zeros(nb, dtype=torch.float64, device="cuda"),
+             True: torch.zeros(nb, dtype=torch.float64, device="cuda")}
+        fb_total, tms = 0, {}
+        for mixed in (False, True):
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            t_ms = 0.0
+            for c in range(draws // chunk):
+                t0.record()
+                x, fb = ctx.sample_model(model, chunk, e_mev, imc_c, SEED + 100 + c, mixed=mixed)
+                t1.record()
+                torch.cuda.synchronize()
+                t_ms += t0.elapsed_time(t1)
+                if mixed:
+                    fb_total += int(fb.item())
+                y = x / e_mev
+                if logb:
+                    y = torch.log(y.clamp_min(1e-300))
+                    edges = (math.log(1e-4), 0.0)
+                else:
+                    edges = (lo, hi)
+                h[mixed] += torch.histc(y, bins=nb, min=edges[0], max=edges[1]).double()
+            tms["fp32" if mixed else "fp64"] = draws / (t_ms / 1e3)
+        a, b = h[False], h[True]
+        m = (a + b) > 0
+        c2 = float(((a[m] - b[m]) ** 2 / (a[m] + b[m])).sum())
+        ndf = int(m.sum())
+        try:
+            from scipy.stats import chi2 as _c2
+            pval = float(_c2.sf(c2, ndf))
+        except Exception:
+            pval = None
+        chi[name] = {"draws": draws, "bins": nb, "chi2": c2, "ndf": ndf, "p_value": pval,
+                     "fp64_fallback_draws": fb_total, "draws_per_s": tms}
+    ctx.close()
+    c = cnts["mixed"].cpu().numpy()
+    return {"workload": f"{n} mixed tracks (configuration-2 mix), 64 Philox uniforms/track, identical streams",
+            "mixed": {"value": n / (ms["mixed"] / 1e3), "unit": UNIT, "ms_per_step": ms["mixed"],
+                      "entry_point": "hepem_step_mixed"},
+            "fp64_batched": {"value": n / (ms["batched"] / 1e3), "unit": UNIT, "ms_per_step": ms["batched"]},
+            "speedup_vs_fp64_batched": ms["batched"] / ms["mixed"],
+            "fp64_fallback_tracks": int(c[12]), "fp64_fallback_fraction_of_charged": int(c[12]) / int(charged.sum()),
+            "discrete_mismatches": mism, "rel_errors": errs, "lookup_rel_errors_c1": lookups, "chi2": chi}
+
+
 def cpu_port_rate(state, threads, n_sample, reps=1):
     from oracle import oracle as O
     O.build_port()
@@ -400,6 +518,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-c3", action="store_true")
     ap.add_argument("--no-c4", action="store_true")
+    ap.add_argument("--no-c5", action="store_true")
     args = ap.parse_args()
     ws, rank, lrank = dist_env()
     if args.impl == "reference":
@@ -508,6 +627,7 @@ def main():
     c1 = c1_lookups(torch, N, ctx, stream, args, hbm)
     c3 = None if args.no_c3 else c3_batching(torch, N, args)
     c4 = None if args.no_c4 else c4_serving(torch, N, args)
+    c5 = None if args.no_c5 else c5_precision(torch, N, args)
     # per-stage device times of one more batched step: CUDA events recorded on
     # the launching stream around every stage kernel (hepem_profile_stages)
     import ctypes as C
@@ -562,7 +682,7 @@ def main():
             "plain_fp64": {"value": ws * n / (ms_plain / 1e3), "unit": UNIT, "ms_per_step": ms_plain,
                            "entry_point": "hepem_step"},
             "vs_plain_fp64": ms_plain / ms_step, "roofline": roof, "roofline_fp64": fp64,
-            "stage_ms": stages, "c1_lookup": c1, "c3_batching": c3, "c4_serving": c4, "cpu_baseline": cpu, "clocks": clk,
+            "stage_ms": stages, "c1_lookup": c1, "c3_batching": c3, "c4_serving": c4, "c5_precision": c5, "cpu_baseline": cpu, "clocks": clk,
             "counters": {"uniforms_per_step": uniforms_consumed, "secondaries_per_step": secondaries,
                          "interactions": [int(x) for x in c[4:12]]}}
     print(json.dumps(line), flush=True)

@@ -118,6 +118,41 @@ int hepem_create_from_file(const char* path, hepem_ctx** out) {
   }
 }
 
+int hepem_image_from_json(const char* json, size_t len, void* out, size_t capacity, size_t* size) {
+  if (!json || !size) return fail(HEPEM_BAD_ARG, "null argument");
+  try {
+    const std::vector<uint8_t> img = hepem::serialize_image(hepem::build_state_image(json, len));
+    *size = img.size();
+    if (!out) return HEPEM_OK;
+    if (capacity < img.size()) return fail(HEPEM_BAD_ARG, "image buffer too small");
+    memcpy(out, img.data(), img.size());
+    return HEPEM_OK;
+  } catch (const std::exception& e) {
+    return fail(HEPEM_PARSE_ERROR, e.what());
+  }
+}
+
+int hepem_image_check(const void* image, size_t size, int64_t* arena_bytes) {
+  try {
+    hepem::StateImage img = hepem::deserialize_image(image, size);
+    if (arena_bytes) *arena_bytes = (int64_t)img.bytes.size();
+    return HEPEM_OK;
+  } catch (const std::exception& e) {
+    return fail(HEPEM_PARSE_ERROR, e.what());
+  }
+}
+
+int hepem_create_from_image(const void* image, size_t size, hepem_ctx** out) {
+  if (!image || !out) return fail(HEPEM_BAD_ARG, "null argument");
+  *out = nullptr;
+  try {
+    hepem::StateImage img = hepem::deserialize_image(image, size);
+    return create_from_image(img, out);
+  } catch (const std::exception& e) {
+    return fail(HEPEM_PARSE_ERROR, e.what());
+  }
+}
+
 int hepem_destroy(hepem_ctx* c) {
   if (!c) return HEPEM_OK;
   cudaError_t e = cudaSuccess;

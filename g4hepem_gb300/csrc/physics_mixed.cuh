@@ -188,7 +188,9 @@ struct MixedEl {
       if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
     } while (r > 1.);
     const float rf = (float)r;
-    const float fac = sqrtf(-2.f * log1pf(-(float)(1.0 - r)) / rf);
+    // ln r to FP32 accuracy on both ends of (0, 1]
+    const float lr = r < 0.5 ? logf(rf) : log1pf(-(float)(1.0 - r));
+    const float fac = sqrtf(-2.f * lr / rf);
     rng.gaussValue = (double)((float)v1 * fac);
     rng.gaussValid = true;
     return (float)v2 * fac * sd + mean;
@@ -200,7 +202,12 @@ struct MixedEl {
       const float position = (float)rng.flat();
       float pv = expf(-mean);
       float ps = pv;
-      while (le(ps, position)) {
+      // the cumulative carries the FP32 error of the mean (~1e-6 of mean times
+      // the largest Poisson probability) and of its sum: an absolute margin of
+      // 2e-5 covers both
+      for (;;) {
+        if (fabsf(ps - position) <= 2.0e-5f) set_trip();
+        if (!(ps <= position)) break;
         ++number;
         pv *= mean / number;
         ps += pv;
@@ -287,7 +294,9 @@ struct MixedEl {
         HEPEM_TR(1, 19, p3);
         HEPEM_TR(1, 20, nnb);
         if (nnb > kMaxIter) { nnb = kMaxIter; t.flags |= kFlagLoopCap; }
-        for (int k = 0; k < nnb; ++k) eloss += (double)(w3 / (1.f - w * (float)rng.flat()));
+        // 1 - w u as (1 - w) + w (1 - u): no cancellation in the Landau tail (u -> 1/w)
+        const float omw = w3 / tcut;
+        for (int k = 0; k < nnb; ++k) eloss += (double)(w3 / (omw + w * (float)(1.0 - rng.flat())));
       }
     }
     return eloss * (double)scaling;
@@ -295,13 +304,16 @@ struct MixedEl {
 
   // Urban MSC cos(theta) (G4HepEmElectronInteractionUMSC.icc:153-270); the
   // result is assembled in FP64 so that 1 - cos keeps its precision
-  __device__ double simple_scatter(float xm, float x2m) {
-    const float d0 = 3.f * x2m - 1.f;
-    const float d1 = 2.f * xm - d0;
+  // d0 = 3 <x^2> - 1 and d1 = 2 <x> - d0, given without cancellation (cos_theta)
+  __device__ double simple_scatter(float xm, float d0, float d1) {
     const float a = 1.f + 4.f * d0 / d1;
     const float prob = (2.f + a) * xm / a;
     const double r0 = rng.flat(), r1 = rng.flat();
-    return lt((float)r0, prob) ? -1. + 2. * (double)powf((float)r1, 1.f / (1.f + a)) : -1. + 2. * r1;
+    if (!lt((float)r0, prob)) return -1. + 2. * r1;
+    // -1 + 2 r1^(1/(1+a)), with 1 - cos or 1 + cos kept to FP32 precision
+    const float lg = (1.f / (1.f + a)) * -neg_log_u(r1);
+    const float pw = expf(lg);
+    return pw < 0.5f ? -1. + 2. * (double)pw : 1. + 2. * (double)expm1f(lg);
   }
 
   __device__ float theta0_of(float srl, float postE, float preE, const DevMat& md) {
@@ -343,22 +355,27 @@ struct MixedEl {
       exactCos = true;
       return 1.0;
     }
-    float xm, x2m;
+    // <x> = xm and <x^2> = x2m of the reference (with its 0.333333); the simple
+    // model needs d0 = 3 x2m - 1 and d1 = 2 xm - d0, formed here so that the
+    // small-tau cancellations of the direct differences do not occur
+    float xm, d0, d1;
     if (tau < 0.01f) {
       xm = 1.0f - tau * (1.0f - 0.5f * tau);
-      x2m = 1.0f - tau * (5.0f - 6.25f * tau) * 0.333333f;
+      d0 = 2.0f - tau * (5.0f - 6.25f * tau) * 0.999999f;
+      d1 = tau * (4.999995f - 2.0f) + tau * tau * (1.0f - 6.2499938f);
     } else {
       xm = expf(-tau);
-      x2m = (1.0f + 2.0f * expf(-2.5f * tau)) * 0.333333f;
+      d0 = 1.999998f * expf(-2.5f * tau) - 1.0e-6f;
+      d1 = 3.0e-6f + 2.0f * expm1f(-tau) - 1.999998f * expm1f(-2.5f * tau);
     }
-    if (lt(postE, 0.5f * preE)) return simple_scatter(xm, x2m);
+    if (lt(postE, 0.5f * preE)) return simple_scatter(xm, d0, d1);
     const float radLen = (float)ld(&md.radLength);
     const float tsmall = fmn(tlimMin, 1.0f);
     // pstep == tlimitMin by construction when the MSC limit chose it
     const bool notSmall = (pIsTlm && tlimMin <= 1.0f) ? false : lt(tsmall, pstep);
     const float theta0 = notSmall ? theta0_of(pstep / radLen, postE, preE, md)
                                   : theta0_of(tsmall / radLen, postE, preE, md) * sqrtf(pstep / tsmall);
-    if (lt((float)kPi * 0.166666f, theta0)) return simple_scatter(xm, x2m);
+    if (lt((float)kPi * 0.166666f, theta0)) return simple_scatter(xm, d0, d1);
     const float th2 = theta0 * theta0;
     if (lt(th2, 1.0E-16f)) {
       exactCos = true;
@@ -381,7 +398,7 @@ struct MixedEl {
       thex = q * q;
     }
     const float xmean1 = 1.f - (1.f - (1.f + xsi) * ea) * thex * eaa;
-    if (le(xmean1, 0.999f * xm)) return simple_scatter(xm, x2m);
+    if (le(xmean1, 0.999f * xm)) return simple_scatter(xm, d0, d1);
     const float x0 = 1.f - xsi * thex;
     const float bx = c * thex;
     const float b = bx + x0;
@@ -794,9 +811,9 @@ struct MixedB {
     const int ne = (int)ld(D + 1);
     const double* x = D + 4;
     const double xv = dmax_(ld(x), dmin_(ld(x + ne * (nd - 1)), E));
-    const double fi = dmax_(0.0, dmin_((le - ld(D + 2)) * ld(D + 3), nd - 2.0));
-    const int ie = (int)fi;
-    if (fi - ie < 1e-6 || fi - ie > 1.0 - 1e-6) set_trip();
+    // (the interpolated cumulatives are continuous across energy knots: only
+    // the comparisons with u are guarded)
+    const int ie = (int)dmax_(0.0, dmin_((le - ld(D + 2)) * ld(D + 3), nd - 2.0));
     int i0 = ie * ne, i1 = i0 + ne;
     const double x1 = ld(x + i0++), x2 = ld(x + i1++);
     const double b = dmax_(0., dmin_(1., (xv - x1) / (x2 - x1)));
@@ -989,10 +1006,12 @@ struct MixedB {
         const double cL = ld(Tb + i3), cH = ld(Tb + i3 + 3);
         const float pA = (float)ld(Tb + i3 + 1), pB = (float)ld(Tb + i3 + 2);
         const float lKL = (float)ld(sb.lkappa + i), lKH = (float)ld(sb.lkappa + i + 1);
-        const float m1 = (float)((cum - cL) / (cH - cL));
-        const float m2 = (1.0f + pA + pB) * m1;
+        // the rational inverse interpolation lk = lKL + m2/m3 (lKH - lKL) written as
+        // lKH - (lKH - lKL)(1 - m1)(1 - pB m1)/m3, exact in the top bin (lKH = 0)
+        const double om1d = (cH - cum) / (cH - cL);
+        const float m1 = (float)(1.0 - om1d), om1 = (float)om1d;
         const float m3 = 1.0f + m1 * (pA + pB * m1);
-        const float lk = lKL + m2 / m3 * (lKH - lKL);
+        const float lk = lKH - (lKH - lKL) * om1 * (1.0f - pB * m1) / m3;
         kappa = expf(lk * lkt);
         k = (double)kappa * E;
         omk = (double)(-expm1f(lk * lkt));
@@ -1300,27 +1319,33 @@ struct MixedB {
     const float eps02 = eps0 * eps0;
     const float al1 = log1pf(2.f * kappa);
     const float al2 = al1 + 0.5f * (1.f - eps02);
-    float eps, ome, omc, s2, gf;
+    // 1 - cos = (1 - eps)/(eps kappa) and 1 + cos = (eps - eps0)(1 + 2 kappa)/(eps kappa)
+    // are both formed from differences computed without cancellation
+    float eps, ome, omc, opc, s2, gf;
     double r2;
     int it = 0;
     do {
       const double r0 = rng.flat(), r1 = rng.flat();
       r2 = rng.flat();
+      float dlt;  // eps - eps0
       if (lt(al2 * (float)r0, al1)) {
         eps = expf(-al1 * (float)r1);
         ome = -expm1f(-al1 * (float)r1);
+        dlt = eps0 * expm1f(al1 * (float)(1.0 - r1));
       } else {
         const float eps2 = eps02 + (1.f - eps02) * (float)r1;
         eps = sqrtf(eps2);
         ome = (1.f - eps02) * (float)(1.0 - r1) / (1.f + eps);
+        dlt = (1.f - eps02) * (float)r1 / (eps + eps0);
       }
       omc = ome / (eps * kappa);
-      s2 = omc * (2.f - omc);
+      opc = dlt * (1.f + 2.f * kappa) / (eps * kappa);
+      s2 = omc * opc;
       gf = 1.f - eps * s2 / (1.f + eps * eps);
       near(gf, (float)r2);
       if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
     } while (gf < (float)r2);
-    const double cost = 1.0 - (double)omc;
+    const double cost = omc < 1.f ? 1.0 - (double)omc : (double)opc - 1.0;
     const double sint = sqrt((double)fmx(0.f, s2));
     float sp, cp;
     sincosf((float)k2Pi * (float)rng.flat(), &sp, &cp);

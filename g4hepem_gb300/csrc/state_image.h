@@ -19,6 +19,10 @@ struct StateImage {
 // Parse + validate a G4HepEmState JSON document; throws std::runtime_error.
 StateImage build_state_image(const char* text, size_t len);
 StateImage build_state_image_file(const char* path);
+// Binary image of a StateImage (serialize) and back (deserialize; throws
+// std::runtime_error on a damaged or foreign image).
+std::vector<uint8_t> serialize_image(const StateImage& img);
+StateImage deserialize_image(const void* data, size_t size);
 // Resolve the pointer fields against the arena base address `base`.
 void relocate(StateImage& img, DevTables& out, const void* base);
 

@@ -517,4 +517,90 @@ StateImage build_state_image_file(const char* path) {
   return build_state_image(s.data(), s.size());
 }
 
+// ---- binary image of the arena ---------------------------------------------------
+// Layout (host byte order, 64-bit):
+//   "HEPEMIMG" | u32 version | u32 sizeof(DevTables) | u64 arena bytes |
+//   u64 number of relocations | DevTables (pointer fields meaningless) |
+//   relocations (u64 field offset, u64 arena offset)... | arena bytes |
+//   u64 FNV-1a checksum of everything before it.
+// Loading it skips parsing and validation of the JSON document: the arena was
+// validated when the image was made, and the image carries a checksum.
+namespace {
+const char kImgMagic[8] = {'H', 'E', 'P', 'E', 'M', 'I', 'M', 'G'};
+constexpr uint32_t kImgVersion = 1;
+
+uint64_t fnv1a(const uint8_t* p, size_t n) {
+  uint64_t h = 1469598103934665603ull;
+  for (size_t i = 0; i < n; ++i) {
+    h ^= p[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+template <class T>
+void put_pod(std::vector<uint8_t>& out, const T& v) {
+  const uint8_t* b = reinterpret_cast<const uint8_t*>(&v);
+  out.insert(out.end(), b, b + sizeof(T));
+}
+
+template <class T>
+T get_pod(const uint8_t* p, size_t size, size_t& off) {
+  if (off + sizeof(T) > size) throw std::runtime_error("image: truncated");
+  T v;
+  memcpy(&v, p + off, sizeof(T));
+  off += sizeof(T);
+  return v;
+}
+}  // namespace
+
+std::vector<uint8_t> serialize_image(const StateImage& img) {
+  std::vector<uint8_t> out;
+  out.insert(out.end(), kImgMagic, kImgMagic + 8);
+  put_pod(out, kImgVersion);
+  put_pod(out, (uint32_t)sizeof(DevTables));
+  put_pod(out, (uint64_t)img.bytes.size());
+  put_pod(out, (uint64_t)img.relocs.size());
+  DevTables t = img.host;
+  for (auto& r : img.relocs) memset(reinterpret_cast<uint8_t*>(&t) + r.first, 0, sizeof(void*));
+  put_pod(out, t);
+  for (auto& r : img.relocs) {
+    put_pod(out, (uint64_t)r.first);
+    put_pod(out, (uint64_t)r.second);
+  }
+  out.insert(out.end(), img.bytes.begin(), img.bytes.end());
+  put_pod(out, fnv1a(out.data(), out.size()));
+  return out;
+}
+
+StateImage deserialize_image(const void* data, size_t size) {
+  const uint8_t* p = static_cast<const uint8_t*>(data);
+  if (!p || size < 8 + 8 || memcmp(p, kImgMagic, 8) != 0) throw std::runtime_error("image: bad magic");
+  if (size < 8 + 8 + 8 + 8 + sizeof(uint64_t)) throw std::runtime_error("image: truncated");
+  const uint64_t sum = fnv1a(p, size - sizeof(uint64_t));
+  uint64_t stored;
+  memcpy(&stored, p + size - sizeof(uint64_t), sizeof(uint64_t));
+  if (sum != stored) throw std::runtime_error("image: checksum mismatch");
+  size_t off = 8;
+  const uint32_t ver = get_pod<uint32_t>(p, size, off);
+  if (ver != kImgVersion) throw std::runtime_error("image: unsupported version " + std::to_string(ver));
+  const uint32_t tsz = get_pod<uint32_t>(p, size, off);
+  if (tsz != sizeof(DevTables)) throw std::runtime_error("image: made by an incompatible build (table record size)");
+  const uint64_t nb = get_pod<uint64_t>(p, size, off);
+  const uint64_t nr = get_pod<uint64_t>(p, size, off);
+  StateImage img;
+  img.host = get_pod<DevTables>(p, size, off);
+  if (nr > sizeof(DevTables) / sizeof(void*)) throw std::runtime_error("image: bad relocation count");
+  for (uint64_t k = 0; k < nr; ++k) {
+    const uint64_t fo = get_pod<uint64_t>(p, size, off);
+    const uint64_t ao = get_pod<uint64_t>(p, size, off);
+    if (fo % alignof(void*) != 0 || fo + sizeof(void*) > sizeof(DevTables) || ao > nb)
+      throw std::runtime_error("image: relocation out of range");
+    img.relocs.push_back({(size_t)fo, (size_t)ao});
+  }
+  if (off + nb + sizeof(uint64_t) != size) throw std::runtime_error("image: size mismatch");
+  img.bytes.assign(p + off, p + off + nb);
+  return img;
+}
+
 }  // namespace hepem

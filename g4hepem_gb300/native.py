@@ -80,7 +80,8 @@ class ServerStats(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
-EXPORTED = ["hepem_create", "hepem_create_from_file", "hepem_destroy", "hepem_info", "hepem_status_string",
+EXPORTED = ["hepem_create", "hepem_create_from_file", "hepem_image_from_json", "hepem_image_check",
+            "hepem_create_from_image", "hepem_destroy", "hepem_info", "hepem_status_string",
             "hepem_last_error", "hepem_electron_lookup", "hepem_electron_lookup_mixed", "hepem_step", "hepem_step_batched",
             "hepem_step_batched_noalloc", "hepem_step_mixed", "hepem_step_host",
             "hepem_philox_uniform", "hepem_fill_uniforms", "hepem_profile_stages", "hepem_stage_times",
@@ -108,6 +109,9 @@ def lib():
         L.hepem_create.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(_vp)]
         L.hepem_create_from_file.argtypes = [C.c_char_p, C.POINTER(_vp)]
         L.hepem_destroy.argtypes = [_vp]
+        L.hepem_image_from_json.argtypes = [C.c_char_p, C.c_size_t, _vp, C.c_size_t, C.POINTER(C.c_size_t)]
+        L.hepem_image_check.argtypes = [_vp, C.c_size_t, C.POINTER(C.c_int64)]
+        L.hepem_create_from_image.argtypes = [_vp, C.c_size_t, C.POINTER(_vp)]
         L.hepem_info.argtypes = [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                  C.POINTER(C.c_int64)]
         L.hepem_status_string.argtypes = [C.c_int]
@@ -185,10 +189,13 @@ def make_out_struct(arrs: dict) -> StepOut:
 class Context:
     """Tables of one G4HepEmState on the current CUDA device."""
 
-    def __init__(self, json_path: str | None = None, json_text: str | bytes | None = None):
+    def __init__(self, json_path: str | None = None, json_text: str | bytes | None = None,
+                 image: bytes | None = None):
         L = lib()
         h = _vp()
-        if json_text is not None:
+        if image is not None:
+            check(L.hepem_create_from_image(image, len(image), C.byref(h)))
+        elif json_text is not None:
             b = json_text.encode() if isinstance(json_text, str) else json_text
             check(L.hepem_create(b, len(b), C.byref(h)))
         else:
@@ -368,6 +375,24 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def image_from_json(json_text) -> bytes:
+    """Binary image of the table arena of a G4HepEmState JSON document (no GPU needed)."""
+    if isinstance(json_text, str):
+        json_text = json_text.encode()
+    size = C.c_size_t()
+    check(lib().hepem_image_from_json(json_text, len(json_text), None, 0, C.byref(size)))
+    buf = C.create_string_buffer(size.value)
+    check(lib().hepem_image_from_json(json_text, len(json_text), buf, size.value, C.byref(size)))
+    return buf.raw[:size.value]
+
+
+def image_check(image: bytes) -> int:
+    """Validates an image; returns its arena size in bytes."""
+    nb = C.c_int64()
+    check(lib().hepem_image_check(image, len(image), C.byref(nb)))
+    return nb.value
 
 
 def philox_uniform(seed: int, tid: int, k: int) -> float:

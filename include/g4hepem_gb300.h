@@ -120,6 +120,17 @@ typedef struct hepem_step_counters {
  * CopyG4HepEmDataToGPU (G4HepEm/G4HepEmData/src/G4HepEmData.cc:78-101). */
 int  hepem_create(const char* state_json, size_t len, hepem_ctx** out);
 int  hepem_create_from_file(const char* path, hepem_ctx** out);
+/* Binary image of the table arena: parsing the JSON document once and keeping
+ * the image makes later loads a checksum and one copy (JSON loading is slow
+ * for large states: G4HepEm/G4HepEmDataJsonIO/src/G4HepEmDataJsonIOImpl.hh).
+ * hepem_image_from_json needs no GPU: with out == NULL it only reports the
+ * size.  hepem_image_check validates an image (magic, version, build
+ * compatibility, checksum, bounds).  hepem_create_from_image builds the same
+ * context as hepem_create on the same document. */
+int  hepem_image_from_json(const char* state_json, size_t len, void* out,
+                           size_t capacity, size_t* size);
+int  hepem_image_check(const void* image, size_t size, int64_t* arena_bytes);
+int  hepem_create_from_image(const void* image, size_t size, hepem_ctx** out);
 /* Replaces FreeG4HepEmData / FreeG4HepEmDataOnGPU (G4HepEmData.hh:80-88). */
 int  hepem_destroy(hepem_ctx* ctx);
 /* Table sizes: number of couples, materials, regions; bytes of the arena. */

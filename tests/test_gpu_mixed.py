@@ -122,3 +122,19 @@ def test_mixed_in_place_and_deterministic(native, gpu_ctx):
     rb = native.to_numpy(res)
     for k in ("edep", "winner", "gstep"):
         assert np.array_equal(a[1][k], rb[k]), k
+
+
+@pytest.mark.parametrize("model,e,imc", [("sb", 999.0, 2), ("rb", 5000.0, 0), ("moller", 50.0, 1),
+                                         ("bhabha", 20.0, 2), ("compton", 1.0, 1), ("conversion", 30.0, 2),
+                                         ("conversion", 2.0e5, 2)])
+def test_sampled_model_fp32_equals_fp64_per_draw(native, gpu_ctx, model, e, imc):
+    # hepem_sample_model: identical streams, so every draw must agree
+    ctx = gpu_ctx(T3)
+    n = 1 << 20
+    a, _ = ctx.sample_model(model, n, e, imc, 99, mixed=False)
+    b, fb = ctx.sample_model(model, n, e, imc, 99, mixed=True)
+    a, b = a.cpu().numpy(), b.cpu().numpy()
+    np.testing.assert_array_equal(a == 0, b == 0)
+    assert np.max(rel_err(b, a)) <= TOL
+    assert int(fb.item()) < 0.02 * n
+    assert np.all(a >= 0) and np.all(a <= e)

@@ -301,3 +301,21 @@ def test_batched_in_place(native, gpu_ctx):
         assert np.array_equal(a[0][k], b[0][k], equal_nan=True), k
     for k in ("edep", "winner", "n_sec", "flags"):
         assert np.array_equal(a[1][k], b[1][k]), k
+
+
+def test_context_from_arena_image_is_identical(native, gpu_ctx):
+    # the binary arena image loads to the same tables: same step, bit for bit
+    ctx_json = gpu_ctx(T16)
+    img = native.image_from_json(open(T16, "rb").read())
+    ctx_img = native.Context(image=img)
+    try:
+        assert ctx_img.info() == ctx_json.info()
+        st = W.mixed_batch(1 << 16, n_couples=16, seed=77)
+        a = gpu_step(native, ctx_json, st, 5, 16, form="batched")
+        b = gpu_step(native, ctx_img, st, 5, 16, form="batched")
+        for x, y in zip(a[:2], b[:2]):
+            for k in x:
+                assert np.array_equal(x[k], y[k], equal_nan=True), k
+        assert np.array_equal(a[2], b[2])
+    finally:
+        ctx_img.close()

@@ -80,3 +80,35 @@ def test_valid_state_without_device_reports_no_device(native):
     with pytest.raises(native.HepEmError) as e:
         native.Context(T3)
     assert e.value.code == 7
+
+
+def test_arena_image_round_trip_and_damage(native):
+    from conftest import T3, T16
+    for path in (T3, T16):
+        text = open(path, "rb").read()
+        img = native.image_from_json(text)
+        assert img[:8] == b"HEPEMIMG"
+        assert img == native.image_from_json(text)           # deterministic
+        nb = native.image_check(img)
+        assert 0 < nb < len(img)
+    # damaged images are parse errors, never accepted
+    bad = bytearray(img)
+    bad[len(bad) // 2] ^= 0x40
+    for b in (bytes(bad), img[:-9], img[:100], b"HEPEMIMG" + b"\0" * 64):
+        with pytest.raises(native.HepEmError) as e:
+            native.image_check(b)
+        assert e.value.code == 2
+    with pytest.raises(native.HepEmError) as e:
+        native.image_from_json(b'{"fParameters": {}}')
+    assert e.value.code == 2
+
+
+def test_context_from_image_without_device_reports_no_device(native):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from conftest import T3
+    img = native.image_from_json(open(T3, "rb").read())
+    with pytest.raises(native.HepEmError) as e:
+        native.Context(image=img)
+    assert e.value.code == 7
