@@ -27,6 +27,7 @@ UNITS = [
     ("noalloc.cu", []),
     ("server.cu", ["-fmad=false"]),
     ("tune.cu", []),
+    ("stack.cu", []),
     ("state_json.cpp", []),
 ]
 

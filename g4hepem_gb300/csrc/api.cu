@@ -7,6 +7,7 @@
 #include <mutex>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "g4hepem_gb300.h"
 #include "ctx.h"
@@ -210,6 +211,29 @@ int hepem_sample_model(const hepem_ctx* c, int model, int precision, int64_t n, 
   if (!out) return fail(HEPEM_BAD_ARG, "null output");
   HEPEM_CUDA(hepem::launch_sample(c->tables, model, precision, n, ekin, imc, seed, out,
                                   reinterpret_cast<unsigned long long*>(n_fallback), (cudaStream_t)stream, c->sms));
+  return HEPEM_OK;
+}
+
+int hepem_woodcock_gamma(const hepem_ctx* c, int64_t n, const hepem_track_state* in, hepem_track_state* out,
+                         double* px, double* py, double* pz, const hepem_layered_box* box, const double* uniforms,
+                         int32_t nu, uint64_t seed, hepem_step_out* res, uint8_t* reached, void* stream) {
+  if (!c || n < 0 || nu < 0 || !box) return fail(HEPEM_BAD_ARG, "bad context, size or box");
+  if (n == 0) return HEPEM_OK;
+  if (!state_ok(in) || !state_ok(out) || !out_ok(res) || (nu > 0 && !uniforms) || !px || !py || !pz)
+    return fail(HEPEM_BAD_ARG, "null array in track batch");
+  if (box->n_layers < 1 || !box->z_bounds || !box->layer_imc || !(box->half_x > 0.0) || !(box->half_y > 0.0) ||
+      box->wdt_imc < 0 || box->wdt_imc >= c->tables.nCouples)
+    return fail(HEPEM_BAD_ARG, "bad layered box");
+  // the layer arrays are device arrays: check them on the host once (small)
+  std::vector<double> zb(box->n_layers + 1);
+  std::vector<int32_t> li(box->n_layers);
+  HEPEM_CUDA(cudaMemcpy(zb.data(), box->z_bounds, sizeof(double) * zb.size(), cudaMemcpyDeviceToHost));
+  HEPEM_CUDA(cudaMemcpy(li.data(), box->layer_imc, sizeof(int32_t) * li.size(), cudaMemcpyDeviceToHost));
+  for (int32_t k = 0; k < box->n_layers; ++k)
+    if (!(zb[k] < zb[k + 1]) || li[k] < 0 || li[k] >= c->tables.nCouples)
+      return fail(HEPEM_BAD_ARG, "layer bounds must increase and layer couples must exist");
+  HEPEM_CUDA(hepem::launch_woodcock(c->tables, n, *in, *out, px, py, pz, *box, uniforms, nu, seed, *res, reached,
+                                    (cudaStream_t)stream, c->sms));
   return HEPEM_OK;
 }
 

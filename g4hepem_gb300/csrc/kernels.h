@@ -62,6 +62,11 @@ cudaError_t launch_sample(const DevTables& T, int model, int mixed, int64_t n, d
 constexpr int kNumStageEvents = 13;
 const char* stage_name(int i);
 
+cudaError_t launch_woodcock(const DevTables& T, int64_t n, const hepem_track_state& in,
+                            const hepem_track_state& out, double* px, double* py, double* pz,
+                            const hepem_layered_box& box, const double* uniforms, int nu, uint64_t seed,
+                            const hepem_step_out& res, uint8_t* reached, cudaStream_t s, int sms);
+
 cudaError_t launch_fill_uniforms(int64_t n, const int32_t* id, int nu, uint64_t seed, double* u, cudaStream_t s,
                                  int sms);
 

@@ -198,6 +198,147 @@ __global__ void __launch_bounds__(256) lookup_mixed_kernel(const __grid_constant
   }
 }
 
+static int grid_for(int64_t n, int block, int sms);
+
+// ---- Woodcock gamma tracking in a layered box (G4HepEmWoodcockHelper.cc:146-299) --------
+struct BoxGeo {
+  double hx, hy;
+  int nl, wdt;
+  const double* zb;
+  const int32_t* limc;
+  double elim;
+};
+
+// distance from p (inside) to the box surface along v (the box solid's DistanceToOut)
+__device__ __forceinline__ double box_dist_out(const BoxGeo& b, const double* p, const double* v) {
+  double d = 1.0e300;
+  if (v[0] > 0.) d = dmin_(d, (b.hx - p[0]) / v[0]);
+  else if (v[0] < 0.) d = dmin_(d, (-b.hx - p[0]) / v[0]);
+  if (v[1] > 0.) d = dmin_(d, (b.hy - p[1]) / v[1]);
+  else if (v[1] < 0.) d = dmin_(d, (-b.hy - p[1]) / v[1]);
+  if (v[2] > 0.) d = dmin_(d, (ld(b.zb + b.nl) - p[2]) / v[2]);
+  else if (v[2] < 0.) d = dmin_(d, (ld(b.zb) - p[2]) / v[2]);
+  return dmax_(d, 0.0);
+}
+
+// layer that contains z (clamped to the box)
+__device__ __forceinline__ int box_layer(const BoxGeo& b, double z) {
+  if (!(z > ld(b.zb))) return 0;
+  if (!(z < ld(b.zb + b.nl))) return b.nl - 1;
+  int lo = 0, hi = b.nl;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (z < ld(b.zb + mid)) hi = mid; else lo = mid;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(256) woodcock_kernel(const __grid_constant__ DevTables T, int64_t n,
+                                                       const hepem_track_state in, const hepem_track_state out,
+                                                       double* __restrict__ px, double* __restrict__ py,
+                                                       double* __restrict__ pz, const BoxGeo b,
+                                                       const double* __restrict__ uniforms, int nu, uint64_t seed,
+                                                       const hepem_step_out res, uint8_t* __restrict__ reached) {
+  const double kDblMax = 1.7976931348623157e308;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int type = in.type[i];
+    Track t;
+    Rng rng;
+    load_track(in, i, t, rng, uniforms, nu, seed, 2);
+    t.isEl = false;
+    double p[3] = {px[i], py[i], pz[i]};
+    bool boundary = false;
+    const bool bad = type != 2 || track_input_bad(T, 2, t.imc, t.e);
+    if (bad) {
+      t.flags = kFlagBadInput;
+    } else if (t.e > b.elim) {
+      Physics P{T, rng, t};
+      double dist = dmax_(box_dist_out(b, p, t.dir) - 1.0E-3, 0.0);
+      t.imc = b.wdt;
+      const double wdtMX = P.gamma_total_xs();
+      const double wdtMFP = wdtMX > 0.0 ? 1.0 / wdtMX : kDblMax;
+      const double wdtPE = t.peXS;
+      const int wdtMat = T.couples[b.wdt].mat;
+      double mx = 0.0, step = 0.0;
+      int prev = -1, it = 0;
+      bool stop = false;
+      while (!stop) {
+        const double ps = wdtMFP < kDblMax ? -vdt_log(rng.flat()) * wdtMFP : kDblMax;
+        if (dist < ps) {
+          step += dist;
+          boundary = true;
+          stop = true;
+        } else {
+          step += ps;
+          dist -= ps;
+          const int imc = ld(b.limc + box_layer(b, p[2] + step * t.dir[2]));
+          if (T.couples[imc].mat != wdtMat) {
+            if (imc != prev) {
+              prev = imc;
+              t.imc = imc;
+              mx = P.gamma_total_xs();
+            }
+            stop = mx * wdtMFP > rng.flat();
+            if (stop) t.mfp[0] = mx > 0.0 ? 1.0 / mx : kDblMax;
+          } else {
+            stop = true;
+            t.imc = b.wdt;
+            t.mfp[0] = wdtMFP;
+            t.peXS = wdtPE;
+          }
+        }
+        if (++it >= kMaxIter) {
+          t.flags |= kFlagLoopCap;
+          boundary = true;
+          break;
+        }
+      }
+      for (int k = 0; k < 3; ++k) p[k] += step * t.dir[k];
+      t.gstep = step;
+      t.nia[0] = -1.0;
+      t.winner = -1;
+      if (!boundary) {
+        // interaction at the end point (G4HepEmTrackingManager.cc:1094-1110)
+        P.gamma_select();
+        t.edep = 0.0;
+        if (t.winner == 0) P.conversion();
+        if (t.winner == 1) P.compton();
+        if (t.winner == 2) P.photoelectric();
+        P.gamma_tracking_cut();
+      }
+      t.imc = ld(b.limc + box_layer(b, p[2]));
+    } else {
+      // an ordinary step in the current layer
+      Physics P{T, rng, t};
+      t.imc = ld(b.limc + box_layer(b, p[2]));
+      P.gamma_howfar();
+      P.gamma_select();
+      P.gamma_perform();
+      for (int k = 0; k < 3; ++k) p[k] += t.gstep * t.dir[k];
+      t.imc = ld(b.limc + box_layer(b, p[2]));
+    }
+    t.pstep = t.gstep;
+    px[i] = p[0];
+    py[i] = p[1];
+    pz[i] = p[2];
+    store_track(in, out, res, i, t, rng, 2, bad);
+    out.imc[i] = bad ? in.imc[i] : t.imc;
+    store_secondaries(res, i, t, 0);
+    if (reached) reached[i] = boundary ? 1 : 0;
+  }
+}
+
+cudaError_t launch_woodcock(const DevTables& T, int64_t n, const hepem_track_state& in,
+                            const hepem_track_state& out, double* px, double* py, double* pz,
+                            const hepem_layered_box& box, const double* uniforms, int nu, uint64_t seed,
+                            const hepem_step_out& res, uint8_t* reached, cudaStream_t s, int sms) {
+  if (n <= 0) return cudaSuccess;
+  BoxGeo b{box.half_x, box.half_y, box.n_layers, box.wdt_imc, box.z_bounds, box.layer_imc, box.energy_limit};
+  woodcock_kernel<<<grid_for(n, 256, sms), 256, 0, s>>>(T, n, in, out, px, py, pz, b, uniforms, nu, seed, res,
+                                                         reached);
+  return cudaGetLastError();
+}
+
 __global__ void fill_uniforms_kernel(int64_t n, const int32_t* __restrict__ id, int nu, uint64_t seed,
                                      double* __restrict__ u) {
   const int64_t total = n * nu;

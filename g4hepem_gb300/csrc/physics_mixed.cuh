@@ -413,7 +413,8 @@ struct MixedEl {
     const float qprb = xm / (prob * xmean1 + (1.f - prob) * xmean2);
     const double r0 = rng.flat(), r1 = rng.flat(), r2 = rng.flat();
     if (lt((float)r0, qprb)) {
-      if (lt((float)r1, prob)) return 1. + (double)(logf(ea + (float)r2 / eaa) * thex);
+      // log(ea + r2/eaa) = log(1 - (1 - r2)(1 - ea)): log1p keeps small angles
+      if (lt((float)r1, prob)) return 1. + (double)(log1pf(-(float)(1.0 - r2) * (1.f - ea)) * thex);
       const float var0 = (1.0f - dd) * (float)r2;
       if (lt(var0, 0.01f * dd)) {
         const float var = var0 / (dd * c1);
@@ -905,8 +906,9 @@ struct MixedB {
     t.dir[2] = pTot * t.dir[2] - dP * s.dir[2];
     const double nrm = 1.0 / sqrt(t.dir[0] * t.dir[0] + t.dir[1] * t.dir[1] + t.dir[2] * t.dir[2]);
     t.dir[0] *= nrm; t.dir[1] *= nrm; t.dir[2] *= nrm;
-    t.setE(!t.isEl && omx < 0.5f ? E * (double)omx : E - dE);
-    s.e = dE;
+    const double eAfter = !t.isEl && omx < 0.5f ? E * (double)omx : E - dE;
+    t.setE(eAfter);
+    s.e = E - eAfter;
   }
 
   // ---- bremsstrahlung (G4HepEmElectronInteractionBrem.icc:35-344) -------------------
@@ -937,8 +939,11 @@ struct MixedB {
     t.dir[2] = pTot * t.dir[2] - k * s.dir[2];
     const double nrm = 1.0 / sqrt(t.dir[0] * t.dir[0] + t.dir[1] * t.dir[1] + t.dir[2] * t.dir[2]);
     t.dir[0] *= nrm; t.dir[1] *= nrm; t.dir[2] *= nrm;
-    t.setE(omk >= 0.0 && omk < 0.5 ? E * omk : E - k);
-    s.e = k;
+    // the smaller of the two energies is formed directly, the other as the
+    // complement, so that E is shared exactly
+    const double eAfter = omk >= 0.0 && omk < 0.5 ? E * omk : E - k;
+    t.setE(eAfter);
+    s.e = E - eAfter;
   }
 
   __device__ double sample_sb(double E, double le) {

@@ -57,6 +57,11 @@ class LaunchConfig(C.Structure):
                 "sort_energy_bins": self.sort_energy_bins, "ms": [round(x, 4) for x in self.ms]}
 
 
+class LayeredBox(C.Structure):
+    _fields_ = [("half_x", C.c_double), ("half_y", C.c_double), ("n_layers", C.c_int32), ("wdt_imc", C.c_int32),
+                ("z_bounds", _vp), ("layer_imc", _vp), ("energy_limit", C.c_double)]
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("memory_budget_bytes", C.c_int64), ("max_steps", C.c_int32), ("max_requests", C.c_int32),
                 ("min_energy", C.c_double)]
@@ -87,7 +92,7 @@ EXPORTED = ["hepem_create", "hepem_create_from_file", "hepem_image_from_json", "
             "hepem_philox_uniform", "hepem_fill_uniforms", "hepem_profile_stages", "hepem_stage_times",
             "hepem_server_create", "hepem_server_capacity", "hepem_server_submit", "hepem_server_poll",
             "hepem_server_wait", "hepem_server_cancel", "hepem_server_get_stats", "hepem_server_reset_stats",
-            "hepem_server_destroy", "hepem_sample_model", "hepem_get_launch_config", "hepem_set_launch_config", "hepem_autotune"]
+            "hepem_server_destroy", "hepem_sample_model", "hepem_stack_secondaries", "hepem_woodcock_gamma", "hepem_get_launch_config", "hepem_set_launch_config", "hepem_autotune"]
 STATUS_CANCELLED, STATUS_TIMEOUT, STATUS_OOM_ADMISSION = 8, 5, 6
 
 
@@ -125,6 +130,11 @@ def lib():
         L.hepem_step_batched.argtypes = L.hepem_step.argtypes
         L.hepem_step_batched_noalloc.argtypes = L.hepem_step.argtypes
         L.hepem_step_mixed.argtypes = L.hepem_step.argtypes
+        L.hepem_woodcock_gamma.argtypes = [_vp, C.c_int64, C.POINTER(TrackState), C.POINTER(TrackState), _vp, _vp,
+                                           _vp, C.POINTER(LayeredBox), _vp, C.c_int32, C.c_uint64,
+                                           C.POINTER(StepOut), _vp, _vp]
+        L.hepem_stack_secondaries.argtypes = [_vp, C.c_int64, C.POINTER(TrackState), C.POINTER(StepOut), C.c_int,
+                                              C.c_int32, C.POINTER(TrackState), C.c_int64, _vp, _vp, _vp]
         L.hepem_sample_model.argtypes = [_vp, C.c_int, C.c_int, C.c_int64, C.c_double, C.c_int32, C.c_uint64, _vp,
                                          _vp, _vp]
         L.hepem_philox_uniform.argtypes = [C.c_uint64, C.c_int32, C.c_int32]
@@ -244,6 +254,35 @@ class Context:
                  _ptr(counters) if counters is not None else None, _stream_ptr(stream)))
 
     # -- host-buffer entry point (numpy arrays) ----------------------------------
+    # -- Woodcock gamma tracking ---------------------------------------------------
+    def woodcock_gamma(self, state_in: dict, state_out: dict, pos: tuple, box: dict, uniforms, n_uniform: int,
+                       seed: int, res: dict, reached=None, stream=None):
+        """hepem_woodcock_gamma; pos = (x, y, z) device arrays (updated in place);
+        box: half_x, half_y, z_bounds (device), layer_imc (device), wdt_imc, energy_limit."""
+        n = state_in["ekin"].numel()
+        b = LayeredBox(box["half_x"], box["half_y"], box["layer_imc"].numel(), box["wdt_imc"],
+                       _ptr(box["z_bounds"]), _ptr(box["layer_imc"]), box["energy_limit"])
+        sin, sout, sres = make_state_struct(state_in), make_state_struct(state_out), make_out_struct(res)
+        check(lib().hepem_woodcock_gamma(self.h, n, C.byref(sin), C.byref(sout), _ptr(pos[0]), _ptr(pos[1]),
+                                         _ptr(pos[2]), C.byref(b), _ptr(uniforms) if n_uniform else None,
+                                         n_uniform, seed, C.byref(sres),
+                                         _ptr(reached) if reached is not None else None, _stream_ptr(stream)))
+
+    # -- secondary stacking ------------------------------------------------------
+    def stack_secondaries(self, parents: dict, res: dict, apply_cuts: bool, id_base: int, capacity: int,
+                          out: dict | None = None, edep_cut=None, stream=None):
+        """hepem_stack_secondaries: returns (new track batch dict, number stacked)."""
+        import torch
+        n = parents["ekin"].numel()
+        if out is None:
+            out = empty_state_torch(max(capacity, 1))
+        n_out = torch.zeros(1, dtype=torch.int64, device="cuda")
+        sp, so, sr = make_state_struct(parents), make_state_struct(out), make_out_struct(res)
+        check(lib().hepem_stack_secondaries(self.h, n, C.byref(sp), C.byref(sr), int(apply_cuts), id_base,
+                                            C.byref(so), capacity, _ptr(n_out),
+                                            _ptr(edep_cut) if edep_cut is not None else None, _stream_ptr(stream)))
+        return out, n_out
+
     # -- per-model sampling -------------------------------------------------------
     SAMPLE_MODELS = {"sb": 0, "rb": 1, "moller": 2, "bhabha": 3, "compton": 4, "conversion": 5}
 

@@ -237,6 +237,54 @@ int  hepem_profile_stages(hepem_ctx* ctx, int enable);
 int  hepem_stage_times(hepem_ctx* ctx, float* ms, const char** names, int32_t max,
                        int32_t* count);
 
+/* ---- Woodcock gamma tracking in a layered box ----------------------------- */
+/* A box |x| <= half_x, |y| <= half_y, z_bounds[0] <= z <= z_bounds[n_layers],
+ * made of n_layers slabs along z with couples layer_imc[] (device arrays).
+ * wdt_imc is the couple of the heaviest material: its total macroscopic cross
+ * section is the Woodcock reference.  Gammas above energy_limit are
+ * Woodcock-tracked through the box as G4HepEmWoodcockHelper::KeepTracking
+ * does (G4HepEm/G4HepEm/src/G4HepEmWoodcockHelper.cc:146-299): steps of
+ * -ln(u) times the reference mean free path, at each point an interaction
+ * with probability sigma(point's material)/sigma(reference) (certain in the
+ * reference material), until an interaction or 1e-3 mm before the box
+ * boundary; the interaction is then selected and performed as in
+ * G4HepEmTrackingManager (G4HepEm/G4HepEm/src/G4HepEmTrackingManager.cc:
+ * 1000-1110).  Gammas at or below energy_limit make one ordinary HowFar +
+ * interaction step in their current layer.  Positions (device, in/out) move
+ * by the step; imc becomes the couple at the new position; nia0 is reset.
+ * reached_boundary[i] (device, may be NULL) = 1 when the box boundary ended
+ * the Woodcock step.  Non-gamma tracks are flagged (flags & 4). */
+typedef struct hepem_layered_box {
+  double half_x, half_y;        /* transverse half widths [mm]                  */
+  int32_t n_layers;
+  int32_t wdt_imc;               /* couple of the Woodcock reference material    */
+  const double* z_bounds;        /* [n_layers + 1], increasing [mm], device      */
+  const int32_t* layer_imc;      /* [n_layers], device                           */
+  double energy_limit;           /* Woodcock tracking above this energy [MeV]    */
+} hepem_layered_box;
+int  hepem_woodcock_gamma(const hepem_ctx* ctx, int64_t n, const hepem_track_state* in,
+                          hepem_track_state* out, double* pos_x, double* pos_y, double* pos_z,
+                          const hepem_layered_box* box, const double* uniforms, int32_t n_uniform,
+                          uint64_t seed, hepem_step_out* res, uint8_t* reached_boundary,
+                          void* stream);
+
+/* ---- secondary stacking with production cuts ------------------------------ */
+/* Turns the secondaries of a step (res, after hepem_step*) into fresh tracks
+ * for the next step, in parent order (parent i: slot 0, then slot 1): type,
+ * energy and direction of the secondary, the parent's couple and safety, id =
+ * id_base + position, and the ReSet() state of a new track.  With apply_cuts
+ * an e- below the couple's electron production cut, an e+ below the positron
+ * cut (when m_e c^2 is below the gamma cut) and a gamma below the gamma cut
+ * are not stacked; their energy (e+: E + 2 m_e c^2) goes to edep_cut[i]
+ * (device, n entries, may be NULL).  *n_out (device) receives the number of
+ * stacked secondaries; at most `capacity` of them are written.  Replaces
+ * G4HepEmTrackingManager::StackSecondaries
+ * (G4HepEm/G4HepEm/src/G4HepEmTrackingManager.cc:1254-1330). */
+int  hepem_stack_secondaries(const hepem_ctx* ctx, int64_t n, const hepem_track_state* parents,
+                             const hepem_step_out* res, int apply_cuts, int32_t id_base,
+                             hepem_track_state* out, int64_t capacity, int64_t* n_out,
+                             double* edep_cut, void* stream);
+
 /* ---- per-model sampling ---------------------------------------------------- */
 /* n independent draws of one interaction model for a particle of kinetic
  * energy ekin in couple imc (direction +z; draw i uses the pure Philox stream

@@ -1598,10 +1598,179 @@ int step_range(const State& S, int64_t b, int64_t e, const hepem_track_state* in
   return 0;
 }
 
+// ---- Woodcock gamma tracking in a layered box (G4HepEmWoodcockHelper.cc:146-299) ------
+// The reference helper navigates a Geant4 geometry; here the geometry is a box
+// of slabs along z and the helper's loop is restated over it, with the
+// track's own uniform stream (G4UniformRand in the reference).
+struct BoxGeo {
+  double hx, hy;
+  int nl, wdt;
+  const double* zb;
+  const int32_t* limc;
+  double elim;
+};
+
+double box_dist_out(const BoxGeo& b, const double* p, const double* v) {
+  double d = 1.0e300;
+  if (v[0] > 0.) d = dmin(d, (b.hx - p[0]) / v[0]);
+  else if (v[0] < 0.) d = dmin(d, (-b.hx - p[0]) / v[0]);
+  if (v[1] > 0.) d = dmin(d, (b.hy - p[1]) / v[1]);
+  else if (v[1] < 0.) d = dmin(d, (-b.hy - p[1]) / v[1]);
+  if (v[2] > 0.) d = dmin(d, (b.zb[b.nl] - p[2]) / v[2]);
+  else if (v[2] < 0.) d = dmin(d, (b.zb[0] - p[2]) / v[2]);
+  return dmax(d, 0.0);
+}
+
+int box_layer(const BoxGeo& b, double z) {
+  if (!(z > b.zb[0])) return 0;
+  if (!(z < b.zb[b.nl])) return b.nl - 1;
+  int lo = 0, hi = b.nl;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (z < b.zb[mid]) hi = mid; else lo = mid;
+  }
+  return lo;
+}
+
+void woodcock_one(const State& S, const BoxGeo& b, int64_t i, const hepem_track_state* in, hepem_track_state* out,
+                  double* px, double* py, double* pz, const double* uniforms, int32_t nu, uint64_t seed,
+                  hepem_step_out* res, uint8_t* reached) {
+  const double kDblMax = 1.7976931348623157e308;
+  Rng rng{uniforms + i * (int64_t)nu, nu, in->rng_cursor[i], seed, in->id[i], false, in->gauss_valid[i] != 0,
+          in->gauss_value[i]};
+  Step s(S, rng);
+  Track& t = s.t;
+  const int type = in->type[i];
+  t.setE(in->ekin[i]);
+  t.dir[0] = in->dir_x[i]; t.dir[1] = in->dir_y[i]; t.dir[2] = in->dir_z[i];
+  t.imc = in->imc[i];
+  t.id = in->id[i];
+  t.onBoundary = in->on_boundary[i] != 0;
+  t.nia[0] = in->nia0[i];
+  t.charge = 0.0;
+  double p[3] = {px[i], py[i], pz[i]};
+  bool boundary = false;
+  const bool bad = type != 2 || !(t.imc >= 0 && t.imc < (int)S.couples.size()) || !(t.e > 0.0) || !(t.e < 1.0e300);
+  uint8_t flags = 0;
+  if (bad) {
+    flags = 4;
+  } else if (t.e > b.elim) {
+    double dist = dmax(box_dist_out(b, p, t.dir) - 1.0E-3, 0.0);
+    t.imc = b.wdt;
+    const double wdtMX = s.gammaTotalXS();
+    const double wdtMFP = wdtMX > 0.0 ? 1.0 / wdtMX : kDblMax;
+    const double wdtPE = t.peXS;
+    const int wdtMat = S.couples[b.wdt].mat;
+    double mx = 0.0, step = 0.0;
+    int prev = -1, it = 0;
+    bool stop = false;
+    while (!stop) {
+      const double ps = wdtMFP < kDblMax ? -vlog(rng.flat()) * wdtMFP : kDblMax;
+      if (dist < ps) {
+        step += dist;
+        boundary = true;
+        stop = true;
+      } else {
+        step += ps;
+        dist -= ps;
+        const int imc = b.limc[box_layer(b, p[2] + step * t.dir[2])];
+        if (S.couples[imc].mat != wdtMat) {
+          if (imc != prev) {
+            prev = imc;
+            t.imc = imc;
+            mx = s.gammaTotalXS();
+          }
+          stop = mx * wdtMFP > rng.flat();
+          if (stop) t.mfp[0] = mx > 0.0 ? 1.0 / mx : kDblMax;
+        } else {
+          stop = true;
+          t.imc = b.wdt;
+          t.mfp[0] = wdtMFP;
+          t.peXS = wdtPE;
+        }
+      }
+      if (++it >= (1 << 16)) {
+        flags |= 2;
+        boundary = true;
+        break;
+      }
+    }
+    for (int k = 0; k < 3; ++k) p[k] += step * t.dir[k];
+    t.gstep = step;
+    t.nia[0] = -1.0;
+    t.winner = -1;
+    if (!boundary) {
+      s.gammaSelect();
+      t.edep = 0.0;
+      if (t.winner == 0) s.conversion();
+      if (t.winner == 1) s.compton();
+      if (t.winner == 2) s.photoelectric();
+      const double fe = t.e;
+      if (fe > 0.0 && fe <= S.pars.gammaTrackingCut) {
+        t.setE(0.0);
+        t.edep += fe;
+      }
+    }
+    t.imc = b.limc[box_layer(b, p[2])];
+  } else {
+    t.imc = b.limc[box_layer(b, p[2])];
+    s.gammaHowFar();
+    s.gammaSelect();
+    s.gammaPerform();
+    for (int k = 0; k < 3; ++k) p[k] += t.gstep * t.dir[k];
+    t.imc = b.limc[box_layer(b, p[2])];
+  }
+  px[i] = p[0]; py[i] = p[1]; pz[i] = p[2];
+  out->ekin[i] = t.e;
+  out->dir_x[i] = t.dir[0]; out->dir_y[i] = t.dir[1]; out->dir_z[i] = t.dir[2];
+  out->nia0[i] = t.nia[0];
+  if (out != in) {
+    out->nia1[i] = in->nia1[i]; out->nia2[i] = in->nia2[i]; out->nia3[i] = in->nia3[i];
+    out->msc_init_range[i] = in->msc_init_range[i];
+    out->msc_dyn_factor[i] = in->msc_dyn_factor[i];
+    out->msc_tlimit_min[i] = in->msc_tlimit_min[i];
+    out->msc_first_step[i] = in->msc_first_step[i];
+    out->type[i] = in->type[i];
+    out->id[i] = in->id[i];
+    out->safety[i] = in->safety[i];
+    out->on_boundary[i] = in->on_boundary[i];
+  }
+  out->imc[i] = bad ? in->imc[i] : t.imc;
+  out->gauss_valid[i] = rng.gaussValid ? 1 : 0;
+  out->gauss_value[i] = rng.gaussValue;
+  out->rng_cursor[i] = rng.cursor;
+  res->edep[i] = t.edep;
+  res->gstep[i] = t.gstep;
+  res->pstep[i] = t.gstep;
+  res->winner[i] = (int8_t)t.winner;
+  res->disp_x[i] = res->disp_y[i] = res->disp_z[i] = 0.0;
+  res->flags[i] = (uint8_t)(flags | (rng.overflow ? 1 : 0));
+  res->n_sec[i] = (int8_t)(s.nsec > 2 ? 2 : s.nsec);
+  for (int k = 0; k < s.nsec && k < 2; ++k) {
+    res->sec_type[2 * i + k] = (int8_t)s.sec[k].type;
+    res->sec_ekin[2 * i + k] = s.sec[k].e;
+    res->sec_dir_x[2 * i + k] = s.sec[k].dir[0];
+    res->sec_dir_y[2 * i + k] = s.sec[k].dir[1];
+    res->sec_dir_z[2 * i + k] = s.sec[k].dir[2];
+  }
+  if (reached) reached[i] = boundary ? 1 : 0;
+}
+
 }  // namespace
 }  // namespace port
 
 extern "C" {
+
+int port_woodcock_gamma(void* st, int64_t n, const hepem_track_state* in, hepem_track_state* out, double* px,
+                        double* py, double* pz, double hx, double hy, int nl, int wdt, const double* zb,
+                        const int32_t* limc, double elim, const double* u, int32_t nu, uint64_t seed,
+                        hepem_step_out* res, uint8_t* reached) {
+  const port::State& S = *static_cast<port::State*>(st);
+  port::BoxGeo b{hx, hy, nl, wdt, zb, limc, elim};
+  for (int64_t i = 0; i < n; ++i) port::woodcock_one(S, b, i, in, out, px, py, pz, u, nu, seed, res, reached);
+  return 0;
+}
+
 
 void* port_load_state(const char* path) {
   const char* err = nullptr;

@@ -234,6 +234,32 @@ class PortLib(_Lib):
         L.port_fill_uniforms.argtypes = [C.c_int64, _ip, C.c_int32, C.c_uint64, _dp]
         L.port_vdt_log.argtypes = [C.c_int64, _dp, _dp]
         L.port_vdt_exp.argtypes = [C.c_int64, _dp, _dp]
+        L.port_woodcock_gamma.argtypes = [C.c_void_p, C.c_int64, C.POINTER(TrackState), C.POINTER(TrackState),
+                                          _dp, _dp, _dp, C.c_double, C.c_double, C.c_int, C.c_int, _dp, _ip,
+                                          C.c_double, _dp, C.c_int32, C.c_uint64, C.POINTER(StepOut),
+                                          C.POINTER(C.c_uint8)]
+        L.port_woodcock_gamma.restype = C.c_int
+
+    def woodcock_gamma(self, state: dict, pos, box: dict, uniforms, n_uniform, seed):
+        """Woodcock gamma step in a layered box (restatement of the reference
+        helper's loop); pos = (x, y, z) arrays, updated copies are returned."""
+        n = len(state["ekin"])
+        out_state = copy_state(state)
+        res = alloc_out(n)
+        px, py, pz = (np.array(a, dtype=np.float64, copy=True) for a in pos)
+        reached = np.zeros(n, dtype=np.uint8)
+        zb = np.ascontiguousarray(box["z_bounds"], dtype=np.float64)
+        li = np.ascontiguousarray(box["layer_imc"], dtype=np.int32)
+        sin, sout, sres = make_state_struct(state), make_state_struct(out_state), make_out_struct(res)
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        rc = self.lib.port_woodcock_gamma(self.st, n, C.byref(sin), C.byref(sout), _ptr(px, _dp), _ptr(py, _dp),
+                                          _ptr(pz, _dp), box["half_x"], box["half_y"], len(li), box["wdt_imc"],
+                                          _ptr(zb, _dp), _ptr(li, _ip), box["energy_limit"], _ptr(u, _dp),
+                                          n_uniform, seed, C.byref(sres),
+                                          reached.ctypes.data_as(C.POINTER(C.c_uint8)))
+        if rc != 0:
+            raise RuntimeError(f"woodcock failed rc={rc}")
+        return out_state, res, (px, py, pz), reached
 
     def step_mt(self, state: dict, uniforms, n_uniform, seed, threads, in_place=False):
         n = len(state["ekin"])
