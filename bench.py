@@ -39,6 +39,8 @@ NU = 64
 SEED = 20261203
 WORKLOAD_SEED = 7
 LAUNCHES_PER_STEP = 14  # 3 sort kernels, 2 stage-A kernels, 9 interaction kernels (plus two memsets)
+# precision form: + the FP64 fallback kernels of e+- stage A and of 7 interaction models
+LAUNCHES_PER_STEP_MIXED = 22
 METRIC = "mixed e±/γ physics steps/s (1 GB300) vs plain FP64 path; p50/p99 batch latency"
 UNIT = "steps/s"
 CONFIG = {"workload": "plain FP64 full step, 4,194,304 mixed tracks (45% gamma, 45% e-, 10% e+), "
@@ -138,6 +140,29 @@ def fp64_peak_tflops(torch):
         e.synchronize()
         best = min(best, s.elapsed_time(e) / 1e3)
     return 2 * 4096 ** 3 / best / 1e12
+
+
+def fp32_peak_tflops(torch):
+    """Measured FP32 (SIMT) peak of this GPU: cuBLAS SGEMM 8192^3 with TF32 off, best of 5."""
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        a = torch.randn(8192, 8192, dtype=torch.float32, device="cuda")
+        b = torch.randn(8192, 8192, dtype=torch.float32, device="cuda")
+        for _ in range(2):
+            a @ b
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(5):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            a @ b
+            e.record()
+            e.synchronize()
+            best = min(best, s.elapsed_time(e) / 1e3)
+        return 2 * 8192 ** 3 / best / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = old
 
 
 def profile_summary(name):
@@ -519,6 +544,8 @@ def main():
     ap.add_argument("--no-c3", action="store_true")
     ap.add_argument("--no-c4", action="store_true")
     ap.add_argument("--no-c5", action="store_true")
+    ap.add_argument("--form", default="mixed", choices=["mixed", "batched"],
+                    help="form timed as the headline value (the other FP64 forms are reported beside it)")
     args = ap.parse_args()
     ws, rank, lrank = dist_env()
     if args.impl == "reference":
@@ -578,14 +605,21 @@ def main():
             t = float(tt.item())
         return t / steps
 
-    # the plain form (one thread per track), the denominator of the batched form
+    # the plain form (one thread per track) is the denominator of the target;
+    # the FP64 batched form and the precision form are timed beside it
     ms_plain = timed("plain", max(3, args.steps // 3))
+    other = "batched" if args.form == "mixed" else "mixed"
+    ms_other = timed(other, args.steps)
     clocks = Clocks(lrank)
     clocks.start()
     time.sleep(0.3)
-    ms_step = timed("batched", args.steps)
+    ms_step = timed(args.form, args.steps)
     clk = clocks.stop()
     value = ws * n / (ms_step / 1e3)
+    fcnt = torch.zeros(13, dtype=torch.int64, device="cuda")
+    ctx.step(sin, sout, u, NU, SEED, res, counters=fcnt, form="mixed")
+    torch.cuda.synchronize()
+    fallback = int(fcnt[12].item())
 
     # e2e through the host-buffer entry point
     e2e = None
@@ -601,9 +635,11 @@ def main():
         sin_h, sout_h, sres_h = N.make_state_struct(h_in), N.make_state_struct(h_out), N.make_out_struct(h_res)
         hcnt = N.StepCounters()
 
+        host_fn = N.lib().hepem_step_host_mixed if args.form == "mixed" else N.lib().hepem_step_host
+
         def host_step():
-            N.check(N.lib().hepem_step_host(ctx.h, n, C.byref(sin_h), C.byref(sout_h), h_u.data_ptr(), NU, SEED,
-                                            C.byref(sres_h), C.byref(hcnt), stream.cuda_stream))
+            N.check(host_fn(ctx.h, n, C.byref(sin_h), C.byref(sout_h), h_u.data_ptr(), NU, SEED, C.byref(sres_h),
+                            C.byref(hcnt), stream.cuda_stream))
         host_step()
         barrier()
         t0 = time.perf_counter()
@@ -619,7 +655,8 @@ def main():
         d2h += sum(v.numel() * v.element_size() for v in h_res.values())
         e2e = {"value": ws * n * ctx_steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "steps": ctx_steps, "ms_per_step": 1e3 * t_e2e / ctx_steps,
-               "entry_point": "hepem_step_host (pinned host buffers)"}
+               "entry_point": ("hepem_step_host_mixed" if args.form == "mixed" else "hepem_step_host")
+               + " (pinned host buffers)"}
 
     if rank != 0:
         return
@@ -628,45 +665,54 @@ def main():
     c3 = None if args.no_c3 else c3_batching(torch, N, args)
     c4 = None if args.no_c4 else c4_serving(torch, N, args)
     c5 = None if args.no_c5 else c5_precision(torch, N, args)
-    # per-stage device times of one more batched step: CUDA events recorded on
-    # the launching stream around every stage kernel (hepem_profile_stages)
+    # per-stage device times of one more step of each batched form: CUDA events
+    # recorded on the launching stream around every stage (hepem_profile_stages)
     import ctypes as C
-    N.check(N.lib().hepem_profile_stages(ctx.h, 1))
-    ctx.step(sin, sout, u, NU, SEED, res, form="batched")
-    ms_c, nm_c, cnt_c = (C.c_float * 16)(), (C.c_char_p * 16)(), C.c_int32()
-    N.check(N.lib().hepem_stage_times(ctx.h, ms_c, nm_c, 16, C.byref(cnt_c)))
-    N.check(N.lib().hepem_profile_stages(ctx.h, 0))
-    stages = {nm_c[i].decode(): float(ms_c[i]) for i in range(cnt_c.value)}
-    dom = max(stages, key=stages.get)
-    ms_dom = stages[dom]
-    # dominant kernel: e+- stage A.  Algorithmic bytes per e+- track: input state
-    # 128 B, output state 102 B, step results 51 B, queue entry 4 B, and 8 B per
-    # uniform the track consumed in the step (cursor sum, a slight overestimate
-    # for stage A alone).
+
+    def stage_times(form):
+        N.check(N.lib().hepem_profile_stages(ctx.h, 1))
+        ctx.step(sin, sout, u, NU, SEED, res, form=form)
+        ms_c, nm_c, cnt_c = (C.c_float * 16)(), (C.c_char_p * 16)(), C.c_int32()
+        N.check(N.lib().hepem_stage_times(ctx.h, ms_c, nm_c, 16, C.byref(cnt_c)))
+        N.check(N.lib().hepem_profile_stages(ctx.h, 0))
+        return {nm_c[i].decode(): float(ms_c[i]) for i in range(cnt_c.value)}
+
+    stages = {"mixed": stage_times("mixed"), "batched": stage_times("batched")}
+    head = stages[args.form]
+    dom = max(head, key=head.get)
+    ms_dom = head[dom]
+    # dominant kernel: e+- stage A (with its FP64 fallback in the precision
+    # form).  Algorithmic bytes per e+- track: input state 128 B, output state
+    # 102 B, step results 51 B, queue entry 4 B, and 8 B per uniform the track
+    # consumed in the step (cursor sum, a slight overestimate for stage A alone).
     charged = st_np["type"] != 2
     n_ch = int(charged.sum())
     cur = sout["rng_cursor"].cpu().numpy()
     alg = n_ch * (128 + 102 + 51 + 4) + 8 * int(cur[charged].sum())
     achieved = alg / (ms_dom / 1e3) / 1e9
-    prof = profile_summary("stage_a_charged.json")
+    prof = profile_summary("stage_a_charged_mixed.json" if args.form == "mixed" else "stage_a_charged.json")
     traffic = prof["dram_bytes_per_track"] * n_ch if prof else None
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "traffic": traffic,
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_src == "measured" else "fallback",
             "algorithmic_bytes_per_launch": alg, "ms_per_launch": ms_dom,
-            "note": "HBM is not the limit of this kernel; it is FP64-issue bound (roofline_fp64)"}
+            "note": "HBM is not the limit of this kernel: see roofline_fp64 / roofline_fp32 and profiles/"}
     fp64 = {"bound": "fp64", "kernel": dom, "unit": "TFLOP/s", "peak": None,
             "peak_source": "measured here: cuBLAS DGEMM 4096^3 (MEASURED_PEAKS.json has no FP64 figure)"}
+    fp32 = {"bound": "fp32", "kernel": dom, "unit": "TFLOP/s", "peak": None,
+            "peak_source": "measured here: cuBLAS SGEMM 8192^3, TF32 off (MEASURED_PEAKS.json has no FP32 figure)"}
     try:
         fp64["peak"] = fp64_peak_tflops(torch)
+        fp32["peak"] = fp32_peak_tflops(torch)
     except Exception as ex:  # pragma: no cover
         fp64["error"] = str(ex)
-    if prof and fp64["peak"]:
-        flops = prof["dflop_per_track"] * n_ch
-        fp64["achieved"] = flops / (ms_dom / 1e3) / 1e12
-        fp64["frac"] = fp64["achieved"] / fp64["peak"]
-        fp64["flops_per_launch"] = flops
-        fp64["dflop_per_track"] = prof["dflop_per_track"]
+    for rf, key in ((fp64, "dflop_per_track"), (fp32, "sflop_per_track")):
+        if prof and rf["peak"] and key in prof:
+            flops = prof[key] * n_ch
+            rf["achieved"] = flops / (ms_dom / 1e3) / 1e12
+            rf["frac"] = rf["achieved"] / rf["peak"]
+            rf["flops_per_launch"] = flops
+            rf[key] = prof[key]
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -676,13 +722,20 @@ def main():
                "sample": f"first {nsamp} tracks of the workload, 2 passes ({dt:.2f} s), {threads} host threads"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": CONFIG, "e2e": e2e,
-            "gpu_launches": LAUNCHES_PER_STEP * args.steps,
-            "form": "batched FP64 (hepem_step_batched): bit-identical to the plain FP64 path",
+            "vs_baseline": None, "dtype": "f32+f64" if args.form == "mixed" else "f64", "data": "synthetic", "config": CONFIG, "e2e": e2e,
+            "gpu_launches": (LAUNCHES_PER_STEP_MIXED if args.form == "mixed" else LAUNCHES_PER_STEP) * args.steps,
+            "form": ("precision form (hepem_step_mixed): discrete outcomes of the FP64 path, continuous within "
+                     "1e-5" if args.form == "mixed" else
+                     "batched FP64 (hepem_step_batched): bit-identical to the plain FP64 path"),
+            "fp64_fallback_per_step": fallback,
             "plain_fp64": {"value": ws * n / (ms_plain / 1e3), "unit": UNIT, "ms_per_step": ms_plain,
                            "entry_point": "hepem_step"},
-            "vs_plain_fp64": ms_plain / ms_step, "roofline": roof, "roofline_fp64": fp64,
-            "stage_ms": stages, "c1_lookup": c1, "c3_batching": c3, "c4_serving": c4, "c5_precision": c5, "cpu_baseline": cpu, "clocks": clk,
+            ("batched_fp64" if other == "batched" else "mixed"): {
+                "value": ws * n / (ms_other / 1e3), "unit": UNIT, "ms_per_step": ms_other,
+                "entry_point": "hepem_step_batched" if other == "batched" else "hepem_step_mixed"},
+            "vs_plain_fp64": ms_plain / ms_step, "roofline": roof, "roofline_fp64": fp64, "roofline_fp32": fp32,
+            "stage_ms": stages, "c1_lookup": c1, "c3_batching": c3, "c4_serving": c4, "c5_precision": c5,
+            "cpu_baseline": cpu, "clocks": clk,
             "counters": {"uniforms_per_step": uniforms_consumed, "secondaries_per_step": secondaries,
                          "interactions": [int(x) for x in c[4:12]]}}
     print(json.dumps(line), flush=True)

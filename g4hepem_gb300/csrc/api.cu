@@ -296,9 +296,10 @@ int hepem_step_mixed(const hepem_ctx* c, int64_t n, const hepem_track_state* in,
   return step_batched(c, n, in, out, uniforms, nu, seed, res, counters, stream, true);
 }
 
-int hepem_step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem_track_state* out,
-                    const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res,
-                    hepem_step_counters* counters, void* stream) {
+namespace {
+int step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem_track_state* out,
+              const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res, hepem_step_counters* counters,
+              void* stream, bool mixed) {
   hepem_ctx* c = const_cast<hepem_ctx*>(cc);
   if (!c || n < 0 || nu < 0) return fail(HEPEM_BAD_ARG, "bad context or size");
   if (n == 0) return HEPEM_OK;
@@ -317,6 +318,8 @@ int hepem_step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in,
   for (size_t b : kStateSizes) need += al(b * m);
   for (size_t b : kOutSizes) need += al(b * m);
   need += al(sizeof(double) * (size_t)m * nu) + al(sizeof(hepem_step_counters)) + al(hepem::batched_workspace_bytes(m));
+  // the precision form steps the chunk in place: room for its pre-step copy
+  if (mixed) need += al(hepem::mixed_pre_state_bytes(m));
   if (!c->slotsReady) {
     for (int k = 0; k < hepem_ctx::kSlots; ++k) {
       HEPEM_CUDA(cudaStreamCreateWithFlags(&c->slot[k].s, cudaStreamNonBlocking));
@@ -359,6 +362,8 @@ int hepem_step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in,
     hepem_step_counters* cnt = (hepem_step_counters*)p;
     p += al(sizeof(hepem_step_counters));
     void* dwork = p;
+    p += al(hepem::batched_workspace_bytes(m));
+    void* dpre = p;
     if (counters && ch < hepem_ctx::kSlots) {
       HEPEM_CUDA(cudaMemsetAsync(cnt, 0, sizeof(*cnt), ss));
       dcnt[ch] = cnt;
@@ -374,6 +379,12 @@ int hepem_step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in,
       HEPEM_CUDA(cudaMemcpyAsync(du, uniforms + off * nu, sizeof(double) * (size_t)mc * nu, cudaMemcpyHostToDevice, ss));
     hepem::BatchOpts o;
     o.cfg = &c->launch;
+    o.mixed = mixed;
+    hepem_track_state pre;
+    if (mixed) {
+      pre = hepem::carve_pre_state(dpre, m, ds);
+      o.preState = &pre;
+    }
     HEPEM_CUDA(hepem::launch_step_batched(c->tables, mc, ds, ds, du, nu, seed, dr, counters ? cnt : nullptr, dwork,
                                           ss, c->sms, o));
     // persistent per-track fields come back (type/imc/id/safety/boundary are inputs only)
@@ -406,6 +417,19 @@ int hepem_step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in,
     }
   }
   return HEPEM_OK;
+}
+}  // namespace
+
+int hepem_step_host(const hepem_ctx* c, int64_t n, const hepem_track_state* in, hepem_track_state* out,
+                    const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res,
+                    hepem_step_counters* counters, void* stream) {
+  return step_host(c, n, in, out, uniforms, nu, seed, res, counters, stream, false);
+}
+
+int hepem_step_host_mixed(const hepem_ctx* c, int64_t n, const hepem_track_state* in, hepem_track_state* out,
+                          const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res,
+                          hepem_step_counters* counters, void* stream) {
+  return step_host(c, n, in, out, uniforms, nu, seed, res, counters, stream, true);
 }
 
 int hepem_profile_stages(hepem_ctx* c, int enable) {

@@ -496,6 +496,8 @@ struct Physics {
     m.displace = m.displace && T.mscDisplacement;
     if (m.displace && pstep > m.zPath) {
       const double r = 0.73 * sqrt((pstep - m.zPath) * (pstep + m.zPath));
+      HEPEM_TR(0, 22, r);
+      HEPEM_TR(0, 23, pstep - m.zPath);
       const double cbeta = 2.16;
       const double cbeta1 = 1. - vdt_exp(-cbeta * kPi);
       const double r0 = rng.flat(), r1 = rng.flat();

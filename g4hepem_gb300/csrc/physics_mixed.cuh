@@ -265,7 +265,8 @@ struct MixedEl {
       } else {
         const int p = poisson(a1);
         HEPEM_TR(1, 17, p);
-        eloss = p > 0 ? (double)(((float)(p + 1) - 2.f * (float)rng.flat()) * e1) : 0.;
+        // ((p + 1) - 2u) e1 as ((p - 1) + 2 (1 - u)) e1: no cancellation for p = 1, u -> 1
+        eloss = p > 0 ? (double)(((float)(p - 1) + 2.f * (float)(1.0 - rng.flat())) * e1) : 0.;
       }
     }
     if (a3 > 0.f) {
@@ -691,6 +692,8 @@ struct MixedEl {
         bool dsp = displace && T.mscDisplacement;
         if (dsp && delta > 0.f) {
           const float r = 0.73f * sqrtf(delta * (p + zPath));
+          HEPEM_TR(1, 22, r);
+          HEPEM_TR(1, 23, delta);
           const float cbeta = 2.16f;
           const float cbeta1 = -expm1f(-cbeta * (float)kPi);
           const double r0 = rng.flat(), r1 = rng.flat();
@@ -909,6 +912,7 @@ struct MixedB {
     const double eAfter = !t.isEl && omx < 0.5f ? E * (double)omx : E - dE;
     t.setE(eAfter);
     s.e = E - eAfter;
+    if (eAfter * (eAfter + 2.0 * kMec2) < 4.0e-4 * pTot * pTot) set_trip();  // as in brem
   }
 
   // ---- bremsstrahlung (G4HepEmElectronInteractionBrem.icc:35-344) -------------------
@@ -944,6 +948,9 @@ struct MixedB {
     const double eAfter = omk >= 0.0 && omk < 0.5 ? E * omk : E - k;
     t.setE(eAfter);
     s.e = E - eAfter;
+    // the electron's new direction is a difference of momenta ~ pTot: its
+    // error is the incoming direction's (~1e-7, FP32 MSC) times pTot / p_after
+    if (eAfter * (eAfter + 2.0 * kMec2) < 4.0e-4 * pTot * pTot) set_trip();
   }
 
   __device__ double sample_sb(double E, double le) {
@@ -1193,7 +1200,9 @@ struct MixedB {
     const double px = ip * t.dir[0] - g1.dir[0] * e1;
     const double py = ip * t.dir[1] - g1.dir[1] * e1;
     const double pz = ip * t.dir[2] - g1.dir[2] * e1;
-    const double nrm = 1.0 / sqrt(px * px + py * py + pz * pz);
+    const double p2 = px * px + py * py + pz * pz;
+    if (p2 < 4.0e-4 * ip * ip) set_trip();  // second photon from a difference of momenta, as in brem
+    const double nrm = 1.0 / sqrt(p2);
     g2.dir[0] = px * nrm; g2.dir[1] = py * nrm; g2.dir[2] = pz * nrm;
     t.setE(0.0);
   }
@@ -1230,9 +1239,12 @@ struct MixedB {
     const DevElem& el = T.elems[Z < kMaxZ ? Z : kMaxZ];
     // kinematic limits in FP64
     const double eps0 = kMec2 / E;
-    double eps = 0.0;
+    // eps and dlt = eps - eps0: the kinetic energy of the lepton that takes
+    // eps is E dlt, which near the threshold the difference eps E - m c^2 loses
+    double eps = 0.0, dlt = 0.0;
     if (E < 2.0) {
-      eps = eps0 + (0.5 - eps0) * rng.flat();
+      dlt = (0.5 - eps0) * rng.flat();
+      eps = eps0 + dlt;
     } else {
       const double df = eps0 * 136. / ld(&el.Z13);
       const double dmn = 4. * df;
@@ -1269,8 +1281,15 @@ struct MixedB {
         const double r0 = rng.flat(), r1 = rng.flat();
         r2 = rng.flat();
         const bool first = lt((float)r0, cond);
-        if (first) eps = 0.5 - epsRange * (double)cbrtf((float)r1);
-        else eps = epsMin + epsRange * r1;
+        if (first) {
+          const double cr = (double)cbrtf((float)r1);
+          eps = 0.5 - epsRange * cr;
+          // 1 - cbrt(r1) = (1 - r1) / (1 + c + c^2)
+          dlt = (epsMin - eps0) + epsRange * ((1.0 - r1) / (1.0 + cr + cr * cr));
+        } else {
+          eps = epsMin + epsRange * r1;
+          dlt = (epsMin - eps0) + epsRange * r1;
+        }
         const float ef = (float)eps;
         const float dd = dff / (ef * (1.f - ef));
         if (!lpmRegime) {
@@ -1286,16 +1305,17 @@ struct MixedB {
         if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
       } while (gr < (float)r2);
     }
-    double eT, pT;
+    // kinetic energies: E dlt for the eps lepton, the rest of E - 2 m c^2 for the other
+    const double kEps = E * dlt;
+    const double kOther = dmax_(0., (E - 2.0 * kMec2) - kEps);
+    double eK, pK;
     if (rng.flat() > 0.5) {
-      eT = (1. - eps) * E;
-      pT = eps * E;
+      eK = kOther;
+      pK = kEps;
     } else {
-      pT = (1. - eps) * E;
-      eT = eps * E;
+      pK = kOther;
+      eK = kEps;
     }
-    const double eK = dmax_(0., eT - kMec2);
-    const double pK = dmax_(0., pT - kMec2);
     Sec& se = t.addSec(0);
     Sec& sp = t.addSec(1);
     float sph, cph;
@@ -1375,7 +1395,11 @@ struct MixedB {
       s.dir[0] = E * org[0] - post * t.dir[0];
       s.dir[1] = E * org[1] - post * t.dir[1];
       s.dir[2] = E * org[2] - post * t.dir[2];
-      const double nrm = 1.0 / sqrt(s.dir[0] * s.dir[0] + s.dir[1] * s.dir[1] + s.dir[2] * s.dir[2]);
+      const double q2 = s.dir[0] * s.dir[0] + s.dir[1] * s.dir[1] + s.dir[2] * s.dir[2];
+      // the electron direction is a difference of ~E-sized vectors built with
+      // the FP32 photon angle: its error grows as E / |q|
+      if (q2 < 4.0e-4 * E * E) set_trip();
+      const double nrm = 1.0 / sqrt(q2);
       s.dir[0] *= nrm; s.dir[1] *= nrm; s.dir[2] *= nrm;
       s.e = se;
     } else {

@@ -47,11 +47,13 @@ const size_t kOutSizes[14] = {8, 8, 8, 1, 8, 8, 8, 1, 1, 2, 16, 16, 16, 16};
 
 // bytes of pool memory per resident track: state, results, RNG key, owner,
 // accumulators, active index and the batched-step workspace share
-size_t bytes_per_slot() {
+size_t bytes_per_slot(bool mixed) {
   size_t b = 0;
   for (size_t x : kStateSizes) b += x;
   for (size_t x : kOutSizes) b += x;
-  return b + 8 + 4 + 8 + 8 + 4 + 4 + 52;
+  // + RNG key, owner-free accumulators, active index, workspace, and for the
+  // precision form the pre-step copy of the in-place step
+  return b + 8 + 4 + 8 + 8 + 4 + 4 + 52 + (mixed ? 102 : 0);
 }
 
 struct Request {
@@ -172,6 +174,7 @@ struct hepem_server {
   int32_t* stepSum = nullptr;
   int32_t* active = nullptr;
   void* work = nullptr;
+  void* pre = nullptr;                 // precision form: pre-step copy (mixed_pre_state_bytes)
   // per-iteration request tables (device + pinned host mirrors)
   int64_t maxReq = 0;
   size_t tableBytes = 0;
@@ -296,6 +299,12 @@ cudaError_t hepem_server::iterate() {
     o.active = active;
     o.seeds = seeds;
     o.cfg = &ctx->launch;
+    hepem_track_state preState;
+    if (cfg.precision) {
+      o.mixed = true;
+      preState = hepem::carve_pre_state(pre, capacity, st);
+      o.preState = &preState;
+    }
     SRV_CUDA(hepem::launch_step_batched(ctx->tables, nAct, st, st, nullptr, 0, 0, res, nullptr, work, stream,
                                         ctx->sms, o));
     account_kernel<<<g, 256, 0, stream>>>(active, dNActive, res, edepSum, eSecSum, nSecSum, stepSum);
@@ -401,7 +410,8 @@ int hepem_server_create(const hepem_ctx* ctx, const hepem_server_config* cfg, he
   s->ctx = ctx;
   s->cfg = *cfg;
   s->maxReq = cfg->max_requests;
-  const size_t per = bytes_per_slot();
+  if (cfg->precision != 0 && cfg->precision != 1) return hepem::set_error(HEPEM_BAD_ARG, "precision must be 0 or 1");
+  const size_t per = bytes_per_slot(cfg->precision == 1);
   const size_t fixed = hepem::batched_workspace_bytes(0) + 64 * 256;  // + rounding of ~45 arrays
   if ((size_t)cfg->memory_budget_bytes <= fixed + per) return hepem::set_error(HEPEM_BAD_ARG, "budget too small");
   s->capacity = (int64_t)(((size_t)cfg->memory_budget_bytes - fixed) / per);
@@ -412,6 +422,7 @@ int hepem_server_create(const hepem_ctx* ctx, const hepem_server_config* cfg, he
   for (size_t b : kStateSizes) bytes += al(b * C);
   for (size_t b : kOutSizes) bytes += al(b * C);
   bytes += al(8 * C) * 3 + al(4 * C) * 3 + al(hepem::batched_workspace_bytes(C));
+  if (cfg->precision) bytes += al(hepem::mixed_pre_state_bytes(C));
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&s->pool, bytes);
@@ -431,6 +442,8 @@ int hepem_server_create(const hepem_ctx* ctx, const hepem_server_config* cfg, he
   s->stepSum = (int32_t*)p; p += al(4 * C);
   s->active = (int32_t*)p; p += al(4 * C);
   s->work = p;
+  p += al(hepem::batched_workspace_bytes(C));
+  if (cfg->precision) s->pre = p;
   // request tables, same layout on the device and in pinned host memory:
   // slot0[R] cnt[R] off[R+1] outI[2R] outD[2R] nActive[1] alive[R]
   const int64_t R = s->maxReq;

@@ -64,7 +64,7 @@ class LayeredBox(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("memory_budget_bytes", C.c_int64), ("max_steps", C.c_int32), ("max_requests", C.c_int32),
-                ("min_energy", C.c_double)]
+                ("min_energy", C.c_double), ("precision", C.c_int32), ("reserved", C.c_int32)]
 
 
 class RequestResult(C.Structure):
@@ -88,7 +88,7 @@ class ServerStats(C.Structure):
 EXPORTED = ["hepem_create", "hepem_create_from_file", "hepem_image_from_json", "hepem_image_check",
             "hepem_create_from_image", "hepem_destroy", "hepem_info", "hepem_status_string",
             "hepem_last_error", "hepem_electron_lookup", "hepem_electron_lookup_mixed", "hepem_step", "hepem_step_batched",
-            "hepem_step_batched_noalloc", "hepem_step_mixed", "hepem_step_host",
+            "hepem_step_batched_noalloc", "hepem_step_mixed", "hepem_step_host", "hepem_step_host_mixed",
             "hepem_philox_uniform", "hepem_fill_uniforms", "hepem_profile_stages", "hepem_stage_times",
             "hepem_server_create", "hepem_server_capacity", "hepem_server_submit", "hepem_server_poll",
             "hepem_server_wait", "hepem_server_cancel", "hepem_server_get_stats", "hepem_server_reset_stats",
@@ -127,6 +127,7 @@ def lib():
         L.hepem_step.argtypes = [_vp, C.c_int64, C.POINTER(TrackState), C.POINTER(TrackState), _vp, C.c_int32,
                                  C.c_uint64, C.POINTER(StepOut), _vp, _vp]
         L.hepem_step_host.argtypes = L.hepem_step.argtypes
+        L.hepem_step_host_mixed.argtypes = L.hepem_step.argtypes
         L.hepem_step_batched.argtypes = L.hepem_step.argtypes
         L.hepem_step_batched_noalloc.argtypes = L.hepem_step.argtypes
         L.hepem_step_mixed.argtypes = L.hepem_step.argtypes
@@ -325,12 +326,14 @@ class Context:
         return c.as_dict()
 
     def step_host(self, state_in: dict, state_out: dict, uniforms: np.ndarray, n_uniform: int, seed: int,
-                  res: dict, stream=None):
+                  res: dict, stream=None, mixed=False):
+        """hepem_step_host (or hepem_step_host_mixed): host buffers in and out."""
         n = len(state_in["ekin"])
         cnt = StepCounters()
         sin, sout, sres = make_state_struct(state_in), make_state_struct(state_out), make_out_struct(res)
-        check(lib().hepem_step_host(self.h, n, C.byref(sin), C.byref(sout), _ptr(uniforms), n_uniform, seed,
-                                    C.byref(sres), C.byref(cnt), _stream_ptr(stream)))
+        fn = lib().hepem_step_host_mixed if mixed else lib().hepem_step_host
+        check(fn(self.h, n, C.byref(sin), C.byref(sout), _ptr(uniforms), n_uniform, seed, C.byref(sres),
+                 C.byref(cnt), _stream_ptr(stream)))
         return cnt
 
 
@@ -341,9 +344,10 @@ class Server:
     are RequestResult dicts, and optionally the final track state."""
 
     def __init__(self, ctx: Context, memory_budget_bytes: int, max_steps: int = 1000, max_requests: int = 4096,
-                 min_energy: float = 1.0e-3):
+                 min_energy: float = 1.0e-3, mixed: bool = False):
         self.ctx = ctx
-        cfg = ServerConfig(int(memory_budget_bytes), int(max_steps), int(max_requests), float(min_energy))
+        cfg = ServerConfig(int(memory_budget_bytes), int(max_steps), int(max_requests), float(min_energy),
+                           int(mixed), 0)
         h = _vp()
         check(lib().hepem_server_create(ctx.h, C.byref(cfg), C.byref(h)))
         self.h = h

@@ -227,6 +227,12 @@ int  hepem_step_host(const hepem_ctx* ctx, int64_t n, const hepem_track_state* i
                      int32_t n_uniform, uint64_t seed, hepem_step_out* res,
                      hepem_step_counters* counters, void* stream);
 
+/* The same through the precision form (hepem_step_mixed). */
+int  hepem_step_host_mixed(const hepem_ctx* ctx, int64_t n, const hepem_track_state* in,
+                           hepem_track_state* out, const double* uniforms,
+                           int32_t n_uniform, uint64_t seed, hepem_step_out* res,
+                           hepem_step_counters* counters, void* stream);
+
 /* ---- stage timing (profiling aid; not thread-safe) ------------------------ */
 /* enable != 0: the following hepem_step_batched calls on this context record
  * CUDA events around each of their stage kernels (no reference counterpart:
@@ -357,6 +363,8 @@ typedef struct hepem_server_config {
   int32_t max_steps;            /* step budget of a request (iterations)         */
   int32_t max_requests;         /* requests resident at once                     */
   double  min_energy;           /* a track is alive while ekin > min_energy (MeV) */
+  int32_t precision;            /* 0: FP64 batched form, 1: precision form       */
+  int32_t reserved;             /* 0                                             */
 } hepem_server_config;
 
 typedef struct hepem_request_result {

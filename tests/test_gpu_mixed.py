@@ -6,7 +6,8 @@ here the precision form must give the same discrete outcomes on every track
 cache state, which tracks stop) and continuous outputs within 1e-5 relative:
   energies, deposits, step lengths, MSC range data   |d| <= 1e-5 |x|
   unit directions (track and secondaries)            |d| <= 1e-5
-  lateral displacement                               |d| <= 1e-5 max(|disp|, 1e-3 pstep)
+  lateral displacement                               |d| <= 1e-5 max(|disp|, 1e-3 pstep), widened by
+                                                     the FP64 path's own rounding of p - z (see below)
   number of interaction lengths left                 |d| <= 1e-5 max(|nia|, 1)
   cached Gaussian value                              |d| <= 1e-5
 """
@@ -75,7 +76,13 @@ def compare(st, ref, mix):
     check("dir", np.max([np.abs(s32[k] - s64[k]) for k in ("dir_x", "dir_y", "dir_z")], axis=0))
     dnorm = np.sqrt(sum(r64[k] ** 2 for k in ("disp_x", "disp_y", "disp_z")))
     dd = np.sqrt(sum((r32[k] - r64[k]) ** 2 for k in ("disp_x", "disp_y", "disp_z")))
-    check("disp", dd / np.maximum(np.maximum(dnorm, 1e-3 * r64["pstep"]), 1e-300))
+    # The displacement length is 0.73 sqrt((p - z)(p + z)); the reference forms
+    # z = lambda (1 - exp(-p/lambda)) in FP64, whose rounding (~eps lambda)
+    # is a relative error of about eps p^2 / (p - z)^2 in p - z when p << lambda.
+    # That part of the difference is the FP64 path's, and is allowed for.
+    dz = np.maximum(r64["pstep"] - r64["gstep"], 1e-300)
+    ref_round = 2.2e-16 * r64["pstep"] ** 2 / dz ** 2
+    check("disp", dd / np.maximum(np.maximum(dnorm, 1e-3 * r64["pstep"]), 1e-300) / (1.0 + ref_round / TOL))
     check("nia", np.max([rel_err(s32[k], s64[k], 1.0) for k in ("nia0", "nia1", "nia2", "nia3")], axis=0), charged)
     check("gauss_value", np.abs(s32["gauss_value"] - s64["gauss_value"]), s64["gauss_valid"] == 1)
     check("sec_ekin", rel_err(r32["sec_ekin"], r64["sec_ekin"]), valid)

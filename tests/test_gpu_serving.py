@@ -175,3 +175,39 @@ def test_server_cancel_and_bounded_wait(native, gpu_ctx):
             srv.wait(12345678, timeout_s=0.1)       # unknown request id
     finally:
         srv.close()
+
+
+def test_server_precision_form(native, gpu_ctx):
+    # The serving loop over the precision form: results are independent of
+    # the mix.  Against the FP64 server: one iteration gives the same discrete
+    # history (step and secondary counts) and sums within 1e-5.  Over many
+    # iterations the two trajectories start from states that differ by the
+    # FP32 rounding of the previous steps, so only the totals are compared.
+    ctx = gpu_ctx(T3)
+    a = _request(4000, seed=14)
+    res = {}
+    for mixed in (False, True):
+        for steps in (1, 50):
+            srv = native.Server(ctx, memory_budget_bytes=128 << 20, max_steps=steps, min_energy=MIN_E,
+                                mixed=mixed)
+            try:
+                alone, fin_alone = srv.wait(srv.submit(a, seed=5), want_tracks=True)
+                ids = [srv.submit(_request(3000, seed=s), seed=s) for s in (31, 32)]
+                ra = srv.submit(a, seed=5)
+                ids.append(srv.submit(_request(9000, seed=33), seed=33))
+                mix, fin_mix = srv.wait(ra, want_tracks=True)
+                for i in ids:
+                    srv.wait(i)
+            finally:
+                srv.close()
+            _same_result(alone, mix)
+            _same_tracks(fin_alone, fin_mix)
+            res[(mixed, steps)] = alone
+    f64, f32 = res[(False, 1)], res[(True, 1)]
+    for k in ("steps", "n_secondaries", "track_steps", "status"):
+        assert f64[k] == f32[k], k
+    assert f32["edep"] == pytest.approx(f64["edep"], rel=1e-5)
+    assert f32["e_secondaries"] == pytest.approx(f64["e_secondaries"], rel=1e-5)
+    f64, f32 = res[(False, 50)], res[(True, 50)]
+    assert f32["edep"] == pytest.approx(f64["edep"], rel=2e-2)
+    assert f32["n_secondaries"] == pytest.approx(f64["n_secondaries"], rel=2e-2)

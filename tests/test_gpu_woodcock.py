@@ -82,8 +82,11 @@ def test_woodcock_matches_port(native, gpu_ctx, port):
     # both outcomes occur: interactions inside the box and boundary stops
     assert 0.05 < g_reached.mean() < 0.95
     assert np.all(g_res["gstep"] >= 0)
-    inside = np.abs(g_pos[0]) <= box["half_x"] + 1e-9
-    assert inside.all()
+    # Woodcock-tracked gammas stay in the box (ordinary steps below the
+    # energy limit are not limited by the geometry)
+    wdt = st["ekin"] > box["energy_limit"]
+    assert np.all(np.abs(g_pos[0][wdt]) <= box["half_x"]) and np.all(np.abs(g_pos[1][wdt]) <= box["half_y"])
+    assert np.all((g_pos[2][wdt] >= box["z_bounds"][0]) & (g_pos[2][wdt] <= box["z_bounds"][-1]))
 
 
 def test_woodcock_depth_distribution_in_one_material(native, gpu_ctx):
