@@ -54,6 +54,7 @@ struct Work {
   int32_t* perm;                  // [n] valid tracks in sort-key order
   int32_t* queue[kNumQueues + 1];  // interaction queues; [kNumQueues]: tracks the precision form re-steps in FP64
   double* peXS;                   // parallel to queue[kQPhotoelectric]
+  uint8_t* fbKind;                // parallel to queue[kNumQueues]: what the precision form redoes in FP64
   const uint64_t* seeds;          // per-track RNG keys (serving), or null: one key per call
   // precision form: the pre-step state of the tracks (the input batch, or for
   // in-place steps a copy that stage A takes of the e+- tracks it queues)
@@ -76,7 +77,7 @@ static size_t rnd(size_t b) { return (b + 255) / 256 * 256; }
 
 size_t batched_workspace_bytes(int64_t n) {
   return rnd(64 * sizeof(uint32_t)) + 2 * rnd(kMaxSortKeys * sizeof(uint32_t)) +
-         (2 + kNumQueues) * rnd(sizeof(int32_t) * (size_t)n) + rnd(sizeof(double) * (size_t)n);
+         (2 + kNumQueues) * rnd(sizeof(int32_t) * (size_t)n) + rnd(sizeof(double) * (size_t)n) + rnd((size_t)n);
 }
 
 size_t mixed_pre_state_bytes(int64_t n) {
@@ -128,6 +129,8 @@ static Work carve(void* ws, int64_t n) {
     p += rnd(sizeof(int32_t) * (size_t)n);
   }
   w.peXS = reinterpret_cast<double*>(p);
+  p += rnd(sizeof(double) * (size_t)n);
+  w.fbKind = p;
   return w;
 }
 
@@ -254,10 +257,29 @@ __device__ __forceinline__ void save_pre(const hepem_track_state& in, const hepe
 // MODE kStageFp64: the FP64 physics over the e+- tracks in sort order.
 // MODE kStageMixed: the precision form (physics_mixed.cuh) over the same
 //   tracks; a track whose FP32 pass tripped a guard is not stored but appended
-//   to the fallback list.
-// MODE kStageFallback: the FP64 physics over the fallback list (the tracks'
-//   input state is untouched: a tripped track was never stored).
-enum { kStageFp64 = 0, kStageMixed = 1, kStageFallback = 2 };
+//   to the fallback list, whose tracks one last kernel steps in FP64.
+enum { kStageFp64 = 0, kStageMixed = 1 };
+
+// fallback list of the precision form: queue[kNumQueues] with its kinds and
+// the count in counts[kFbCount].  Kind 0: the e+- stage A tripped (the track
+// was not stored); kind 1 + Q: interaction model Q tripped.
+constexpr int kFbCount = 3 + kNumQueues;
+
+// warp-aggregated append to the fallback list; all 32 lanes call it
+__device__ __forceinline__ void fb_push(bool trip, int32_t idx, uint8_t kind, const Work& w) {
+  const unsigned m = __ballot_sync(0xFFFFFFFFu, trip);
+  if (!m) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(&w.counts[kFbCount], (uint32_t)__popc(m));
+  base = __shfl_sync(0xFFFFFFFFu, base, leader);
+  if (trip) {
+    const uint32_t pos = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+    w.queue[kNumQueues][pos] = idx;
+    w.fbKind[pos] = kind;
+  }
+}
 
 template <int BS, int MODE>
 __global__ void __launch_bounds__(BS) stage_a_charged_kernel(const __grid_constant__ DevTables T,
@@ -266,20 +288,20 @@ __global__ void __launch_bounds__(BS) stage_a_charged_kernel(const __grid_consta
                                                               uint64_t seed, const hepem_step_out res, const Work w,
                                                               hepem_step_counters* counters) {
   const uint32_t nEm = w.counts[0], nEp = w.counts[1];
-  const int64_t total = MODE == kStageFallback ? (int64_t)w.counts[3 + kNumQueues] : (int64_t)nEm + nEp;
+  const int64_t total = (int64_t)nEm + nEp;
   StepCount cnt = {};
   for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < total; base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = base + threadIdx.x;
     int key = -1;
     int32_t idx = 0;
+    bool tripped = false;
     if (j < total) {
-      idx = MODE == kStageFallback ? w.queue[kNumQueues][j] : w.perm[j];
-      const int type = MODE == kStageFallback ? (int)in.type[idx] : (j < nEm ? 0 : 1);
+      idx = w.perm[j];
+      const int type = j < nEm ? 0 : 1;
       Track t;
       Rng rng;
       load_track(in, idx, t, rng, uniforms, nu, key_of(w, idx, seed), type);
       const int32_t c0 = rng.cursor;
-      bool tripped = false;
       if (MODE == kStageMixed) {
         MixedEl M{T, rng, t, false};
         key = M.stage_a();
@@ -291,19 +313,19 @@ __global__ void __launch_bounds__(BS) stage_a_charged_kernel(const __grid_consta
         key = P.el_perform_until_discrete();
       }
       if (tripped) {
-        key = kNumQueues;
+        key = -1;
       } else {
-        if (MODE != kStageFp64 && w.preCopy && key >= 0 && key != kQAnnihRest) save_pre(in, w.pre, idx);
+        if (MODE == kStageMixed && w.preCopy && key >= 0 && key != kQAnnihRest) save_pre(in, w.pre, idx);
         store_track(in, out, res, idx, t, rng, type, false);
         res.n_sec[idx] = 0;
         cnt.steps += 1;
         cnt.uniforms += (uint32_t)(rng.cursor - c0);
         cnt.overflow += rng.overflow;
         if (t.winner >= 0 && t.winner < 4) cnt.inter[t.winner] += 1;
-        if (MODE == kStageFallback) cnt.fallback += 1;
       }
     }
     warp_push(key, idx, w.queue, w.counts + 3);
+    if (MODE == kStageMixed) fb_push(tripped, idx, 0, w);
   }
   add_counters(cnt, counters);
 }
@@ -355,142 +377,188 @@ __global__ void __launch_bounds__(BS) stage_a_gamma_kernel(const __grid_constant
 }
 
 // ---- 3. stage B: one interaction model per kernel ------------------------------------------
-// Models with an FP32 version in the precision form (physics_mixed.cuh).
-__host__ __device__ constexpr bool has_mixed(int q) {
-  return q == kQIoniEm || q == kQIoniEp || q == kQBremSB || q == kQBremRB || q == kQAnnihFlight ||
-         q == kQConversion || q == kQCompton;
-}
 // e+- models: their input energy carries the FP32 continuous loss
 __host__ __device__ constexpr bool charged_model(int q) {
   return q == kQIoniEm || q == kQIoniEp || q == kQBremSB || q == kQBremRB || q == kQAnnihFlight;
 }
 
-// Precision form: an e+- track whose FP32 interaction tripped a guard is
-// stepped again from its pre-step state entirely in FP64 (stage A and the
-// interaction).  Its energy after the FP32 continuous step differs from the
-// FP64 one by ~1e-7, so the FP64 interaction alone would not give the FP64
-// path's outcome for the near-tie that tripped the guard.
-template <int Q>
-__device__ void charged_full_step(const DevTables& T, const hepem_track_state& in, const hepem_track_state& out,
-                                  const double* uniforms, int nu, uint64_t seed, const hepem_step_out& res,
-                                  const Work& w, int32_t i, StepCount& cnt) {
-  const int type = in.type[i];
+// one interaction of model Q for track i (j: its queue position, for the
+// photoelectric cross section; < 0 when not queued).  MIXED: the FP32 model,
+// which returns true (storing nothing) when a guard tripped.
+template <int Q, bool MIXED>
+__device__ bool stage_b_one(const DevTables& T, const hepem_track_state& in, const hepem_track_state& out,
+                            const double* uniforms, int nu, uint64_t seed, const hepem_step_out& res, const Work& w,
+                            int32_t i, int64_t j, StepCount& cnt) {
   Track t;
   Rng rng;
-  load_track(w.pre, i, t, rng, uniforms, nu, key_of(w, i, seed), type);
-  Physics P{T, rng, t};
-  P.el_howfar();
-  const int key = P.el_perform_until_discrete();
-  const int32_t cA = rng.cursor;
-  const uint32_t ovA = rng.overflow;
-  if (key == Q) {  // always: the stage-A guards held for this track
+  t.imc = in.imc[i];
+  t.setE(out.ekin[i]);
+  t.dir[0] = out.dir_x[i];
+  t.dir[1] = out.dir_y[i];
+  t.dir[2] = out.dir_z[i];
+  t.isEl = (Q == kQIoniEm) || ((Q == kQBremSB || Q == kQBremRB) && in.type[i] == 0);
+  t.flags = res.flags[i];
+  t.nsec = 0;
+  rng.u = uniforms + (int64_t)i * nu;
+  rng.n = nu;
+  rng.cursor = out.rng_cursor[i];
+  rng.id = in.id[i];
+  rng.overflow = 0u;
+  rng.seed = key_of(w, i, seed);
+  rng.gaussValid = out.gauss_valid[i] != 0;
+  rng.gaussValue = out.gauss_value[i];
+  const int32_t c0 = rng.cursor;
+  if (MIXED) {
+    MixedB M{T, rng, t, false};
+    if (Q == kQIoniEm || Q == kQIoniEp) M.ioni();
+    if (Q == kQBremSB) M.brem(true);
+    if (Q == kQBremRB) M.brem(false);
+    if (Q == kQAnnihFlight) M.annihilate_in_flight();
+    if (Q >= kQConversion) {
+      t.edep = 0.0;
+      if (Q == kQConversion) M.conversion();
+      if (Q == kQCompton) M.compton();
+    }
+    if (M.trip) {
+      HEPEM_COUNT_TRIP(M.tripLine);
+      return true;
+    }
+  } else {
+    Physics P{T, rng, t};
     if (Q == kQIoniEm || Q == kQIoniEp) P.ioni();
     if (Q == kQBremSB) P.brem(true);
     if (Q == kQBremRB) P.brem(false);
     if (Q == kQAnnihFlight) P.annihilate_in_flight();
+    if (Q == kQAnnihRest) P.annihilate_at_rest();
+    if (Q >= kQConversion) {
+      t.edep = 0.0;
+      t.peXS = (Q == kQPhotoelectric && j >= 0) ? w.peXS[j] : 0.0;
+      if (Q == kQConversion) P.conversion();
+      if (Q == kQCompton) P.compton();
+      if (Q == kQPhotoelectric) P.photoelectric();
+    }
   }
-  store_track(in, out, res, i, t, rng, type, false);
+  if (Q >= kQConversion) {
+    Physics P{T, rng, t};
+    P.gamma_tracking_cut();
+    res.edep[i] = t.edep;
+  }
+  out.ekin[i] = t.e;
+  if (Q != kQAnnihRest) {
+    out.dir_x[i] = t.dir[0];
+    out.dir_y[i] = t.dir[1];
+    out.dir_z[i] = t.dir[2];
+  }
+  out.gauss_valid[i] = rng.gaussValid ? 1 : 0;
+  out.gauss_value[i] = rng.gaussValue;
+  out.rng_cursor[i] = rng.cursor;
+  const bool firstOverflow = rng.overflow && !(t.flags & kFlagRngOverflow);
+  res.flags[i] = t.flags | (rng.overflow ? kFlagRngOverflow : 0);
   store_secondaries(res, i, t, 0);
-  cnt.uniforms += (uint32_t)(rng.cursor - cA);
-  cnt.overflow += (rng.overflow && !ovA) ? 1u : 0u;
+  cnt.uniforms += (uint32_t)(rng.cursor - c0);
+  cnt.overflow += firstOverflow ? 1u : 0u;
   cnt.secondaries += (uint32_t)(t.nsec > 2 ? 2 : t.nsec);
-  cnt.fallback += 1;
+  return false;
 }
-// counter of the FP64 fallback list of interaction queue q (precision form)
-constexpr int kFallbackCountB = 16;
 
-// MODE kStageFp64 / kStageMixed: the queue of model Q; kStageFallback: the
-// tracks of queue Q that the mixed kernel gave up on (the fallback list).
 template <int Q, int BS, int MODE>
 __global__ void __launch_bounds__(BS) stage_b_kernel(const __grid_constant__ DevTables T,
                                                       const hepem_track_state in, const hepem_track_state out,
                                                       const double* __restrict__ uniforms, int nu, uint64_t seed,
                                                       const hepem_step_out res, const Work w,
                                                       hepem_step_counters* counters) {
-  const int64_t total = MODE == kStageFallback ? w.counts[kFallbackCountB + Q] : w.counts[3 + Q];
-  const int32_t* q = MODE == kStageFallback ? w.queue[kNumQueues] : w.queue[Q];
+  const int64_t total = w.counts[3 + Q];
+  const int32_t* q = w.queue[Q];
   StepCount cnt = {};
   for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < total; base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = base + threadIdx.x;
     bool tripped = false;
     int32_t i = 0;
-    if (j < total && MODE == kStageFallback && charged_model(Q)) {
-      charged_full_step<Q>(T, in, out, uniforms, nu, seed, res, w, q[j], cnt);
-    } else if (j < total) {
+    if (j < total) {
       i = q[j];
-      Track t;
-      Rng rng;
-      t.imc = in.imc[i];
-      t.setE(out.ekin[i]);
-      t.dir[0] = out.dir_x[i];
-      t.dir[1] = out.dir_y[i];
-      t.dir[2] = out.dir_z[i];
-      t.isEl = (Q == kQIoniEm) || ((Q == kQBremSB || Q == kQBremRB) && in.type[i] == 0);
-      t.flags = res.flags[i];
-      t.nsec = 0;
-      rng.u = uniforms + (int64_t)i * nu;
-      rng.n = nu;
-      rng.cursor = out.rng_cursor[i];
-      rng.id = in.id[i];
-      rng.overflow = 0u;
-      rng.seed = key_of(w, i, seed);
-      rng.gaussValid = out.gauss_valid[i] != 0;
-      rng.gaussValue = out.gauss_value[i];
-      const int32_t c0 = rng.cursor;
-      if (MODE == kStageMixed) {
-        MixedB M{T, rng, t, false};
-        if (Q == kQIoniEm || Q == kQIoniEp) M.ioni();
-        if (Q == kQBremSB) M.brem(true);
-        if (Q == kQBremRB) M.brem(false);
-        if (Q == kQAnnihFlight) M.annihilate_in_flight();
-        if (Q >= kQConversion) {
-          t.edep = 0.0;
-          if (Q == kQConversion) M.conversion();
-          if (Q == kQCompton) M.compton();
-        }
-        tripped = M.trip;
-        if (tripped) HEPEM_COUNT_TRIP(M.tripLine);
-      } else {
-        Physics P{T, rng, t};
-        if (Q == kQIoniEm || Q == kQIoniEp) P.ioni();
-        if (Q == kQBremSB) P.brem(true);
-        if (Q == kQBremRB) P.brem(false);
-        if (Q == kQAnnihFlight) P.annihilate_in_flight();
-        if (Q == kQAnnihRest) P.annihilate_at_rest();
-        if (Q >= kQConversion) {
-          t.edep = 0.0;
-          t.peXS = (Q == kQPhotoelectric) ? w.peXS[j] : 0.0;
-          if (Q == kQConversion) P.conversion();
-          if (Q == kQCompton) P.compton();
-          if (Q == kQPhotoelectric) P.photoelectric();
-        }
-      }
-      if (!tripped) {
-        if (Q >= kQConversion) {
-          Physics P{T, rng, t};
-          P.gamma_tracking_cut();
-          res.edep[i] = t.edep;
-        }
-        out.ekin[i] = t.e;
-        if (Q != kQAnnihRest) {
-          out.dir_x[i] = t.dir[0];
-          out.dir_y[i] = t.dir[1];
-          out.dir_z[i] = t.dir[2];
-        }
-        out.gauss_valid[i] = rng.gaussValid ? 1 : 0;
-        out.gauss_value[i] = rng.gaussValue;
-        out.rng_cursor[i] = rng.cursor;
-        const bool firstOverflow = rng.overflow && !(t.flags & kFlagRngOverflow);
-        res.flags[i] = t.flags | (rng.overflow ? kFlagRngOverflow : 0);
-        store_secondaries(res, i, t, 0);
-        cnt.uniforms += (uint32_t)(rng.cursor - c0);
-        cnt.overflow += firstOverflow ? 1u : 0u;
-        cnt.secondaries += (uint32_t)(t.nsec > 2 ? 2 : t.nsec);
-        if (MODE == kStageFallback) cnt.fallback += 1;
-      }
+      tripped = stage_b_one<Q, MODE == kStageMixed>(T, in, out, uniforms, nu, seed, res, w, i, j, cnt);
     }
-    if (MODE == kStageMixed)
-      warp_push(tripped ? (int)kNumQueues : -1, i, w.queue, w.counts + kFallbackCountB + Q - kNumQueues);
+    if (MODE == kStageMixed) fb_push(tripped, i, (uint8_t)(1 + Q), w);
+  }
+  add_counters(cnt, counters);
+}
+
+// Precision form, last kernel of the step: the FP64 redo of every track on
+// the fallback list.  A tripped e+- stage A, or a tripped e+- interaction, is
+// stepped again entirely in FP64 from its pre-step state (the interaction's
+// input energy carries the FP32 continuous loss, so the FP64 interaction
+// alone would not give the FP64 path's outcome at the near-tie that tripped
+// the guard).  A tripped gamma interaction has exact inputs: only the FP64
+// interaction is redone.  One launch for all of them keeps the latency of
+// these few long FP64 threads to one kernel's tail.
+template <int Q>
+__device__ __forceinline__ void interaction_fp64(Physics& P) {
+  if (Q == kQIoniEm || Q == kQIoniEp) P.ioni();
+  if (Q == kQBremSB) P.brem(true);
+  if (Q == kQBremRB) P.brem(false);
+  if (Q == kQAnnihFlight) P.annihilate_in_flight();
+  if (Q == kQAnnihRest) P.annihilate_at_rest();
+}
+
+__device__ void charged_full_step(const DevTables& T, const hepem_track_state& in, const hepem_track_state& out,
+                                  const double* uniforms, int nu, uint64_t seed, const hepem_step_out& res,
+                                  const Work& w, int32_t i, bool fromStageA, StepCount& cnt) {
+  const hepem_track_state& src = fromStageA ? in : w.pre;
+  const int type = in.type[i];
+  Track t;
+  Rng rng;
+  load_track(src, i, t, rng, uniforms, nu, key_of(w, i, seed), type);
+  Physics P{T, rng, t};
+  const int32_t c0 = rng.cursor;
+  P.el_howfar();
+  const int key = P.el_perform_until_discrete();
+  const int32_t cA = rng.cursor;
+  const uint32_t ovA = rng.overflow;
+  switch (key) {
+    case kQIoniEm: interaction_fp64<kQIoniEm>(P); break;
+    case kQIoniEp: interaction_fp64<kQIoniEp>(P); break;
+    case kQBremSB: interaction_fp64<kQBremSB>(P); break;
+    case kQBremRB: interaction_fp64<kQBremRB>(P); break;
+    case kQAnnihFlight: interaction_fp64<kQAnnihFlight>(P); break;
+    case kQAnnihRest: interaction_fp64<kQAnnihRest>(P); break;
+    default: break;
+  }
+  store_track(in, out, res, i, t, rng, type, false);
+  store_secondaries(res, i, t, 0);
+  if (fromStageA) {
+    // stage A counted nothing for this track
+    cnt.steps += 1;
+    cnt.uniforms += (uint32_t)(rng.cursor - c0);
+    cnt.overflow += rng.overflow;
+    if (t.winner >= 0 && t.winner < 4) cnt.inter[t.winner] += 1;
+  } else {
+    cnt.uniforms += (uint32_t)(rng.cursor - cA);
+    cnt.overflow += (rng.overflow && !ovA) ? 1u : 0u;
+  }
+  cnt.secondaries += (uint32_t)(t.nsec > 2 ? 2 : t.nsec);
+  cnt.fallback += 1;
+}
+
+template <int BS>
+__global__ void __launch_bounds__(BS) final_fallback_kernel(const __grid_constant__ DevTables T,
+                                                             const hepem_track_state in, const hepem_track_state out,
+                                                             const double* __restrict__ uniforms, int nu,
+                                                             uint64_t seed, const hepem_step_out res, const Work w,
+                                                             hepem_step_counters* counters) {
+  const int64_t total = w.counts[kFbCount];
+  StepCount cnt = {};
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < total; j += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t i = w.queue[kNumQueues][j];
+    const int kind = w.fbKind[j];
+    if (kind == 0 || charged_model(kind - 1)) {
+      charged_full_step(T, in, out, uniforms, nu, seed, res, w, i, kind == 0, cnt);
+    } else {
+      if (kind - 1 == kQConversion)
+        stage_b_one<kQConversion, false>(T, in, out, uniforms, nu, seed, res, w, i, -1, cnt);
+      else if (kind - 1 == kQCompton)
+        stage_b_one<kQCompton, false>(T, in, out, uniforms, nu, seed, res, w, i, -1, cnt);
+      cnt.fallback += 1;
+    }
   }
   add_counters(cnt, counters);
 }
@@ -520,33 +588,27 @@ static void stage_table(StageFn* f) {
   f[10] = stage_b_kernel<8, BS, kStageFp64>;
 }
 
-// precision form: [kernel index] -> FP32 kernel and its FP64 fallback (null: none)
+// precision form: [kernel index] -> its FP32 kernel (null: FP64 only)
 template <int BS>
-static void mixed_table(StageFn* m, StageFn* f) {
-  for (int k = 0; k < kNumStageKernels; ++k) m[k] = f[k] = nullptr;
+static void mixed_table(StageFn* m) {
+  for (int k = 0; k < kNumStageKernels; ++k) m[k] = nullptr;
   m[0] = stage_a_charged_kernel<BS, kStageMixed>;
-  f[0] = stage_a_charged_kernel<BS, kStageFallback>;
   m[2 + kQIoniEm] = stage_b_kernel<kQIoniEm, BS, kStageMixed>;
-  f[2 + kQIoniEm] = stage_b_kernel<kQIoniEm, BS, kStageFallback>;
   m[2 + kQIoniEp] = stage_b_kernel<kQIoniEp, BS, kStageMixed>;
-  f[2 + kQIoniEp] = stage_b_kernel<kQIoniEp, BS, kStageFallback>;
   m[2 + kQBremSB] = stage_b_kernel<kQBremSB, BS, kStageMixed>;
-  f[2 + kQBremSB] = stage_b_kernel<kQBremSB, BS, kStageFallback>;
   m[2 + kQBremRB] = stage_b_kernel<kQBremRB, BS, kStageMixed>;
-  f[2 + kQBremRB] = stage_b_kernel<kQBremRB, BS, kStageFallback>;
   m[2 + kQAnnihFlight] = stage_b_kernel<kQAnnihFlight, BS, kStageMixed>;
-  f[2 + kQAnnihFlight] = stage_b_kernel<kQAnnihFlight, BS, kStageFallback>;
   m[2 + kQConversion] = stage_b_kernel<kQConversion, BS, kStageMixed>;
-  f[2 + kQConversion] = stage_b_kernel<kQConversion, BS, kStageFallback>;
   m[2 + kQCompton] = stage_b_kernel<kQCompton, BS, kStageMixed>;
-  f[2 + kQCompton] = stage_b_kernel<kQCompton, BS, kStageFallback>;
 }
 
 struct StageKernels {
   StageFn fn[3][kNumStageKernels];
   int occ[3][kNumStageKernels];  // resident CTAs per SM
-  StageFn mixed[3][kNumStageKernels], fallback[3][kNumStageKernels];  // precision form (null: FP64 only)
-  int occMixed[3][kNumStageKernels], occFallback[3][kNumStageKernels];
+  StageFn mixed[3][kNumStageKernels];  // precision form (null: FP64 only)
+  int occMixed[3][kNumStageKernels];
+  StageFn final_[3];                   // precision form: the FP64 fallback kernel
+  int occFinal[3];
 };
 
 static int occupancy_of(StageFn f, int bs) {
@@ -562,15 +624,19 @@ static const StageKernels& stage_kernels() {
     stage_table<128>(r.fn[0]);
     stage_table<256>(r.fn[1]);
     stage_table<512>(r.fn[2]);
-    mixed_table<128>(r.mixed[0], r.fallback[0]);
-    mixed_table<256>(r.mixed[1], r.fallback[1]);
-    mixed_table<512>(r.mixed[2], r.fallback[2]);
-    for (int b = 0; b < 3; ++b)
+    mixed_table<128>(r.mixed[0]);
+    mixed_table<256>(r.mixed[1]);
+    mixed_table<512>(r.mixed[2]);
+    r.final_[0] = final_fallback_kernel<128>;
+    r.final_[1] = final_fallback_kernel<256>;
+    r.final_[2] = final_fallback_kernel<512>;
+    for (int b = 0; b < 3; ++b) {
       for (int k = 0; k < kNumStageKernels; ++k) {
         r.occ[b][k] = occupancy_of(r.fn[b][k], kBlockSizes[b]);
         r.occMixed[b][k] = r.mixed[b][k] ? occupancy_of(r.mixed[b][k], kBlockSizes[b]) : 0;
-        r.occFallback[b][k] = r.fallback[b][k] ? occupancy_of(r.fallback[b][k], kBlockSizes[b]) : 0;
       }
+      r.occFinal[b] = occupancy_of(r.final_[b], kBlockSizes[b]);
+    }
     return r;
   }();
   return K;
@@ -632,12 +698,21 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
   for (int q = 0; q < kNumStageKernels; ++q) {
     const int b = bs_index(cfg.block[q]);
     if (o.mixed && K.mixed[b][q]) {
-      // precision form: the FP32 kernel, then the FP64 kernel over the tracks it gave up on
+      // precision form: the FP32 kernel (its FP64 fallbacks run after the last stage)
       const int om = K.occMixed[b][q];
       const int pm = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < om ? cfg.ctasPerSM[q] : om;
       K.mixed[b][q]<<<sms * pm, kBlockSizes[b], 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
-      K.fallback[b][q]<<<sms * K.occFallback[b][q], kBlockSizes[b], 0, s>>>(T, in, out, uniforms, nu, seed, res,
-                                                                             w, counters);
+      if (q == kNumStageKernels - 1) {
+        K.final_[1]<<<sms * K.occFinal[1], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+      }
+      mark();
+      continue;
+    }
+    if (o.mixed && q == kNumStageKernels - 1) {
+      const int occ = K.occ[b][q];
+      const int per = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < occ ? cfg.ctasPerSM[q] : occ;
+      K.fn[b][q]<<<sms * per, kBlockSizes[b], 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+      K.final_[1]<<<sms * K.occFinal[1], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
       mark();
       continue;
     }

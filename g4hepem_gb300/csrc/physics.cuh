@@ -331,8 +331,10 @@ struct Physics {
       tlimit = m.initRange;
     }
     const double tlm = m.tlimitMin;
+    HEPEM_TR(0, 24, tlimit);
     if (tlimit < m.trueStep) {
       const double d0 = tlimit > tlm ? dmax_(rng.gauss(tlimit, 0.1 * (tlimit - tlm)), tlm) : tlm;
+      HEPEM_TR(0, 25, d0);
       m.trueStep = dmin_(d0, m.trueStep);
     }
   }

@@ -27,6 +27,46 @@ namespace hepem {
 constexpr float kGuardTol = 2.44140625e-4f;  // 2^-12
 constexpr float kLargeF = 1.0E+20f;
 
+// ---- FP64 <-> FP32 conversions with integer operations ---------------------------------
+// Conversions between double and float issue on the FP64 pipe, which on this
+// GPU runs at 1/64 of the FP32 rate; for the values of this path (normal
+// floats, no NaN) the bit patterns are converted with integer operations.
+// d2f truncates the mantissa (error < 1 float ulp); f2d is exact.
+__device__ __forceinline__ float d2f(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32);
+  const unsigned sign = hi & 0x80000000u;
+  const int ef = (int)((hi >> 20) & 0x7FFu) - 1023 + 127;
+  if (ef <= 0) return __uint_as_float(sign);                  // zero, or below the float range
+  if (ef >= 255) return __uint_as_float(sign | 0x7F800000u);  // beyond the float range
+  const unsigned m = ((hi & 0xFFFFFu) << 3) | ((unsigned)b >> 29);
+  return __uint_as_float(sign | ((unsigned)ef << 23) | m);
+}
+__device__ __forceinline__ double f2d(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned e = (u >> 23) & 0xFFu;
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  if (e == 0u) return __longlong_as_double((long long)sign);  // zero (subnormals flushed)
+  const unsigned long long ed = e == 255u ? 0x7FFull : (unsigned long long)(e - 127u + 1023u);
+  return __longlong_as_double((long long)(sign | (ed << 52) | ((unsigned long long)(u & 0x7FFFFFu) << 29)));
+}
+// 1 - u for a uniform u in (0, 1) to float precision, without FP64 arithmetic:
+// for u >= 1/2, 1 - u = (2^52 - mantissa) 2^-53 is formed exactly in integers
+__device__ __forceinline__ float one_minus_u(double u) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(u);
+  if ((b >> 52) < 1022ull) return 1.0f - d2f(u);  // u < 1/2: no cancellation
+  const unsigned long long k = (1ull << 52) - (b & 0xFFFFFFFFFFFFFull);
+  if (k == 0ull) return 0.0f;
+  const int p = 63 - __clzll((long long)k);                  // k = 1.x 2^p
+  const unsigned m = (unsigned)((k << (63 - p)) >> 40) & 0x7FFFFFu;
+  return __uint_as_float(((unsigned)(p - 53 + 127) << 23) | m);
+}
+// nia <= 0 (or NaN-free zero) by the sign and magnitude bits
+__device__ __forceinline__ bool nonpositive(double x) {
+  const long long b = __double_as_longlong(x);
+  return b <= 0 || b == (long long)0x8000000000000000ull;
+}
+
 __device__ __forceinline__ float fmx(float a, float b) { return a > b ? a : b; }
 __device__ __forceinline__ float fmn(float a, float b) { return a < b ? a : b; }
 
@@ -73,6 +113,20 @@ __device__ __forceinline__ void rotate32(float* d, const float* r) {
     d[0] = -d[0];
     d[2] = -d[2];
   }
+}
+// rotation to the frame of the unit vector r, in FP32 where it is well
+// conditioned; within ~6 degrees of the z axis the division by the transverse
+// length sqrt(r0^2 + r1^2) amplifies FP32 rounding, and FP64 is used (rd: r in FP64)
+__device__ __forceinline__ void rotate_mixed(float* d, const float* r, const double* rd) {
+  if (r[0] * r[0] + r[1] * r[1] > 0.01f) {
+    rotate32(d, r);
+    return;
+  }
+  double v[3] = {d[0], d[1], d[2]};
+  rotate(v, rd);
+  d[0] = (float)v[0];
+  d[1] = (float)v[1];
+  d[2] = (float)v[2];
 }
 // -ln(u) for u in (0,1) to FP32 accuracy, also for u close to 1
 __device__ __forceinline__ float neg_log_u(double u) {
@@ -527,6 +581,7 @@ struct MixedEl {
         }
         // reference: if (tlimit < trueStep) { d0 = tlimit > tlimitMin ? max(gauss, tlimitMin) : tlimitMin;
         //                                     trueStep = min(d0, trueStep) }
+        HEPEM_TR(1, 24, tlimit);
         const bool limits = (tlimIsRange && pIsRange) ? false : lt(tlimit, trueStep);
         if (limits) {
           float d0;
@@ -540,6 +595,7 @@ struct MixedEl {
             d0 = tlimitMin;
             d0IsTlm = true;
           }
+          HEPEM_TR(1, 25, d0);
           near(d0, trueStep);
           if (d0 < trueStep) {
             trueStep = d0;
@@ -695,19 +751,21 @@ struct MixedEl {
           HEPEM_TR(1, 22, r);
           HEPEM_TR(1, 23, delta);
           const float cbeta = 2.16f;
-          const float cbeta1 = -expm1f(-cbeta * (float)kPi);
           const double r0 = rng.flat(), r1 = rng.flat();
-          const float psi = -log1pf(-(float)r0 * cbeta1) / cbeta;
+          // -ln(1 - r0 (1 - e^-cbeta pi)) / cbeta, with 1 - r0 (1 - q) = (1 - r0) + r0 q:
+          // no cancellation as r0 -> 1
+          const float q = expf(-cbeta * (float)kPi);
+          const float psi = -logf((float)(1.0 - r0) + (float)r0 * q) / cbeta;
           const float ph = lt((float)r1, 0.5f) ? phi + psi : phi - psi;
           float s2, c2;
           sincosf(ph, &s2, &c2);
           disp[0] = r * c2;
           disp[1] = r * s2;
-          rotate32(disp, tdir);
+          rotate_mixed(disp, tdir, t.dir);
         } else {
           dsp = false;
         }
-        rotate32(dir, tdir);
+        rotate_mixed(dir, tdir, t.dir);
         // renormalise in FP64 so that repeated steps keep unit directions
         const double nx = dir[0], ny = dir[1], nz = dir[2];
         const double inv = 1.0 / sqrt(nx * nx + ny * ny + nz * nz);
