@@ -281,8 +281,19 @@ __device__ __forceinline__ void fb_push(bool trip, int32_t idx, uint8_t kind, co
   }
 }
 
+// The FP32 stages are latency bound (dependent table gathers and special
+// functions per track): they are compiled for more resident warps per SM
+// (stage A: 32 warps, 64 registers; stage B: 24 warps, 80 registers); the FP64
+// stages keep their registers (their FP64 pipe is the limit).
+#ifndef HEPEM_MIXED_A_WARPS
+#define HEPEM_MIXED_A_WARPS 32
+#endif
+#ifndef HEPEM_MIXED_B_WARPS
+#define HEPEM_MIXED_B_WARPS 24
+#endif
 template <int BS, int MODE>
-__global__ void __launch_bounds__(BS) stage_a_charged_kernel(const __grid_constant__ DevTables T,
+__global__ void __launch_bounds__(BS, MODE == kStageMixed ? HEPEM_MIXED_A_WARPS * 32 / BS : 1)
+    stage_a_charged_kernel(const __grid_constant__ DevTables T,
                                                               const hepem_track_state in, const hepem_track_state out,
                                                               const double* __restrict__ uniforms, int nu,
                                                               uint64_t seed, const hepem_step_out res, const Work w,
@@ -321,7 +332,7 @@ __global__ void __launch_bounds__(BS) stage_a_charged_kernel(const __grid_consta
         cnt.steps += 1;
         cnt.uniforms += (uint32_t)(rng.cursor - c0);
         cnt.overflow += rng.overflow;
-        if (t.winner >= 0 && t.winner < 4) cnt.inter[t.winner] += 1;
+        if (t.winner >= 0 && t.winner < 4) count_inter(cnt, t.winner);
       }
     }
     warp_push(key, idx, w.queue, w.counts + 3);
@@ -369,7 +380,7 @@ __global__ void __launch_bounds__(BS) stage_a_gamma_kernel(const __grid_constant
       cnt.steps += 1;
       cnt.uniforms += (uint32_t)(rng.cursor - c0);
       cnt.overflow += rng.overflow;
-      if (t.winner >= 0 && t.winner < 4) cnt.inter[4 + t.winner] += 1;
+      if (t.winner >= 0 && t.winner < 4) count_inter(cnt, 4 + t.winner);
     }
     warp_push(key, idx, w.queue, w.counts + 3, pe, w.peXS, kQPhotoelectric);
   }
@@ -462,7 +473,7 @@ __device__ bool stage_b_one(const DevTables& T, const hepem_track_state& in, con
 }
 
 template <int Q, int BS, int MODE>
-__global__ void __launch_bounds__(BS) stage_b_kernel(const __grid_constant__ DevTables T,
+__global__ void __launch_bounds__(BS, MODE == kStageMixed ? HEPEM_MIXED_B_WARPS * 32 / BS : 1) stage_b_kernel(const __grid_constant__ DevTables T,
                                                       const hepem_track_state in, const hepem_track_state out,
                                                       const double* __restrict__ uniforms, int nu, uint64_t seed,
                                                       const hepem_step_out res, const Work w,
@@ -530,7 +541,7 @@ __device__ void charged_full_step(const DevTables& T, const hepem_track_state& i
     cnt.steps += 1;
     cnt.uniforms += (uint32_t)(rng.cursor - c0);
     cnt.overflow += rng.overflow;
-    if (t.winner >= 0 && t.winner < 4) cnt.inter[t.winner] += 1;
+    if (t.winner >= 0 && t.winner < 4) count_inter(cnt, t.winner);
   } else {
     cnt.uniforms += (uint32_t)(rng.cursor - cA);
     cnt.overflow += (rng.overflow && !ovA) ? 1u : 0u;
@@ -779,6 +790,7 @@ __global__ void __launch_bounds__(256) sample_kernel(const __grid_constant__ Dev
     bool redo = !MIXED;
     if (MIXED) {
       MixedB mb{T, rng, t, false};
+      mb.dirExact = true;
       sample_run(mb, model);
       if (mb.trip) {
         redo = true;

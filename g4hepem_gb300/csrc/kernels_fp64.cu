@@ -154,7 +154,7 @@ __device__ __forceinline__ void step_one(const DevTables& T, int64_t i, const he
   cnt.uniforms += (uint32_t)(rng.cursor - in.rng_cursor[i]);
   cnt.overflow += rng.overflow;
   cnt.secondaries += ns;
-  if (!bad && t.winner >= 0 && t.winner < 4) cnt.inter[(type == 2 ? 4 : 0) + t.winner] += 1;
+  if (!bad && t.winner >= 0 && t.winner < 4) count_inter(cnt, (type == 2 ? 4 : 0) + t.winner);
 }
 
 __global__ void __launch_bounds__(256) step_kernel(const __grid_constant__ DevTables T, int64_t n,

@@ -55,16 +55,63 @@ __device__ __forceinline__ double f2d(float x) {
 __device__ __forceinline__ float one_minus_u(double u) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(u);
   if ((b >> 52) < 1022ull) return 1.0f - d2f(u);  // u < 1/2: no cancellation
+  if ((b >> 52) > 1022ull) return 0.0f;           // u >= 1
   const unsigned long long k = (1ull << 52) - (b & 0xFFFFFFFFFFFFFull);
   if (k == 0ull) return 0.0f;
   const int p = 63 - __clzll((long long)k);                  // k = 1.x 2^p
   const unsigned m = (unsigned)((k << (63 - p)) >> 40) & 0x7FFFFFu;
   return __uint_as_float(((unsigned)(p - 53 + 127) << 23) | m);
 }
-// nia <= 0 (or NaN-free zero) by the sign and magnitude bits
+// x <= 0 for a double without NaN, from its bit pattern
 __device__ __forceinline__ bool nonpositive(double x) {
   const long long b = __double_as_longlong(x);
   return b <= 0 || b == (long long)0x8000000000000000ull;
+}
+// a < b for doubles a, b >= 0 (no NaN, no -0): the bit patterns order as integers
+__device__ __forceinline__ bool dless(double a, double b) {
+  return __double_as_longlong(a) < __double_as_longlong(b);
+}
+// max(x, 0) for a double without NaN
+__device__ __forceinline__ double dpos(double x) { return __double_as_longlong(x) < 0 ? 0.0 : x; }
+
+// x^2 (c[0] + c[1] x + ... + c[N-1] x^(N-1)), Horner
+template <int N>
+__device__ __forceinline__ float series2(float x, const float (&c)[N]) {
+  float a = c[N - 1];
+#pragma unroll
+  for (int k = N - 2; k >= 0; --k) a = fmaf(a, x, c[k]);
+  return a * x * x;
+}
+// Non-negative functions of the true -> geometrical path length conversion,
+// each by its power series where the direct form cancels (truncation < 1e-8
+// relative in the series' range):
+//   g(x) = x + (1 - x) ln(1 - x)   = sum_{k>=2} x^k / (k (k-1)),        0 <= x < 1
+//   h(y) = e^y - 1 - y             = sum_{k>=2} y^k / k!,               y <= 0
+//   P(b) = 1 - e^-b (1 + b)        = sum_{k>=2} (-1)^k (k-1) b^k / k!,  b >= 0
+//   Q(u) = u - 1 + e^-u            = sum_{k>=2} (-1)^k u^k / k!,        u >= 0
+__device__ __forceinline__ float geom_g(float x) {
+  if (x >= 0.25f) return x + (1.f - x) * log1pf(-x);
+  const float c[13] = {1.f / 2, 1.f / 6, 1.f / 12, 1.f / 20, 1.f / 30, 1.f / 42, 1.f / 56,
+                       1.f / 72, 1.f / 90, 1.f / 110, 1.f / 132, 1.f / 156, 1.f / 182};
+  return series2(x, c);
+}
+__device__ __forceinline__ float geom_h(float y) {
+  if (y <= -0.5f) return expm1f(y) - y;
+  const float c[9] = {1.f / 2, 1.f / 6, 1.f / 24, 1.f / 120, 1.f / 720, 1.f / 5040, 1.f / 40320, 1.f / 362880,
+                      1.f / 3628800};
+  return series2(y, c);
+}
+__device__ __forceinline__ float geom_p(float b) {
+  if (b >= 0.5f) return -expm1f(-b) - b * expf(-b);
+  const float c[10] = {1.f / 2, -2.f / 6, 3.f / 24, -4.f / 120, 5.f / 720, -6.f / 5040, 7.f / 40320,
+                       -8.f / 362880, 9.f / 3628800, -10.f / 39916800};
+  return series2(b, c);
+}
+__device__ __forceinline__ float geom_q(float u) {
+  if (u >= 0.5f) return u + expm1f(-u);
+  const float c[9] = {1.f / 2, -1.f / 6, 1.f / 24, -1.f / 120, 1.f / 720, -1.f / 5040, 1.f / 40320,
+                      -1.f / 362880, 1.f / 3628800};
+  return series2(u, c);
 }
 
 __device__ __forceinline__ float fmx(float a, float b) { return a > b ? a : b; }
@@ -117,20 +164,26 @@ __device__ __forceinline__ void rotate32(float* d, const float* r) {
 // rotation to the frame of the unit vector r, in FP32 where it is well
 // conditioned; within ~6 degrees of the z axis the division by the transverse
 // length sqrt(r0^2 + r1^2) amplifies FP32 rounding, and FP64 is used (rd: r in FP64)
+// (the FP64 branch is out of line: it is rare, and one copy keeps the code small)
+static __device__ __noinline__ float3 rotate64(float3 d, double r0, double r1, double r2) {
+  double v[3] = {d.x, d.y, d.z};
+  const double r[3] = {r0, r1, r2};
+  rotate(v, r);
+  return make_float3((float)v[0], (float)v[1], (float)v[2]);
+}
 __device__ __forceinline__ void rotate_mixed(float* d, const float* r, const double* rd) {
   if (r[0] * r[0] + r[1] * r[1] > 0.01f) {
     rotate32(d, r);
     return;
   }
-  double v[3] = {d[0], d[1], d[2]};
-  rotate(v, rd);
-  d[0] = (float)v[0];
-  d[1] = (float)v[1];
-  d[2] = (float)v[2];
+  const float3 o = rotate64(make_float3(d[0], d[1], d[2]), rd[0], rd[1], rd[2]);
+  d[0] = o.x;
+  d[1] = o.y;
+  d[2] = o.z;
 }
 // -ln(u) for u in (0,1) to FP32 accuracy, also for u close to 1
 __device__ __forceinline__ float neg_log_u(double u) {
-  return u > 0.5 ? -log1pf(-(float)(1.0 - u)) : -logf((float)u);
+  return dless(0.5, u) ? -log1pf(-one_minus_u(u)) : -logf(d2f(u));
 }
 
 // ---- FP32 e+- table accessors (G4HepEmElectronManager.icc:486-599) -----------------
@@ -156,36 +209,95 @@ __device__ __forceinline__ float transport_mfp32(const DevElData32& f, int nL, i
   const float v = fmx(0.f, spline_log_xy32(nL, f.lossGrid, f.tr1 + 2 * nL * imat, e, le, f.lossLogMin, f.lossILD));
   return v > 0.f ? 1.f / v : kLargeF;
 }
-// restricted macroscopic cross section (at the energy e, FP64 threshold tests)
+// restricted macroscopic cross section (at the energy e, exact threshold test)
 __device__ __forceinline__ float rest_macxs32(const DevElData& d, const DevElData32& f, int imc, double e, float ef,
                                               float le, bool ioni) {
   const int i0 = ld(d.xsStart + imc);
-  const int st = ioni ? i0 : i0 + 3 * (int)ld(d.xs + i0) + 5;
-  const int nd = (int)ld(d.xs + st);
-  if (e < ld(d.xs + st + 5)) return 0.f;
+  const int st = ioni ? i0 : i0 + 3 * (int)ld(f.xs + i0) + 5;
+  const int nd = (int)ld(f.xs + st);
+  if (dless(e, ld(d.xs + st + 5))) return 0.f;
   return fmx(0.f, spline_log_3_32(nd, f.xs + st + 5, ef, le, ld(f.xs + st + 3), ld(f.xs + st + 4)));
 }
+// the cross section for stepping, max over [0.8 e, e]: continuous in e at
+// both switches (e at the energy of the maximum, 0.8 e at it), so they are
+// taken in FP32; the threshold test is exact
 __device__ __forceinline__ float rest_macxs_stepping32(const DevElData& d, const DevElData32& f, int imc, double e,
-                                                       float le, bool ioni) {
+                                                       float ef, float le, bool ioni) {
   const int i0 = ld(d.xsStart + imc);
-  const int st = ioni ? i0 : i0 + 3 * (int)ld(d.xs + i0) + 5;
-  const int nd = (int)ld(d.xs + st);
-  const double minE = ld(d.xs + st + 5), maxE = ld(d.xs + st + 1);
-  double ee = e;
-  if (e > maxE) {
-    const double er = 0.8 * e;
+  const int st = ioni ? i0 : i0 + 3 * (int)ld(f.xs + i0) + 5;
+  const int nd = (int)ld(f.xs + st);
+  const float maxE = ld(f.xs + st + 1);
+  float ee = ef;
+  if (ef > maxE) {
+    const float er = 0.8f * ef;
     if (er < maxE) return fmx(0.f, ld(f.xs + st + 2));
     ee = er;
     le += -0.22314355f;  // log(0.8)
+    if (ee < ld(f.xs + st + 5)) return 0.f;
+  } else if (dless(e, ld(d.xs + st + 5))) {
+    return 0.f;
   }
-  if (ee < minE) return 0.f;
-  return fmx(0.f, spline_log_3_32(nd, f.xs + st + 5, (float)ee, le, ld(f.xs + st + 3), ld(f.xs + st + 4)));
+  return fmx(0.f, spline_log_3_32(nd, f.xs + st + 5, ee, le, ld(f.xs + st + 3), ld(f.xs + st + 4)));
 }
 __device__ __forceinline__ float nuc_macxs32(const DevElData& d, const DevElData32& f, int imat, double e, float ef,
                                              float le) {
-  if (e < ld(d.nucGrid)) return 0.f;
+  if (dless(e, ld(d.nucGrid))) return 0.f;
   const int n = d.nNuc;
   return fmx(0.f, spline_log_xy32(n, f.nucGrid, f.nuc + imat * 2 * n, ef, le, f.nucLogMin, f.nucILD));
+}
+
+// ---- FP64 range <-> energy for the mean energy loss ----------------------------------
+// The reference's splines (G4HepEmRunUtils.icc:49-99) in FP64 where the
+// inversion needs it, at a few FP64 operations: the interval is located on the
+// FP32 copy and made exact by comparing the FP64 knots (integer comparisons of
+// positive values); the interpolation variable is an FP32 quotient refined by
+// one FP64 residual step (relative error ~1e-14 instead of an FP64 division);
+// the curvature term, a small fraction of y, is evaluated in FP32.
+__device__ __forceinline__ double spline64_lite(double x1, double x2, double y1, double y2, float s1, float s2,
+                                                double x) {
+  const double dl = x2 - x1, dx = x - x1;
+  const float dlf = d2f(dl);
+  const float b0 = d2f(dx) / dlf;
+  const double res = fma(-f2d(b0), dl, dx);
+  const double b = f2d(b0) + f2d(d2f(res) / dlf);
+  const float bf = d2f(b);
+  const float curv = (bf * (bf - 1.0f)) * ((2.0f - bf) * s1 + (1.0f + bf) * s2) * (dlf * dlf * 0.166666666667f);
+  return fma(b, y2 - y1, y1) + f2d(curv);
+}
+// restricted range at e (lef: FP32 log e for the interval)
+__device__ __forceinline__ double rest_range64(const DevElData& d, const DevElData32& f, int imc, double e,
+                                               float lef) {
+  const int n = d.nLoss;
+  const double* xd = d.lossGrid;
+  const double x0 = ld(xd), xn = ld(xd + n - 1);
+  const double xv = dless(e, x0) ? x0 : dless(xn, e) ? xn : e;
+  int i = bin32(lef, f.lossLogMin, f.lossILD, n);
+  if (i > 0 && dless(xv, ld(xd + i))) --i;
+  else if (i < n - 2 && !dless(xv, ld(xd + i + 1))) ++i;
+  const double* yd = d.loss + 5 * n * imc;
+  const float* yf = f.loss + 5 * n * imc;
+  return dpos(spline64_lite(ld(xd + i), ld(xd + i + 1), ld(yd + 2 * i), ld(yd + 2 * i + 2), ld(yf + 2 * i + 1),
+                            ld(yf + 2 * i + 3), xv));
+}
+// energy of the restricted range r (G4HepEmElectronManager.icc:547-561)
+__device__ __forceinline__ double inv_range64(const DevElData& d, const DevElData32& f, int imc, double r) {
+  const int n = d.nLoss;
+  const double* R = d.loss + 5 * n * imc;
+  const double rmin = ld(R);
+  if (dless(r, rmin)) {  // (also r < 0)
+    const double q = r / rmin;
+    return dpos(ld(d.lossGrid) * q * q);
+  }
+  const float* Rf = f.loss + 5 * n * imc;
+  const double rn = ld(R + 2 * (n - 1));
+  const double rv = dless(rn, r) ? rn : r;
+  int i = lower_bin32(Rf, n, d2f(rv), 2);
+  i = i < 0 ? 0 : i;
+  if (i > 0 && dless(rv, ld(R + 2 * i))) --i;
+  else if (i < n - 2 && !dless(rv, ld(R + 2 * (i + 1)))) ++i;
+  const float* S2 = Rf + 4 * n;
+  return dpos(spline64_lite(ld(R + 2 * i), ld(R + 2 * (i + 1)), ld(d.lossGrid + i), ld(d.lossGrid + i + 1),
+                            ld(S2 + i), ld(S2 + i + 1), rv));
 }
 __device__ __forceinline__ float annih_macxs32(float e, float ne) {
   const float tau = e * (float)kInvMec2;
@@ -230,7 +342,7 @@ struct MixedEl {
   __device__ float gauss(float mean, float sd) {
     if (rng.gaussValid) {
       rng.gaussValid = false;
-      return (float)rng.gaussValue * sd + mean;
+      return d2f(rng.gaussValue) * sd + mean;
     }
     double r, v1, v2;
     int it = 0;
@@ -240,20 +352,20 @@ struct MixedEl {
       v2 = 2. * b - 1.;
       r = v1 * v1 + v2 * v2;
       if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
-    } while (r > 1.);
-    const float rf = (float)r;
-    // ln r to FP32 accuracy on both ends of (0, 1]
-    const float lr = r < 0.5 ? logf(rf) : log1pf(-(float)(1.0 - r));
+    } while (dless(1.0, r));
+    const float rf = d2f(r);
+    // ln r to FP32 accuracy on both ends of (0, 1]; 1 - r is exact for r >= 1/2
+    const float lr = dless(r, 0.5) ? logf(rf) : log1pf(-one_minus_u(r));
     const float fac = sqrtf(-2.f * lr / rf);
-    rng.gaussValue = (double)((float)v1 * fac);
+    rng.gaussValue = f2d(d2f(v1) * fac);
     rng.gaussValid = true;
-    return (float)v2 * fac * sd + mean;
+    return d2f(v2) * fac * sd + mean;
   }
 
   __device__ int poisson(float mean) {
     int number = 0;
     if (le(mean, 16.f)) {
-      const float position = (float)rng.flat();
+      const float position = d2f(rng.flat());
       float pv = expf(-mean);
       float ps = pv;
       // the cumulative carries the FP32 error of the mean (~1e-6 of mean times
@@ -271,7 +383,7 @@ struct MixedEl {
     }
     const double a = rng.flat(), b = rng.flat();
     float sb, cb;
-    sincosf((float)(k2Pi * b), &sb, &cb);
+    sincospif(2.f * d2f(b), &sb, &cb);
     const float tt = sqrtf(2.f * neg_log_u(a)) * cb;
     const float value = mean + tt * sqrtf(mean) + 0.5f;
     // the integer part is a discrete outcome: guard the distance to the nearest integer
@@ -282,7 +394,7 @@ struct MixedEl {
 
   __device__ float gauss_loss(float me, float s2) {
     const float twom = 2.f * me;
-    if (lt(me * me, 0.0625f * s2)) return twom * (float)rng.flat();
+    if (lt(me * me, 0.0625f * s2)) return twom * d2f(rng.flat());
     const float sig = sqrtf(s2);
     float el;
     int it = 0;
@@ -296,8 +408,15 @@ struct MixedEl {
   }
 
   // Urban fluctuation model (G4HepEmElectronEnergyLossFluctuation.icc:11-111);
-  // the sum of the sampled terms is accumulated in FP64
-  __device__ double fluct(float tcut, float excE, float meanE) {
+  // the sampled terms (all >= 0) are summed with compensation (Neumaier), so
+  // that the sum carries the terms' own FP32 accuracy
+  float fsum, fcomp;
+  __device__ __forceinline__ void fadd(float x) {
+    const float s = fsum + x;
+    fcomp += fabsf(fsum) >= fabsf(x) ? (fsum - s) + x : (x - s) + fsum;
+    fsum = s;
+  }
+  __device__ float fluct(float tcut, float excE, float meanE) {
     const float scaling = fmn(1.f + 5.E-4f / tcut, 1.5f);
     const float meanLoss = meanE / scaling;
     const float rate = 0.56f, e0 = 1.E-5f, nmax = 8.f;
@@ -305,7 +424,8 @@ struct MixedEl {
     float a3 = meanLoss * (tcut - e0) / (e0 * tcut * logf(w1));
     float a1 = 0.f;
     float e1 = excE;
-    double eloss = 0.0;
+    fsum = 0.f;
+    fcomp = 0.f;
     HEPEM_TR(1, 18, a3);
     if (lt(excE, tcut)) {
       const float a1t = meanLoss * (1.f - rate) / excE;
@@ -315,12 +435,12 @@ struct MixedEl {
       a3 *= rate;
       if (lt(nmax, a1)) {
         const float em = a1 * e1;
-        eloss = gauss_loss(em, em * e1);
+        fadd(gauss_loss(em, em * e1));
       } else {
         const int p = poisson(a1);
         HEPEM_TR(1, 17, p);
         // ((p + 1) - 2u) e1 as ((p - 1) + 2 (1 - u)) e1: no cancellation for p = 1, u -> 1
-        eloss = p > 0 ? (double)(((float)(p - 1) + 2.f * (float)(1.0 - rng.flat())) * e1) : 0.;
+        if (p > 0) fadd(((float)(p - 1) + 2.f * one_minus_u(rng.flat())) * e1);
       }
     }
     if (a3 > 0.f) {
@@ -339,7 +459,7 @@ struct MixedEl {
         const float nam = a3 * a3 / (nmax + a3);
         const float em = nam * e0 * alfa1;
         const float s2 = e0 * e0 * nam * (alfa - alfa1 * alfa1);
-        eloss += gauss_loss(em, s2);
+        fadd(gauss_loss(em, s2));
         p3 = a3 * nmax / (nmax + a3);
         w = nmax * (w1 - 1.f) / den;
       }
@@ -351,33 +471,38 @@ struct MixedEl {
         if (nnb > kMaxIter) { nnb = kMaxIter; t.flags |= kFlagLoopCap; }
         // 1 - w u as (1 - w) + w (1 - u): no cancellation in the Landau tail (u -> 1/w)
         const float omw = w3 / tcut;
-        for (int k = 0; k < nnb; ++k) eloss += (double)(w3 / (omw + w * (float)(1.0 - rng.flat())));
+        for (int k = 0; k < nnb; ++k) fadd(w3 / (omw + w * one_minus_u(rng.flat())));
       }
     }
-    return eloss * (double)scaling;
+    return (fsum + fcomp) * scaling;
   }
 
-  // Urban MSC cos(theta) (G4HepEmElectronInteractionUMSC.icc:153-270); the
-  // result is assembled in FP64 so that 1 - cos keeps its precision
+  // Urban MSC cos(theta) (G4HepEmElectronInteractionUMSC.icc:153-270), given
+  // as 1 - cos and 1 + cos, each to FP32 relative precision
+  struct CosT {
+    float omc, opc;
+  };
+  // cos = -1 + 2 u for a uniform u
+  __device__ static CosT cos_uniform(double u) { return CosT{2.f * one_minus_u(u), 2.f * d2f(u)}; }
   // d0 = 3 <x^2> - 1 and d1 = 2 <x> - d0, given without cancellation (cos_theta)
-  __device__ double simple_scatter(float xm, float d0, float d1) {
+  __device__ CosT simple_scatter(float xm, float d0, float d1) {
     const float a = 1.f + 4.f * d0 / d1;
     const float prob = (2.f + a) * xm / a;
     const double r0 = rng.flat(), r1 = rng.flat();
-    if (!lt((float)r0, prob)) return -1. + 2. * r1;
-    // -1 + 2 r1^(1/(1+a)), with 1 - cos or 1 + cos kept to FP32 precision
+    if (!lt(d2f(r0), prob)) return cos_uniform(r1);
+    // cos = -1 + 2 pw, pw = r1^(1/(1+a)): 1 + cos = 2 pw, 1 - cos = -2 expm1(ln pw)
     const float lg = (1.f / (1.f + a)) * -neg_log_u(r1);
     const float pw = expf(lg);
-    return pw < 0.5f ? -1. + 2. * (double)pw : 1. + 2. * (double)expm1f(lg);
+    return CosT{pw < 0.5f ? 2.f - 2.f * pw : -2.f * expm1f(lg), 2.f * pw};
   }
 
-  __device__ float theta0_of(float srl, float postE, float preE, const DevMat& md) {
+  __device__ float theta0_of(float srl, float postE, float preE, const DevMat32& md) {
     const float me = (float)kMec2;
     const float postInv = (postE + me) / (postE * (postE + 2.f * me));
     const float inv = preE != postE ? sqrtf(postInv * (preE + me) / (preE * (preE + 2.f * me))) : postInv;
     float y = srl;
-    if (!t.isEl && T.mscPosCor) y = srl * pos_correction32(preE * postE, (float)ld(&md.zeff));
-    return 13.6f * sqrtf(y) * inv * ((float)ld(&md.theta[0]) + (float)ld(&md.theta[1]) * logf(y));
+    if (!t.isEl && T.mscPosCor) y = srl * pos_correction32(preE * postE, ld(&md.zeff));
+    return 13.6f * sqrtf(y) * inv * (ld(&md.theta[0]) + ld(&md.theta[1]) * logf(y));
   }
 
   __device__ static float pos_correction32(float eekin, float zeff) {
@@ -399,16 +524,16 @@ struct MixedEl {
 
   bool exactCos;  // cos_theta returned an exact 1.0 of the reference's own shortcuts
 
-  __device__ double cos_theta(float pstep, float preE, float preMFP, float postE, float postMFP, float tlimMin,
-                              const DevMat& md, bool pIsTlm) {
+  __device__ CosT cos_theta(float pstep, float preE, float preMFP, float postE, float postMFP, float tlimMin,
+                            const DevMat32& md, bool pIsTlm) {
     exactCos = false;
     const float iPre = 1.0f / preMFP;
     const float dR = preMFP - postMFP;
     const float tau = lt(0.01f * preMFP, fabsf(dR)) ? pstep * logf(preMFP / postMFP) / dR : pstep * iPre;
-    if (lt(8.0f, tau)) return 2.0 * rng.flat() - 1.0;
+    if (lt(8.0f, tau)) return cos_uniform(rng.flat());
     if (lt(tau, 1.0E-16f)) {
       exactCos = true;
-      return 1.0;
+      return CosT{0.f, 2.f};
     }
     // <x> = xm and <x^2> = x2m of the reference (with its 0.333333); the simple
     // model needs d0 = 3 x2m - 1 and d1 = 2 xm - d0, formed here so that the
@@ -424,7 +549,7 @@ struct MixedEl {
       d1 = 3.0e-6f + 2.0f * expm1f(-tau) - 1.999998f * expm1f(-2.5f * tau);
     }
     if (lt(postE, 0.5f * preE)) return simple_scatter(xm, d0, d1);
-    const float radLen = (float)ld(&md.radLength);
+    const float radLen = ld(&md.radLength);
     const float tsmall = fmn(tlimMin, 1.0f);
     // pstep == tlimitMin by construction when the MSC limit chose it
     const bool notSmall = (pIsTlm && tlimMin <= 1.0f) ? false : lt(tsmall, pstep);
@@ -434,12 +559,12 @@ struct MixedEl {
     const float th2 = theta0 * theta0;
     if (lt(th2, 1.0E-16f)) {
       exactCos = true;
-      return 1.0;
+      return CosT{0.f, 2.f};
     }
     const float dumtau = notSmall ? tau : tsmall * iPre;
-    const float u = powf(dumtau, 0.1666666f);
-    const float dumxsi = (float)ld(&md.tail[0]) + u * ((float)ld(&md.tail[1]) + u * (float)ld(&md.tail[2])) +
-                         (float)ld(&md.tail[3]) * logf(pstep / (tau * radLen));
+    const float u = exp2f(0.1666666f * log2f(dumtau));
+    const float dumxsi = ld(&md.tail[0]) + u * (ld(&md.tail[1]) + u * ld(&md.tail[2])) +
+                         ld(&md.tail[3]) * logf(pstep / (tau * radLen));
     const float xsi = fmx(dumxsi, 1.9f);
     // the reference moves c off the poles of its formulas at 2 and 3
     const bool pole3 = lt(fabsf(xsi - 3.f), 0.001f), pole2 = lt(fabsf(xsi - 2.f), 0.001f);
@@ -449,7 +574,7 @@ struct MixedEl {
     const float eaa = 1.f / (1.f - ea);
     float thex = th2 * (1.0f - th2 * 0.0833333f);
     if (th2 > 0.01f) {
-      const float q = 2.0f * sinf(0.5f * theta0);
+      const float q = 2.0f * sinpif(theta0 * (float)(0.5 / kPi));
       thex = q * q;
     }
     const float xmean1 = 1.f - (1.f - (1.f + xsi) * ea) * thex * eaa;
@@ -458,26 +583,29 @@ struct MixedEl {
     const float bx = c * thex;
     const float b = bx + x0;
     const float b1 = b + 1.f;
-    const float eb1 = powf(b1, c1);
-    const float ebx = powf(bx, c1);
-    const float dd = ebx / eb1;
+    const float dd = powf(bx / b1, c1);  // bx^c1 / b1^c1
     const float xmean2 = (x0 + dd - (bx - b1 * dd) / (c - 2.f)) / (1.f - dd);
     const float f1x0 = ea * eaa;
     const float f2x0 = c1 / (c * (1.f - dd));
     const float prob = f2x0 / (f1x0 + f2x0);
     const float qprb = xm / (prob * xmean1 + (1.f - prob) * xmean2);
     const double r0 = rng.flat(), r1 = rng.flat(), r2 = rng.flat();
-    if (lt((float)r0, qprb)) {
+    if (lt(d2f(r0), qprb)) {
       // log(ea + r2/eaa) = log(1 - (1 - r2)(1 - ea)): log1p keeps small angles
-      if (lt((float)r1, prob)) return 1. + (double)(log1pf(-(float)(1.0 - r2) * (1.f - ea)) * thex);
-      const float var0 = (1.0f - dd) * (float)r2;
+      if (lt(d2f(r1), prob)) {
+        const float omc = -(log1pf(-one_minus_u(r2) * (1.f - ea)) * thex);
+        return CosT{omc, 2.f - omc};
+      }
+      const float var0 = (1.0f - dd) * d2f(r2);
       if (lt(var0, 0.01f * dd)) {
         const float var = var0 / (dd * c1);
-        return -1.0 + (double)(var * (1.0f - var * 0.5f * c) * b1);
+        const float opc = var * (1.0f - var * 0.5f * c) * b1;
+        return CosT{2.f - opc, opc};
       }
-      return 1.0 + (double)(thex * (c - xsi - c * powf(var0 + dd, -1.f / c1)));
+      const float omc = -(thex * (c - xsi - c * powf(var0 + dd, -1.f / c1)));
+      return CosT{omc, 2.f - omc};
     }
-    return 2.0 * r1 - 1.0;
+    return cos_uniform(r1);
   }
 
   // ---- the stage: HowFar + Perform up to the pending discrete interaction ------------
@@ -488,17 +616,17 @@ struct MixedEl {
     const DevElData32& f = elf();
     const int nL = d.nLoss;
     const int imc = t.imc;
-    const DevCouple c = T.couples[imc];
-    const DevRegion& reg = T.regions[c.region];
-    const DevMat& md = T.mats[c.mat];
+    const int cMat = ld(&T.couples[imc].mat), cRegion = ld(&T.couples[imc].region);
+    const DevRegion32& reg = T.regions32[cRegion];
+    const DevMat32& md = T.mats32[cMat];
     // -- HowFar (G4HepEmElectronManager.icc:35-101)
 #pragma unroll
     for (int ip = 0; ip < 4; ++ip)
-      if (t.nia[ip] <= 0.) t.nia[ip] = (double)neg_log_u(rng.flat());
+      if (nonpositive(t.nia[ip])) t.nia[ip] = f2d(neg_log_u(rng.flat()));
     const double e = t.e;
-    const float ef = (float)e, lef = logf(ef);
+    const float ef = d2f(e), lef = logf(ef);
     const float range = rest_range32(f, nL, imc, ef, lef);
-    const float frange = (float)ld(&reg.finalRange), drange = (float)ld(&reg.dRoverRange);
+    const float frange = ld(&reg.finalRange), drange = ld(&reg.dRoverRange);
     // The step function.  Some later comparisons of the reference meet values
     // that are equal by construction (pstep == range, trueStep == pstep,
     // trueStep == tlimitMin); their provenance is tracked here so that those
@@ -510,13 +638,13 @@ struct MixedEl {
     HEPEM_TR(1, 1, pstep);
     int winner = -1;
     float mx[4], mfp[4], nia[4];
-    mx[0] = rest_macxs_stepping32(d, f, imc, e, lef, true);
-    mx[1] = rest_macxs_stepping32(d, f, imc, e, lef, false);
-    mx[2] = t.isEl ? 0.f : annih_macxs32(0.8f * ef, (float)ld(&md.elDensity));
-    mx[3] = nuc_macxs32(d, f, c.mat, e, ef, lef);
+    mx[0] = rest_macxs_stepping32(d, f, imc, e, ef, lef, true);
+    mx[1] = rest_macxs_stepping32(d, f, imc, e, ef, lef, false);
+    mx[2] = t.isEl ? 0.f : annih_macxs32(0.8f * ef, ld(&md.elDensity));
+    mx[3] = nuc_macxs32(d, f, cMat, e, ef, lef);
 #pragma unroll
     for (int ip = 0; ip < 4; ++ip) {
-      nia[ip] = (float)t.nia[ip];
+      nia[ip] = d2f(t.nia[ip]);
       mfp[ip] = mx[ip] > 0.f ? 1.f / mx[ip] : kLargeF;
       const float lim = mfp[ip] * nia[ip];
       if (lt(lim, pstep)) { pstep = lim; winner = ip; pIsRange = false; }
@@ -528,24 +656,24 @@ struct MixedEl {
     // MSC step limit and true -> geometrical length (UMSC.icc:19-126, Manager.icc:602-650)
     float trueStep = pstep, zPath = pstep, lambtr1 = kLargeF;
     float delta = 0.f;  // trueStep - zPath, kept without cancellation (lateral displacement)
-    float initRange = (float)t.msc.initRange, dynFactor = (float)t.msc.dynFactor;
-    float tlimitMin = (float)t.msc.tlimitMin;
+    float initRange = d2f(t.msc.initRange), dynFactor = d2f(t.msc.dynFactor);
+    float tlimitMin = d2f(t.msc.tlimitMin);
     bool firstStep = t.msc.firstStep;
     bool active = false, displace = false;
     bool tsIsP = true, tsIsTlm = false;  // trueStep == pstep / == tlimitMin
     bool atRange = pIsRange;             // trueStep == range
     float gstep = pstep;
-    if (lt(5.E-8f, pstep) && e > 1.0E-3) {
+    if (lt(5.E-8f, pstep) && dless(1.0E-3, e)) {
       active = true;
-      lambtr1 = transport_mfp32(f, nL, c.mat, ef, lef);
+      lambtr1 = transport_mfp32(f, nL, cMat, ef, lef);
       // -- step limit
       const float kTLimitMinfix = 1.0E-8f;
-      const float safety = (float)t.safety;
+      const float safety = d2f(t.safety);
       displace = true;
-      if (lt(trueStep, kTLimitMinfix) || lt(range * (float)ld(&md.umscPar), safety)) {
+      if (lt(trueStep, kTLimitMinfix) || lt(range * ld(&md.umscPar), safety)) {
         displace = false;
       } else {
-        const float rf = (float)ld(&reg.mscRangeFactor), sf = (float)ld(&reg.mscSafetyFactor);
+        const float rf = ld(&reg.mscRangeFactor), sf = ld(&reg.mscSafetyFactor);
         float tlimit;
         bool tlimIsRange = false, tlimIsTlm = false;  // tlimit == range / == tlimitMin
         if (!ld(&reg.mscMinimal)) {
@@ -553,10 +681,9 @@ struct MixedEl {
             const float l1 = lambtr1;
             initRange = fmx(range, l1);
             dynFactor = l1 > 1.0f ? rf * (0.75f + 0.25f * l1) : rf;
-            const float stepMin = l1 * 1.0E-3f /
-                (2.0E-3f + ef * ((float)ld(&md.stepMin[0]) + ef * (float)ld(&md.stepMin[1])));
-            const float d0 = t.isEl ? 0.87f * (float)ld(&md.zeff23) : 0.70f * (float)ld(&md.zeffSqrt);
-            const float d1 = e > 5.0E-3 ? d0 * stepMin : d0 * stepMin * 0.5f * (1.0f + ef * 200.0f);
+            const float stepMin = l1 * 1.0E-3f / (2.0E-3f + ef * (ld(&md.stepMin[0]) + ef * ld(&md.stepMin[1])));
+            const float d0 = t.isEl ? 0.87f * ld(&md.zeff23) : 0.70f * ld(&md.zeffSqrt);
+            const float d1 = dless(5.0E-3, e) ? d0 * stepMin : d0 * stepMin * 0.5f * (1.0f + ef * 200.0f);
             tlimitMin = fmx(d1, kTLimitMinfix);
             firstStep = false;
           }
@@ -628,29 +755,38 @@ struct MixedEl {
           // below ~1e-12 the reference's own rounding decides whether zPath < trueStep
           if (tau < 1.0e-12f) set_trip();
         } else {
-          // the range-based conversions: evaluated in FP64 from the FP32 inputs,
-          // so that trueStep - zPath (the displacement length) keeps the
-          // inputs' relative accuracy where zPath is close to trueStep
-          const double R = range, L = lambtr1, ts = trueStep;
-          double z;
-          if (e < kMec2 || atRange) {
-            const double par1 = 1. / R;
-            const double par3 = 1. + 1. / (par1 * L);
-            z = 1. / (par1 * par3);
-            if (!atRange) z *= -expm1(par3 * log1p(-ts / R));
+          // the range-based conversions (UMSC.icc:105-126) in forms without
+          // cancellation, so that trueStep - zPath (the displacement length)
+          // keeps the inputs' FP32 accuracy where zPath is close to trueStep.
+          // Below m_e c^2, with x = trueStep / range and q = range / lambda:
+          //   trueStep - zPath = range (q g(x) + (1 - x) h(q ln(1 - x))) / (1 + q);
+          // above, with lambda1 the transport mfp at E(range - trueStep),
+          // b = ln(lambda / lambda1), s = trueStep / (lambda (1 - e^-b)), u = s b:
+          //   trueStep - zPath = trueStep (u P(b) + b e^-b Q(u)) / ((b + u)(1 - e^-b))
+          // (g, h, P, Q >= 0: geom_g .. geom_q)
+          float dz;
+          if (dless(e, kMec2) || atRange) {
+            const float q = range / lambtr1;
+            if (atRange) {
+              dz = range * q / (1.f + q);
+            } else {
+              const float x = trueStep / range;
+              dz = range * (q * geom_g(x) + (1.f - x) * geom_h(q * log1pf(-x))) / (1.f + q);
+            }
           } else {
             const float rfin = fmx(range - trueStep, 0.01f * range);
             const float t1 = inv_range32(f, nL, imc, rfin);
-            const double l1 = transport_mfp32(f, nL, c.mat, t1, logf(t1));
-            const double par1 = (L - l1) / (L * ts);
-            const double par3 = 1. + 1. / (par1 * L);
-            z = -expm1(par3 * log(l1 / L)) / (par1 * par3);
+            const float l1 = transport_mfp32(f, nL, cMat, t1, logf(t1));
+            const float b = logf(lambtr1 / l1);
+            if (!(b > 1.0e-6f)) set_trip();  // lambda1 >= lambda: left to the FP64 code
+            const float omea = -expm1f(-b);
+            const float u = trueStep / (lambtr1 * omea) * b;
+            dz = trueStep * (u * geom_p(b) + b * expf(-b) * geom_q(u)) / ((b + u) * omea);
           }
-          const double dz = ts - z;
           // the reference displaces only when zPath < trueStep
-          if (dz < 1.0e-9 * ts) set_trip();
-          zPath = (float)z;
-          delta = (float)dz;
+          if (!(dz >= 1.0e-9f * trueStep)) set_trip();
+          zPath = trueStep - dz;
+          delta = dz;
         }
         if (delta == 0.f) delta = trueStep - zPath;
         if (zPath > lambtr1) {
@@ -669,14 +805,14 @@ struct MixedEl {
       if (gstep < zPath) set_trip();
     }
     t.winner = winner;
-    t.gstep = (double)gstep;
-    t.msc.initRange = (double)initRange;
-    t.msc.dynFactor = (double)dynFactor;
-    t.msc.tlimitMin = (double)tlimitMin;
+    t.gstep = f2d(gstep);
+    t.msc.initRange = f2d(initRange);
+    t.msc.dynFactor = f2d(dynFactor);
+    t.msc.tlimitMin = f2d(tlimitMin);
     t.msc.firstStep = firstStep;
     t.msc.disp[0] = t.msc.disp[1] = t.msc.disp[2] = 0.;
 #pragma unroll
-    for (int ip = 0; ip < 4; ++ip) t.mfp[ip] = (double)mfp[ip];
+    for (int ip = 0; ip < 4; ++ip) t.mfp[ip] = f2d(mfp[ip]);
 
     // -- Perform: continuous part (G4HepEmElectronManager.icc:375-405).  With
     // no geometry the geometrical step is the one HowFar proposed, so the
@@ -691,31 +827,30 @@ struct MixedEl {
       pAtRange = atRange;
       if (le(p, 5.E-8f) || atRange) active = false;
     }
-    t.pstep = (double)p;
+    t.pstep = f2d(p);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) t.nia[i] = (double)(nia[i] - p / mfp[i]);
+    for (int i = 0; i < 4; ++i) t.nia[i] = f2d(nia[i] - p / mfp[i]);
     // mean energy loss (G4HepEmElectronManager.icc:216-259); the range->energy
     // inversion in FP64
     const double preE = e;
     const float preEf = ef;
-    if (pAtRange || e <= T.minLossE) {
+    if (pAtRange || !dless(T.minLossE, e)) {
       t.edep = e;
       t.setE(0.0);
       return t.isEl ? -1 : kQAnnihRest;
     }
-    double eloss = (double)(p * rest_dedx32(f, nL, imc, ef, lef));
-    if (lt((float)((double)ld(&reg.linELossLimit) * e), (float)eloss)) {
-      const double le64 = vdt_log(e);
-      const double range64 = dmax_(0.0, spline_log_xy(nL, d.lossGrid, d.loss + 5 * nL * imc, e, le64, d.lossLogMin,
-                                                      d.lossILD));
-      eloss = e - inv_range(d, imc, range64 - (double)p);
+    const float elossF = p * rest_dedx32(f, nL, imc, ef, lef);
+    double eloss = f2d(elossF);
+    if (lt(ld(&reg.linELossLimit) * ef, elossF)) {
+      const double range64 = rest_range64(d, f, imc, e, lef);
+      eloss = e - inv_range64(d, f, imc, range64 - f2d(p));
       // E(range - p) is ill-conditioned when p is close to the range: its
       // relative error is that of p times range / (range - p); keep <= 8x
       if (range - p < 0.125f * range) set_trip();
     }
-    eloss = dmax_(eloss, 0.0);
+    eloss = dpos(eloss);
     HEPEM_TR(1, 14, eloss);
-    if (eloss >= e) {  // only after the inversion, where p close to the range has tripped
+    if (!dless(eloss, e)) {  // only after the inversion, where p close to the range has tripped
       t.setE(0.0);
       t.edep = e;
       return t.isEl ? -1 : kQAnnihRest;
@@ -727,23 +862,25 @@ struct MixedEl {
     if (active && lt(fmx(1.0E-8f, 1.0e-16f * lambtr1), p)) {
       float pE = preEf, pLE = lef;
       if (lt(range * 0.01f, p)) {
-        pE = (float)postE;
+        pE = d2f(postE);
         pLE = logf(pE);
       }
-      const float postMFP = transport_mfp32(f, nL, c.mat, pE, pLE);
-      const double cost = cos_theta(p, preEf, lambtr1, pE, postMFP, tlimitMin, md, tsIsTlm);
-      HEPEM_TR(1, 21, cost);
+      const float postMFP = transport_mfp32(f, nL, cMat, pE, pLE);
+      const CosT ct = cos_theta(p, preEf, lambtr1, pE, postMFP, tlimitMin, md, tsIsTlm);
+      HEPEM_TR(1, 21, 1.0 - (double)ct.omc);
       // the reference skips the deflection when cos(theta) rounds to +-1 in
       // FP64: a computed value within a few ulp of that is undecidable here
-      if (!exactCos && 1.0 - fabs(cost) < 1.0E-15) set_trip();
-      if (fabs(cost) < 1.0) {
-        const double sth = sqrt((1.0 - cost) * (1.0 + cost));
+      const float mc = fmn(ct.omc, ct.opc);
+      if (!exactCos && mc < 1.0E-15f) set_trip();
+      if (mc > 0.f) {
+        const float sth = sqrtf(ct.omc * ct.opc);
+        const float cost = ct.omc < 1.f ? 1.f - ct.omc : ct.opc - 1.f;
         const double uphi = rng.flat();
-        const float phi = (float)k2Pi * (float)uphi;
+        const float phiN = 2.f * d2f(uphi);  // phi / pi
         float sp, cp;
-        sincosf(phi, &sp, &cp);
-        float dir[3] = {(float)sth * cp, (float)sth * sp, (float)cost};
-        const float tdir[3] = {(float)t.dir[0], (float)t.dir[1], (float)t.dir[2]};
+        sincospif(phiN, &sp, &cp);
+        float dir[3] = {sth * cp, sth * sp, cost};
+        const float tdir[3] = {d2f(t.dir[0]), d2f(t.dir[1]), d2f(t.dir[2])};
         float disp[3] = {0.f, 0.f, 0.f};
         bool dsp = displace && T.mscDisplacement;
         if (dsp && delta > 0.f) {
@@ -755,10 +892,11 @@ struct MixedEl {
           // -ln(1 - r0 (1 - e^-cbeta pi)) / cbeta, with 1 - r0 (1 - q) = (1 - r0) + r0 q:
           // no cancellation as r0 -> 1
           const float q = expf(-cbeta * (float)kPi);
-          const float psi = -logf((float)(1.0 - r0) + (float)r0 * q) / cbeta;
-          const float ph = lt((float)r1, 0.5f) ? phi + psi : phi - psi;
+          const float psi = -logf(one_minus_u(r0) + d2f(r0) * q) / cbeta;
+          const float psiN = psi * (float)(1.0 / kPi);
+          const float phN = lt(d2f(r1), 0.5f) ? phiN + psiN : phiN - psiN;
           float s2, c2;
-          sincosf(ph, &s2, &c2);
+          sincospif(phN, &s2, &c2);
           disp[0] = r * c2;
           disp[1] = r * s2;
           rotate_mixed(disp, tdir, t.dir);
@@ -766,31 +904,33 @@ struct MixedEl {
           dsp = false;
         }
         rotate_mixed(dir, tdir, t.dir);
-        // renormalise in FP64 so that repeated steps keep unit directions
-        const double nx = dir[0], ny = dir[1], nz = dir[2];
-        const double inv = 1.0 / sqrt(nx * nx + ny * ny + nz * nz);
-        t.dir[0] = nx * inv;
-        t.dir[1] = ny * inv;
-        t.dir[2] = nz * inv;
+        // renormalise (one Newton step on the reciprocal square root) so that
+        // repeated steps keep unit directions
+        const float n2 = dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2];
+        float inv = rsqrtf(n2);
+        inv = inv * (1.5f - 0.5f * n2 * inv * inv);
+        t.dir[0] = f2d(dir[0] * inv);
+        t.dir[1] = f2d(dir[1] * inv);
+        t.dir[2] = f2d(dir[2] * inv);
         if (dsp) {
-          t.msc.disp[0] = disp[0];
-          t.msc.disp[1] = disp[1];
-          t.msc.disp[2] = disp[2];
+          t.msc.disp[0] = f2d(disp[0]);
+          t.msc.disp[1] = f2d(disp[1]);
+          t.msc.disp[2] = f2d(disp[2]);
         }
       }
     }
     // energy loss fluctuations (G4HepEmElectronManager.icc:324-368)
     double finalE = postE;
-    if (ld(&T.regions[c.region].eLossFluct) && lt(1.E-5f, (float)eloss)) {
+    if (ld(&reg.eLossFluct) && lt(1.E-5f, d2f(eloss))) {
       const float tmax = t.isEl ? 0.5f * preEf : preEf;
-      const float tcut = fmn((float)c.elCut, tmax);
-      eloss = dmax_(fluct(tcut, (float)ld(&md.meanExc), (float)eloss), 0.0);
+      const float tcut = fmn(ld(&T.couples32[imc].elCut), tmax);
+      eloss = f2d(fmx(fluct(tcut, ld(&md.meanExc), d2f(eloss)), 0.f));
       finalE = preE - eloss;
       HEPEM_TR(1, 15, eloss);
       // the final energy inherits eloss's relative error times eloss / finalE
-      if (finalE < 0.125 * preE) set_trip();
+      if (d2f(finalE) < 0.125f * preEf) set_trip();
     }
-    if (le((float)finalE, (float)T.elTrackingCut)) {
+    if (le(d2f(finalE), T.elTrackingCut32)) {
       t.setE(0.0);
       t.edep = preE;
       return t.isEl ? -1 : kQAnnihRest;
@@ -800,15 +940,18 @@ struct MixedEl {
     // the delta-interaction test (G4HepEmElectronManager.icc:408-423)
     const int ip = t.winner;
     if (ip < 0 || t.onBoundary) return -1;
-    t.nia[ip] = -1.0;
-    const float fe = (float)finalE, lfe = logf(fe);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k == ip) t.nia[k] = -1.0;
+    const float fe = d2f(finalE), lfe = logf(fe);
     const float mxp = ip < 2 ? rest_macxs32(d, f, imc, finalE, fe, lfe, ip == 0)
-                   : (ip < 3 ? annih_macxs32(fe, (float)ld(&md.elDensity)) : nuc_macxs32(d, f, c.mat, finalE, fe, lfe));
+                   : (ip < 3 ? annih_macxs32(fe, ld(&md.elDensity)) : nuc_macxs32(d, f, cMat, finalE, fe, lfe));
     const double u = rng.flat();
-    if (mxp <= 0.f || !lt((float)u, mxp * mfp[ip])) return -1;
+    const float mfpw = ip == 0 ? mfp[0] : ip == 1 ? mfp[1] : ip == 2 ? mfp[2] : mfp[3];
+    if (mxp <= 0.f || !lt(d2f(u), mxp * mfpw)) return -1;
     switch (ip) {
       case 0: return t.isEl ? kQIoniEm : kQIoniEp;
-      case 1: near(fe, (float)T.bremModelLim); return finalE < T.bremModelLim ? kQBremSB : kQBremRB;
+      case 1: near(fe, T.bremModelLim32); return dless(finalE, T.bremModelLim) ? kQBremSB : kQBremRB;
       case 2: return kQAnnihFlight;
       default: return -1;
     }
@@ -849,18 +992,42 @@ struct MixedB {
   __device__ __forceinline__ const DevCouple& couple() const { return T.couples[t.imc]; }
 
   // modified-Tsai polar angle (G4HepEmInteractionUtils.icc:10-22); 1 - cos in FP32
+  // Near the backward limit u -> umax, 1 + cos = 2 (1 - u/umax)(1 + u/umax)
+  // carries u's relative error times umax / (umax - u): for u/umax > 0.9 the
+  // accepted u is recomputed in FP64, which gives the FP64 value of cos.
   __device__ double tsai_cost(double E) {
-    const float umax = 2.0f * (1.0f + (float)(E * kInvMec2));
+    const float umax = 2.0f * (1.0f + d2f(E) * (float)kInvMec2);
     float u;
+    double r01;
+    bool low;
     int it = 0;
     do {
       const double r0 = rng.flat(), r1 = rng.flat(), r2 = rng.flat();
-      const float uu = neg_log_u(r0 * r1);
-      u = 0.25 > r2 ? uu * 1.6f : uu * 0.533333333f;
+      r01 = r0 * r1;
+      low = dless(r2, 0.25);
+      const float uu = neg_log_u(r01);
+      u = low ? uu * 1.6f : uu * 0.533333333f;
       near(u, umax);
       if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
     } while (u > umax);
-    return 1.0 - (double)(2.0f * u * u / (umax * umax));
+    const float w = u / umax;
+    if (w > 0.9f) {
+      const double umax64 = 2.0 * (1.0 + E * kInvMec2);
+      const double u64 = -vdt_log(r01) * (low ? 1.6 : 0.533333333);
+      return 1.0 - 2.0 * u64 * u64 / (umax64 * umax64);
+    }
+    return 1.0 - (double)(2.0f * w * w);
+  }
+
+  // The secondaries of an e+- interaction are rotated to the frame of the
+  // track direction, whose azimuthal axes turn by (direction error) / sin(theta_z)
+  // close to the z axis: there the FP32-stepped direction (error ~3e-7) would
+  // not give the FP64 secondary directions to 1e-5, and the FP64 code takes the track.
+  bool dirExact;  // the track direction is an exact input (not stepped in FP32): no guard
+  __device__ __forceinline__ void frame_guard() {
+    if (dirExact) return;
+    const float x = d2f(t.dir[0]), y = d2f(t.dir[1]);
+    if (x * x + y * y < 0.01f) set_trip();
   }
 
   // the e+- target element of a brem model: the FP64 interpolation of the
@@ -896,6 +1063,7 @@ struct MixedB {
     const double tmaxE = t.isEl ? 0.5 * E : E;
     neard(tmaxE, cut);
     if (tmaxE <= cut) return;
+    frame_guard();
     const float Ef = (float)E;
     const float xmin = (float)(cut / E);
     float x, omx = 1.f;
@@ -957,7 +1125,7 @@ struct MixedB {
     const double ct = dmax_(-1.0, dmin_(cost, 1.0));
     const double st = sqrt((1.0 - ct) * (1.0 + ct));
     float sp, cp;
-    sincosf((float)k2Pi * (float)rng.flat(), &sp, &cp);
+    sincospif(2.f * d2f(rng.flat()), &sp, &cp);
     s.dir[0] = st * cp;
     s.dir[1] = st * sp;
     s.dir[2] = ct;
@@ -983,13 +1151,14 @@ struct MixedB {
     const double le = vdt_log(E);
     neard(E, couple().gamCut);
     if (E <= couple().gamCut) return;
+    frame_guard();
     omk = -1.0;
     const double k = sbModel ? sample_sb(E, le) : sample_rb(E, le);
     Sec& s = t.addSec(2);
     const double cost = tsai_cost(E);
     const double sint = sqrt((1.0 - cost) * (1.0 + cost));
     float sp, cp;
-    sincosf((float)k2Pi * (float)rng.flat(), &sp, &cp);
+    sincospif(2.f * d2f(rng.flat()), &sp, &cp);
     s.dir[0] = sint * cp;
     s.dir[1] = sint * sp;
     s.dir[2] = cost;
@@ -1220,6 +1389,7 @@ struct MixedB {
   // ---- annihilation in flight (G4HepEmPositronInteractionAnnihilation.icc) -----------
   // the FP64 model (it is cheap) with its rejection test guarded
   __device__ void annihilate_in_flight() {
+    frame_guard();
     const double E = t.e;
     Sec& g1 = t.addSec(2);
     Sec& g2 = t.addSec(2);
@@ -1377,7 +1547,7 @@ struct MixedB {
     Sec& se = t.addSec(0);
     Sec& sp = t.addSec(1);
     float sph, cph;
-    sincosf((float)k2Pi * (float)rng.flat(), &sph, &cph);
+    sincospif(2.f * d2f(rng.flat()), &sph, &cph);
     const double ce = tsai_cost(eK);
     const double st = sqrt((1.0 - ce) * (1.0 + ce));
     se.dir[0] = st * cph; se.dir[1] = st * sph; se.dir[2] = ce;
@@ -1431,7 +1601,7 @@ struct MixedB {
     const double cost = omc < 1.f ? 1.0 - (double)omc : (double)opc - 1.0;
     const double sint = sqrt((double)fmx(0.f, s2));
     float sp, cp;
-    sincosf((float)k2Pi * (float)rng.flat(), &sp, &cp);
+    sincospif(2.f * d2f(rng.flat()), &sp, &cp);
     t.dir[0] = sint * cp;
     t.dir[1] = sint * sp;
     t.dir[2] = cost;

@@ -448,10 +448,46 @@ StateImage build_state_image(const char* text, size_t len) {
     }
   }
 
+  // -- FP32 parameter copies (precision form)
+  T.elTrackingCut32 = (float)T.elTrackingCut;
+  T.gammaTrackingCut32 = (float)T.gammaTrackingCut;
+  T.minLossE32 = (float)T.minLossE;
+  T.bremModelLim32 = (float)T.bremModelLim;
+  std::vector<DevRegion32> regions32(regions.size());
+  for (size_t i = 0; i < regions.size(); ++i) {
+    const DevRegion& r = regions[i];
+    regions32[i] = DevRegion32{(float)r.finalRange, (float)r.dRoverRange, (float)r.linELossLimit,
+                               (float)r.mscRangeFactor, (float)r.mscSafetyFactor, r.mscMinimal, r.eLossFluct, 0};
+  }
+  std::vector<DevCouple32> couples32(couples.size());
+  for (size_t i = 0; i < couples.size(); ++i) {
+    const DevCouple& c = couples[i];
+    couples32[i] = DevCouple32{(float)c.elCut, (float)c.posCut, (float)c.gamCut, (float)c.logGamCut};
+  }
+  std::vector<DevMat32> mats32(mats.size());
+  for (size_t i = 0; i < mats.size(); ++i) {
+    const DevMat& m = mats[i];
+    DevMat32& f = mats32[i];
+    f = DevMat32{};
+    f.elDensity = (float)m.elDensity;
+    f.radLength = (float)m.radLength;
+    f.meanExc = (float)m.meanExc;
+    f.zeff = (float)m.zeff;
+    f.zeff23 = (float)m.zeff23;
+    f.zeffSqrt = (float)m.zeffSqrt;
+    f.umscPar = (float)m.umscPar;
+    for (int k = 0; k < 2; ++k) f.stepMin[k] = (float)m.stepMin[k];
+    for (int k = 0; k < 2; ++k) f.theta[k] = (float)m.theta[k];
+    for (int k = 0; k < 4; ++k) f.tail[k] = (float)m.tail[k];
+  }
+
   // -- pack the arena
   B.put(T.regions, regions);
   B.put(T.couples, couples);
   B.put(T.mats, mats);
+  B.put(T.regions32, regions32);
+  B.put(T.couples32, couples32);
+  B.put(T.mats32, mats32);
   B.put(T.elems, elems);
   B.put(T.matElemZ, matZ);
   B.put(T.matElemN, matN);

@@ -12,6 +12,12 @@ namespace hepem {
 struct StepCount {
   uint32_t steps, uniforms, overflow, secondaries, inter[8], fallback;
 };
+// inter[k] += 1 for k = w in [0, 8) (constant indices: the counters stay in registers)
+__device__ __forceinline__ void count_inter(StepCount& c, int w) {
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+    if (w == k) c.inter[k] += 1;
+}
 
 // Block-level sum of the step counters: warp reduce, then one atomic per block.
 // Every thread of the block must call it.

@@ -89,9 +89,26 @@ struct DevElData32 {
   const float* tr1;                 // [2*nLoss*nMats]
 };
 
+// FP32 copies of the per-region, per-couple and per-material parameters that
+// the precision form reads (rounded to nearest from the FP64 records)
+struct alignas(16) DevRegion32 {
+  float finalRange, dRoverRange, linELossLimit, mscRangeFactor, mscSafetyFactor;
+  int32_t mscMinimal, eLossFluct, pad;
+};
+
+struct alignas(16) DevCouple32 {
+  float elCut, posCut, gamCut, logGamCut;
+};
+
+struct alignas(16) DevMat32 {
+  float elDensity, radLength, meanExc, zeff, zeff23, zeffSqrt, umscPar, pad;
+  float stepMin[2], theta[2], tail[4];
+};
+
 struct DevTables {
   // G4HepEmParameters (G4HepEmParameters.hh:48-93)
   double elTrackingCut, gammaTrackingCut, minLossE, bremModelLim;
+  float elTrackingCut32, gammaTrackingCut32, minLossE32, bremModelLim32;
   int32_t mscPosCor, mscDisplacement;
   int32_t nCouples, nMats, nRegions, pad;
   const DevRegion* regions;
@@ -106,6 +123,9 @@ struct DevTables {
   DevSB sb;
   DevGamma gm;
   DevElData32 el32[2];              // FP32 copies (precision form)
+  const DevRegion32* regions32;
+  const DevCouple32* couples32;
+  const DevMat32* mats32;
 };
 
 }  // namespace hepem
