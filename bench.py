@@ -13,8 +13,9 @@ writes separate outputs, so every step does identical work; the inputs
 
 Prints one JSON line (rank 0).  `value` is device-resident throughput
 (steps/s over all ranks); `e2e` is the same metric through the host-buffer
-C-ABI entry point hepem_step_host with the host<->device copies inside the
-timed region.  `--impl reference` times the reference algorithm on the host
+C-ABI entry point hepem_step_host with the host<->device copies of the track
+state inside the timed region (the uniforms are drawn on the device from the
+same counter-based stream, n_uniform = 0).  `--impl reference` times the reference algorithm on the host
 cores: the CPU port of the oracle (the reference build itself cannot exist on
 the GPU host), all host threads, same workload and metric.
 """
@@ -649,7 +650,6 @@ def main():
     if not args.no_e2e:
         pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()  # noqa: E731
         h_in = {k: pin(v) for k, v in st_np.items()}
-        h_u = u.cpu().pin_memory()
         h_out = {k: torch.empty_like(v).pin_memory() for k, v in h_in.items()}
         h_res = {k: torch.from_numpy(v).pin_memory() for k, v in N.alloc_out_numpy(n).items()}
         ctx_steps = max(3, min(args.steps, 10))
@@ -661,7 +661,11 @@ def main():
         host_fn = N.lib().hepem_step_host_mixed if args.form == "mixed" else N.lib().hepem_step_host
 
         def host_step():
-            N.check(host_fn(ctx.h, n, C.byref(sin_h), C.byref(sout_h), h_u.data_ptr(), NU, SEED, C.byref(sres_h),
+            # n_uniform = 0: every uniform is drawn on the device from the
+            # counter-based stream (seed, track id, k) that fill_uniforms writes
+            # into the buffer of the device-resident runs: the same values, so the
+            # same results, without moving 8 * NU bytes per track over the link
+            N.check(host_fn(ctx.h, n, C.byref(sin_h), C.byref(sout_h), None, 0, SEED, C.byref(sres_h),
                             C.byref(hcnt), stream.cuda_stream))
         host_step()
         barrier()
@@ -673,7 +677,7 @@ def main():
             tt = torch.tensor([t_e2e], device="cuda")
             torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
             t_e2e = float(tt.item())
-        h2d = sum(v.numel() * v.element_size() for v in h_in.values()) + h_u.numel() * 8
+        h2d = sum(v.numel() * v.element_size() for v in h_in.values())
         d2h = sum(h_out[k].numel() * h_out[k].element_size() for k in N.STATE_OUT_FIELDS)
         d2h += sum(v.numel() * v.element_size() for v in h_res.values())
         link = host_link_gbs(torch)
@@ -684,7 +688,9 @@ def main():
                              "note": "e2e is bound by the host<->device copies: measured = concurrent pinned "
                                      "H2D + D2H copies of 2 GiB each (torch)"},
                "entry_point": ("hepem_step_host_mixed" if args.form == "mixed" else "hepem_step_host")
-               + " (pinned host buffers)"}
+               + " (pinned host buffers)",
+               "uniforms": "n_uniform = 0: drawn on the device from the same (seed, id, k) stream as the "
+                           "buffer of the device-resident runs (identical results), not copied"}
 
     if rank != 0:
         return

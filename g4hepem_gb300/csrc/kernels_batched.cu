@@ -209,28 +209,56 @@ __global__ void __launch_bounds__(1024) sort_scan_kernel(const Work w, int ncb, 
   }
 }
 
+// Scatter in tiles of 2048 tracks: ranks within the tile from shared-memory
+// counters (warp-aggregated), then one global atomic per key and tile reserves
+// the tile's range of each key.  (The order within a key is not fixed; no
+// result depends on it.)
+constexpr int kScatterItems = 8;
 __global__ void __launch_bounds__(256) sort_scatter_kernel(const __grid_constant__ DevTables T, int64_t n,
                                                            const int32_t* __restrict__ active,
                                                            const hepem_track_state in, const Work w, int ncb,
                                                            int neb) {
-  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t j = base + threadIdx.x;
-    const int64_t i = (active && j < n) ? (int64_t)active[j] : j;
-    int key = -1;
-    if (j < n) {
-      const int type = in.type[i];
-      const int imc = in.imc[i];
-      const double e = in.ekin[i];
-      if (!track_input_bad(T, type, imc, e)) key = sort_key(type, imc, e, ncb, neb);
+  extern __shared__ uint32_t sh[];
+  const int nkeys = 3 * ncb * neb;
+  const int lane = threadIdx.x & 31;
+  const int64_t tile = 256 * kScatterItems;
+  for (int64_t base = blockIdx.x * tile; base < n; base += (int64_t)gridDim.x * tile) {
+    for (int k = threadIdx.x; k < nkeys; k += 256) sh[k] = 0;
+    __syncthreads();
+    int key[kScatterItems];
+    uint32_t rank[kScatterItems];
+    int32_t idx[kScatterItems];
+#pragma unroll
+    for (int it = 0; it < kScatterItems; ++it) {
+      const int64_t j = base + it * 256 + threadIdx.x;
+      key[it] = -1;
+      idx[it] = 0;
+      if (j < n) {
+        const int64_t i = active ? (int64_t)active[j] : j;
+        idx[it] = (int32_t)i;
+        const int type = in.type[i];
+        const int imc = in.imc[i];
+        const double e = in.ekin[i];
+        if (!track_input_bad(T, type, imc, e)) key[it] = sort_key(type, imc, e, ncb, neb);
+      }
+      // warp-aggregated: one shared atomic per distinct key in the warp
+      const unsigned same = __match_any_sync(0xFFFFFFFFu, key[it]);
+      const int leader = __ffs(same) - 1;
+      uint32_t b = 0;
+      if (key[it] >= 0 && lane == leader) b = atomicAdd(&sh[key[it]], (uint32_t)__popc(same));
+      b = __shfl_sync(0xFFFFFFFFu, b, leader);
+      rank[it] = b + __popc(same & ((1u << lane) - 1u));
     }
-    // warp-aggregated: one atomic per distinct key in the warp
-    const unsigned same = __match_any_sync(0xFFFFFFFFu, key);
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(same) - 1;
-    uint32_t base2 = 0;
-    if (key >= 0 && lane == leader) base2 = atomicAdd(&w.cursor[key], (uint32_t)__popc(same));
-    base2 = __shfl_sync(0xFFFFFFFFu, base2, leader);
-    if (key >= 0) w.perm[base2 + __popc(same & ((1u << lane) - 1u))] = (int32_t)i;
+    __syncthreads();
+    for (int k = threadIdx.x; k < nkeys; k += 256) {
+      const uint32_t c = sh[k];
+      if (c) sh[k] = atomicAdd(&w.cursor[k], c);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < kScatterItems; ++it)
+      if (key[it] >= 0) w.perm[sh[key[it]] + rank[it]] = idx[it];
+    __syncthreads();
   }
 }
 
@@ -704,7 +732,9 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
   mark();
   sort_hist_kernel<<<gC, 256, nkeys * sizeof(uint32_t), s>>>(T, n, o.active, in, out, res, w, ncb, neb, counters);
   sort_scan_kernel<<<1, 1024, 0, s>>>(w, ncb, neb);
-  sort_scatter_kernel<<<gC, 256, 0, s>>>(T, n, o.active, in, w, ncb, neb);
+  const int64_t tiles = (n + 256 * kScatterItems - 1) / (256 * kScatterItems);
+  const int gS = (int)(tiles < (int64_t)sms * 8 ? tiles : (int64_t)sms * 8);
+  sort_scatter_kernel<<<gS, 256, nkeys * sizeof(uint32_t), s>>>(T, n, o.active, in, w, ncb, neb);
   mark();
   for (int q = 0; q < kNumStageKernels; ++q) {
     const int b = bs_index(cfg.block[q]);

@@ -170,7 +170,9 @@ def check(rc):
 
 
 def _ptr(x):
-    """Raw data pointer of a torch tensor or numpy array."""
+    """Raw data pointer of a torch tensor or numpy array (None: a null pointer)."""
+    if x is None:
+        return None
     if isinstance(x, np.ndarray):
         return x.ctypes.data
     return x.data_ptr()

@@ -147,6 +147,38 @@ def test_host_entry_point_equals_device_entry_point(native, gpu_ctx):
     assert cnt.steps == len(st["ekin"])
 
 
+@pytest.mark.parametrize("mixed", [False, True])
+def test_host_entry_point_without_buffer_draws_the_same_stream(native, gpu_ctx, mixed):
+    # n_uniform = 0: every uniform comes from the on-device counter-based
+    # stream, whose values the buffer holds in the device entry point: the
+    # results are the same bit for bit
+    import torch
+    st = W.mixed_batch(30000, seed=19)
+    ctx = gpu_ctx(T3)
+    n = len(st["ekin"])
+    sin = native.state_to_torch(st)
+    sout = native.empty_state_torch(n)
+    res = native.alloc_out_torch(n)
+    u = native.fill_uniforms(sin["id"], 64, 23)
+    ctx.step(sin, sout, u, 64, 23, res, form="mixed" if mixed else "batched")
+    torch.cuda.synchronize()
+    out_d, res_d = native.to_numpy(sout), native.to_numpy(res)
+    out_h = {k: np.empty_like(v) for k, v in st.items()}
+    res_h = native.alloc_out_numpy(n)
+    ctx.step_host(st, out_h, None, 0, 23, res_h, mixed=mixed)
+    for k in native.STATE_OUT_FIELDS:
+        assert np.array_equal(out_d[k], out_h[k], equal_nan=True), k
+    # bit 0 of flags records draws past the buffer: every draw, without one
+    assert np.array_equal(res_h["flags"] & 1, (out_d["rng_cursor"] > st["rng_cursor"]).astype(np.uint8))
+    res_h["flags"] &= 0xFE
+    res_d["flags"] &= 0xFE
+    ns = res_d["n_sec"].astype(int)
+    valid = (np.arange(2)[None, :] < ns[:, None]).reshape(-1)
+    for k in res_d:
+        a, b = (res_d[k][valid], res_h[k][valid]) if k.startswith("sec_") else (res_d[k], res_h[k])
+        assert np.array_equal(a, b, equal_nan=True), k
+
+
 def test_device_uniform_fill_matches_contract(native):
     torch = _torch()
     ids = torch.arange(0, 1000, dtype=torch.int32, device="cuda") * 7919
