@@ -369,10 +369,10 @@ struct MixedEl {
       float pv = expf(-mean);
       float ps = pv;
       // the cumulative carries the FP32 error of the mean (~1e-6 of mean times
-      // the largest Poisson probability) and of its sum: an absolute margin of
-      // 2e-5 covers both
+      // the largest Poisson probability, <= 2e-6) and of its sum (<= 2e-6): an
+      // absolute margin of 8e-6 covers both
       for (;;) {
-        if (fabsf(ps - position) <= 2.0e-5f) set_trip();
+        if (fabsf(ps - position) <= 8.0e-6f) set_trip();
         if (!(ps <= position)) break;
         ++number;
         pv *= mean / number;
@@ -822,9 +822,11 @@ struct MixedEl {
     if (!(gstep > 0.f)) return -1;
     float p = gstep;
     bool pAtRange = pIsRange && winner == -1;  // p == range
+    bool pIsStepFn = stepFn && winner == -1;   // p is the step-function value
     if (active) {
       p = trueStep;
       pAtRange = atRange;
+      pIsStepFn = pIsStepFn && tsIsP;
       if (le(p, 5.E-8f) || atRange) active = false;
     }
     t.pstep = f2d(p);
@@ -843,10 +845,21 @@ struct MixedEl {
     double eloss = f2d(elossF);
     if (lt(ld(&reg.linELossLimit) * ef, elossF)) {
       const double range64 = rest_range64(d, f, imc, e, lef);
-      eloss = e - inv_range64(d, f, imc, range64 - f2d(p));
-      // E(range - p) is ill-conditioned when p is close to the range: its
-      // relative error is that of p times range / (range - p); keep <= 8x
-      if (range - p < 0.125f * range) set_trip();
+      double rp;
+      if (pIsStepFn) {
+        // range - p of the step function, (1 - dR/R)(range - finalRange)^2 / range,
+        // in FP64 without the cancellation of range - p (range close to finalRange)
+        const DevRegion& r64 = T.regions[cRegion];
+        const double dF = range64 - ld(&r64.finalRange);
+        rp = (1.0 - ld(&r64.dRoverRange)) * dF * dF / range64;
+      } else {
+        rp = range64 - f2d(p);
+        // E(range - p) is ill-conditioned when p is close to the range: it
+        // inherits p's FP32 error (~3e-7) times 0.6 p / (range - p); keep that
+        // below ~5e-6 (range - p >= range / 25)
+        if (range - p < 0.04f * range) set_trip();
+      }
+      eloss = e - inv_range64(d, f, imc, rp);
     }
     eloss = dpos(eloss);
     HEPEM_TR(1, 14, eloss);
@@ -927,8 +940,9 @@ struct MixedEl {
       eloss = f2d(fmx(fluct(tcut, ld(&md.meanExc), d2f(eloss)), 0.f));
       finalE = preE - eloss;
       HEPEM_TR(1, 15, eloss);
-      // the final energy inherits eloss's relative error times eloss / finalE
-      if (d2f(finalE) < 0.125f * preEf) set_trip();
+      // the final energy inherits eloss's relative error (~3e-7) times
+      // eloss / finalE: keep that below ~4e-6
+      if (d2f(finalE) < 0.08f * preEf) set_trip();
     }
     if (le(d2f(finalE), T.elTrackingCut32)) {
       t.setE(0.0);
@@ -1021,13 +1035,14 @@ struct MixedB {
 
   // The secondaries of an e+- interaction are rotated to the frame of the
   // track direction, whose azimuthal axes turn by (direction error) / sin(theta_z)
-  // close to the z axis: there the FP32-stepped direction (error ~3e-7) would
-  // not give the FP64 secondary directions to 1e-5, and the FP64 code takes the track.
+  // close to the z axis: within sin(theta_z) < 0.063 the FP32-stepped direction
+  // (error ~3e-7) would not give the FP64 secondary directions to ~5e-6, and the
+  // FP64 code takes the track.
   bool dirExact;  // the track direction is an exact input (not stepped in FP32): no guard
   __device__ __forceinline__ void frame_guard() {
     if (dirExact) return;
     const float x = d2f(t.dir[0]), y = d2f(t.dir[1]);
-    if (x * x + y * y < 0.01f) set_trip();
+    if (x * x + y * y < 0.004f) set_trip();
   }
 
   // the e+- target element of a brem model: the FP64 interpolation of the
