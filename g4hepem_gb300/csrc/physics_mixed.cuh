@@ -140,6 +140,19 @@ __device__ __forceinline__ float spline_log_3_32(int nd, const float* d, float x
   const int i = 3 * bin32(lx, lxm, ild, nd);
   return spline32(ld(d + i), ld(d + i + 3), ld(d + i + 1), ld(d + i + 4), ld(d + i + 2), ld(d + i + 5), xv);
 }
+// The same over (x, y, y'') triplets with the offset x - x1 taken in FP64
+// (d64: the FP64 table).  The restricted cross sections start from zero at a
+// threshold knot: just above it y ~ (x - x1), and the FP32 rounding of x
+// (~6e-8 x) would be a relative error ~6e-8 x / (x - x1) of the cross section.
+__device__ __forceinline__ float spline_log_3_32x(int nd, const float* d, const double* d64, double x, float lx,
+                                                  float lxm, float ild) {
+  const int i = 3 * bin32(lx, lxm, ild, nd);
+  const double x1 = ld(d64 + i), x2 = ld(d64 + i + 3);
+  const float dl = d2f(x2 - x1);
+  const float b = fmx(0.f, fmn(1.f, d2f(x - x1) / dl));
+  const float s1 = ld(d + i + 2), s2 = ld(d + i + 5), y1 = ld(d + i + 1), y2 = ld(d + i + 4);
+  return y1 + b * (y2 - y1) + (b * (b - 1.0f)) * ((2.0f - b) * s1 + (1.0f + b) * s2) * (dl * dl * 0.16666667f);
+}
 __device__ __forceinline__ int lower_bin32(const float* xd, int num, float x, int step) {
   int ml = -1, mu = num - 1;
   while (abs(mu - ml) > 1) {
@@ -216,7 +229,7 @@ __device__ __forceinline__ float rest_macxs32(const DevElData& d, const DevElDat
   const int st = ioni ? i0 : i0 + 3 * (int)ld(f.xs + i0) + 5;
   const int nd = (int)ld(f.xs + st);
   if (dless(e, ld(d.xs + st + 5))) return 0.f;
-  return fmx(0.f, spline_log_3_32(nd, f.xs + st + 5, ef, le, ld(f.xs + st + 3), ld(f.xs + st + 4)));
+  return fmx(0.f, spline_log_3_32x(nd, f.xs + st + 5, d.xs + st + 5, e, le, ld(f.xs + st + 3), ld(f.xs + st + 4)));
 }
 // the cross section for stepping, max over [0.8 e, e]: continuous in e at
 // both switches (e at the energy of the maximum, 0.8 e at it), so they are
@@ -234,10 +247,10 @@ __device__ __forceinline__ float rest_macxs_stepping32(const DevElData& d, const
     ee = er;
     le += -0.22314355f;  // log(0.8)
     if (ee < ld(f.xs + st + 5)) return 0.f;
-  } else if (dless(e, ld(d.xs + st + 5))) {
-    return 0.f;
+    return fmx(0.f, spline_log_3_32(nd, f.xs + st + 5, ee, le, ld(f.xs + st + 3), ld(f.xs + st + 4)));
   }
-  return fmx(0.f, spline_log_3_32(nd, f.xs + st + 5, ee, le, ld(f.xs + st + 3), ld(f.xs + st + 4)));
+  if (dless(e, ld(d.xs + st + 5))) return 0.f;
+  return fmx(0.f, spline_log_3_32x(nd, f.xs + st + 5, d.xs + st + 5, e, le, ld(f.xs + st + 3), ld(f.xs + st + 4)));
 }
 __device__ __forceinline__ float nuc_macxs32(const DevElData& d, const DevElData32& f, int imat, double e, float ef,
                                              float le) {
@@ -941,8 +954,8 @@ struct MixedEl {
       finalE = preE - eloss;
       HEPEM_TR(1, 15, eloss);
       // the final energy inherits eloss's relative error (~3e-7) times
-      // eloss / finalE: keep that below ~4e-6
-      if (d2f(finalE) < 0.08f * preEf) set_trip();
+      // eloss / finalE: keep that below ~3e-6
+      if (d2f(finalE) < 0.1f * preEf) set_trip();
     }
     if (le(d2f(finalE), T.elTrackingCut32)) {
       t.setE(0.0);
