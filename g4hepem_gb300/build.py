@@ -22,7 +22,9 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 # (source, extra nvcc flags)
 UNITS = [
     ("kernels_fp64.cu", ["-fmad=false"]),
-    ("kernels_batched.cu", ["-fmad=false"]),
+    # single-precision division and square root to ~2 ulp (the precision form's
+    # FP32 stages; FP64 arithmetic is not affected by these two flags)
+    ("kernels_batched.cu", ["-fmad=false", "-prec-div=false", "-prec-sqrt=false"]),
     ("api.cu", ["-fmad=false"]),
     ("noalloc.cu", []),
     ("server.cu", ["-fmad=false"]),
