@@ -296,6 +296,12 @@ int hepem_step_mixed(const hepem_ctx* c, int64_t n, const hepem_track_state* in,
   return step_batched(c, n, in, out, uniforms, nu, seed, res, counters, stream, true);
 }
 
+// chunks of a host-buffer step: more overlap of the copies against smaller,
+// less efficient device steps
+#ifndef HEPEM_HOST_CHUNKS
+#define HEPEM_HOST_CHUNKS 8
+#endif
+
 namespace {
 int step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem_track_state* out,
               const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res, hepem_step_counters* counters,
@@ -311,7 +317,8 @@ int step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem
   // The batch is cut into chunks that cycle over kSlots streams, each with its
   // own device buffers: the copy-in of one chunk, the step of the previous one
   // and the copy-out of the one before overlap.
-  const int64_t m = std::min<int64_t>(n, std::max<int64_t>(1 << 16, ((n + 7) / 8 + 255) / 256 * 256));
+  const int64_t m = std::min<int64_t>(
+      n, std::max<int64_t>(1 << 16, ((n + HEPEM_HOST_CHUNKS - 1) / HEPEM_HOST_CHUNKS + 255) / 256 * 256));
   const int nChunks = (int)((n + m - 1) / m);
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
   size_t need = 0;
