@@ -290,8 +290,10 @@ enum { kStageFp64 = 0, kStageMixed = 1 };
 
 // fallback list of the precision form: queue[kNumQueues] with its kinds and
 // the count in counts[kFbCount].  Kind 0: the e+- stage A tripped (the track
-// was not stored); kind 1 + Q: interaction model Q tripped.
+// was not stored); kind 1 + Q: interaction model Q tripped; kind kFbGammaA:
+// the gamma stage A tripped (the track was not stored).
 constexpr int kFbCount = 3 + kNumQueues;
+constexpr uint8_t kFbGammaA = 1 + kNumQueues;
 
 // warp-aggregated append to the fallback list; all 32 lanes call it
 __device__ __forceinline__ void fb_push(bool trip, int32_t idx, uint8_t kind, const Work& w) {
@@ -369,7 +371,9 @@ __global__ void __launch_bounds__(BS, MODE == kStageMixed ? HEPEM_MIXED_A_WARPS 
   add_counters(cnt, counters);
 }
 
-template <int BS>
+// MODE kStageMixed: HowFar and the interaction choice from the FP32 table
+// (MixedG); a tripped gamma is not stored but goes to the fallback list.
+template <int BS, int MODE>
 __global__ void __launch_bounds__(BS) stage_a_gamma_kernel(const __grid_constant__ DevTables T,
                                                             const hepem_track_state in, const hepem_track_state out,
                                                             const double* __restrict__ uniforms, int nu,
@@ -382,35 +386,50 @@ __global__ void __launch_bounds__(BS) stage_a_gamma_kernel(const __grid_constant
     int key = -1;
     int32_t idx = 0;
     double pe = 0.0;
+    bool tripped = false;
     if (j < total) {
       idx = w.perm[w.counts[0] + w.counts[1] + j];
       Track t;
       Rng rng;
       load_track(in, idx, t, rng, uniforms, nu, key_of(w, idx, seed), 2);
       const int32_t c0 = rng.cursor;
-      Physics P{T, rng, t};
       t.isEl = false;
-      P.gamma_howfar();
-      if (t.onBoundary) {
-        t.nia[0] -= t.gstep / t.mfp[0];
+      if (MODE == kStageMixed) {
+        MixedG G{T, rng, t, false};
+        key = G.stage_a();
+        tripped = G.trip;
+        if (tripped) {
+          HEPEM_COUNT_TRIP(G.tripLine);
+          key = -1;
+        }
       } else {
-        P.gamma_select();
-        key = P.gamma_perform_until_interaction();
+        Physics P{T, rng, t};
+        P.gamma_howfar();
+        if (t.onBoundary) {
+          t.nia[0] -= t.gstep / t.mfp[0];
+        } else {
+          P.gamma_select();
+          key = P.gamma_perform_until_interaction();
+        }
+        t.pstep = t.gstep;
+      }
+      if (!tripped) {
         if (key == -2) {
+          Physics P{T, rng, t};
           P.gamma_tracking_cut();
           key = -1;
         }
+        pe = t.peXS;
+        store_track(in, out, res, idx, t, rng, 2, false);
+        res.n_sec[idx] = 0;
+        cnt.steps += 1;
+        cnt.uniforms += (uint32_t)(rng.cursor - c0);
+        cnt.overflow += rng.overflow;
+        if (t.winner >= 0 && t.winner < 4) count_inter(cnt, 4 + t.winner);
       }
-      t.pstep = t.gstep;
-      pe = t.peXS;
-      store_track(in, out, res, idx, t, rng, 2, false);
-      res.n_sec[idx] = 0;
-      cnt.steps += 1;
-      cnt.uniforms += (uint32_t)(rng.cursor - c0);
-      cnt.overflow += rng.overflow;
-      if (t.winner >= 0 && t.winner < 4) count_inter(cnt, 4 + t.winner);
     }
     warp_push(key, idx, w.queue, w.counts + 3, pe, w.peXS, kQPhotoelectric);
+    if (MODE == kStageMixed) fb_push(tripped, idx, kFbGammaA, w);
   }
   add_counters(cnt, counters);
 }
@@ -578,6 +597,41 @@ __device__ void charged_full_step(const DevTables& T, const hepem_track_state& i
   cnt.fallback += 1;
 }
 
+// the FP64 step of a gamma whose FP32 stage A tripped: stage A as
+// stage_a_gamma_kernel (MODE kStageFp64) and its interaction as stage_b_one,
+// in one thread from the unchanged input state
+__device__ void gamma_full_step(const DevTables& T, const hepem_track_state& in, const hepem_track_state& out,
+                                const double* uniforms, int nu, uint64_t seed, const hepem_step_out& res,
+                                const Work& w, int32_t i, StepCount& cnt) {
+  Track t;
+  Rng rng;
+  load_track(in, i, t, rng, uniforms, nu, key_of(w, i, seed), 2);
+  const int32_t c0 = rng.cursor;
+  t.isEl = false;
+  Physics P{T, rng, t};
+  P.gamma_howfar();
+  int key = -1;
+  if (t.onBoundary) {
+    t.nia[0] -= t.gstep / t.mfp[0];
+  } else {
+    P.gamma_select();
+    key = P.gamma_perform_until_interaction();
+  }
+  t.pstep = t.gstep;
+  if (key == kQConversion) P.conversion();
+  if (key == kQCompton) P.compton();
+  if (key == kQPhotoelectric) P.photoelectric();
+  if (key != -1) P.gamma_tracking_cut();
+  store_track(in, out, res, i, t, rng, 2, false);
+  store_secondaries(res, i, t, 0);
+  cnt.steps += 1;
+  cnt.uniforms += (uint32_t)(rng.cursor - c0);
+  cnt.overflow += rng.overflow;
+  if (t.winner >= 0 && t.winner < 4) count_inter(cnt, 4 + t.winner);
+  cnt.secondaries += (uint32_t)(t.nsec > 2 ? 2 : t.nsec);
+  cnt.fallback += 1;
+}
+
 template <int BS>
 __global__ void __launch_bounds__(BS) final_fallback_kernel(const __grid_constant__ DevTables T,
                                                              const hepem_track_state in, const hepem_track_state out,
@@ -589,7 +643,9 @@ __global__ void __launch_bounds__(BS) final_fallback_kernel(const __grid_constan
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < total; j += (int64_t)gridDim.x * blockDim.x) {
     const int32_t i = w.queue[kNumQueues][j];
     const int kind = w.fbKind[j];
-    if (kind == 0 || charged_model(kind - 1)) {
+    if (kind == kFbGammaA) {
+      gamma_full_step(T, in, out, uniforms, nu, seed, res, w, i, cnt);
+    } else if (kind == 0 || charged_model(kind - 1)) {
       charged_full_step(T, in, out, uniforms, nu, seed, res, w, i, kind == 0, cnt);
     } else {
       if (kind - 1 == kQConversion)
@@ -615,7 +671,7 @@ static int bs_index(int bs) { return bs == 128 ? 0 : (bs == 512 ? 2 : 1); }
 template <int BS>
 static void stage_table(StageFn* f) {
   f[0] = stage_a_charged_kernel<BS, kStageFp64>;
-  f[1] = stage_a_gamma_kernel<BS>;
+  f[1] = stage_a_gamma_kernel<BS, kStageFp64>;
   f[2] = stage_b_kernel<0, BS, kStageFp64>;
   f[3] = stage_b_kernel<1, BS, kStageFp64>;
   f[4] = stage_b_kernel<2, BS, kStageFp64>;
@@ -632,6 +688,7 @@ template <int BS>
 static void mixed_table(StageFn* m) {
   for (int k = 0; k < kNumStageKernels; ++k) m[k] = nullptr;
   m[0] = stage_a_charged_kernel<BS, kStageMixed>;
+  m[1] = stage_a_gamma_kernel<BS, kStageMixed>;
   m[2 + kQIoniEm] = stage_b_kernel<kQIoniEm, BS, kStageMixed>;
   m[2 + kQIoniEp] = stage_b_kernel<kQIoniEp, BS, kStageMixed>;
   m[2 + kQBremSB] = stage_b_kernel<kQBremSB, BS, kStageMixed>;

@@ -985,6 +985,158 @@ struct MixedEl {
   }
 };
 
+// ---- the gamma stage A in FP32 ---------------------------------------------------------
+// G4HepEmGammaManager HowFar + SelectInteraction (G4HepEmGammaManager.icc:27-130;
+// Physics::gamma_howfar / gamma_select): the total macroscopic cross section,
+// the step and the interaction choice from the FP32 table copy.  The energy
+// windows of the table are chosen exactly (the cross section is discontinuous
+// between them), the interaction choice is guarded as in MixedEl, and the
+// photoelectric cross section that the photoelectric model's element selection
+// uses is evaluated in FP64 for the tracks that pick it.
+
+// spline over a row of 9 of the gamma window-2 table (G4HepEmRunUtils.icc)
+__device__ __forceinline__ float spline_log_9_32(int nd, const float* d, float x, float lx, float lxm, float ild,
+                                                 int iwhich) {
+  const int i0 = 9 * bin32(lx, lxm, ild, nd);
+  const int i1 = i0 + 9;
+  const int w = (iwhich - 1) * 2 + 1;
+  return spline32(ld(d + i0), ld(d + i1), ld(d + i0 + w), ld(d + i1 + w), ld(d + i0 + w + 1), ld(d + i1 + w + 1), x);
+}
+
+// FP64 photoelectric cross section of the window of e, as Physics::gamma_total_xs
+// and Physics::gamma_select leave it in Track::peXS (out of line: rare)
+static __device__ __noinline__ double gamma_pe_xs64(const DevTables& T, int imat, double e) {
+  const DevGamma& g = T.gm;
+  const double le = vdt_log(e);
+  if (e > g.eMax1) {
+    const int st = imat * g.dataPerMat + g.nData0 + g.nData1;
+    return spline_log_9(g.nE2, g.mx + st, e, le, g.logEMin2, g.ild2, 4);
+  }
+  if (e > g.eMax0) {
+    const double* d = g.mx + imat * g.dataPerMat + g.nData0;
+    const int i3 = 3 * bin_of(le, g.logEMin1, g.ild1, g.nE1);
+    const int j3 = i3 + 3;
+    const double x0 = ld(d + i3);
+    const double dl = ld(d + j3) - x0;
+    const double b = dmax_(0., dmin_(1., (e - x0) / dl));
+    return dmax_(0.0, ld(d + i3 + 2) + b * (ld(d + j3 + 2) - ld(d + i3 + 2)));
+  }
+  const DevMat& m = T.mats[imat];
+  const int n = ld(&m.nSandia), off = ld(&m.sandiaOff);
+  int iv = 0;
+  if (e >= ld(T.sandiaE + off)) {
+    for (int i = n - 1; i >= 0; --i)
+      if (e >= ld(T.sandiaE + off + i)) { iv = i; break; }
+  }
+  const double* c = T.sandiaC + 4 * (off + iv);
+  const double inv = 1 / e;
+  return dmax_(0.0, inv * (ld(c) + inv * (ld(c + 1) + inv * (ld(c + 2) + inv * ld(c + 3)))));
+}
+
+struct MixedG {
+  const DevTables& T;
+  Rng& rng;
+  Track& t;
+  bool trip;
+  int tripLine;
+
+  __device__ __forceinline__ void set_trip(int line = __builtin_LINE()) {
+    if (!trip) tripLine = line;
+    trip = true;
+  }
+  __device__ __forceinline__ void near(float a, float b, int line = __builtin_LINE()) {
+    if (fabsf(a - b) <= kGuardTol * fmx(fabsf(a), fabsf(b))) set_trip(line);
+  }
+
+  // Sandia photoabsorption cross section (Physics::macxs_pe) in FP32; the
+  // interval is found with exact comparisons
+  __device__ float macxs_pe32(int imat, double e, float ef) {
+    const DevMat& m = T.mats[imat];
+    const int n = ld(&m.nSandia), off = ld(&m.sandiaOff);
+    int iv = 0;
+    if (!dless(e, ld(T.sandiaE + off))) {
+      for (int i = n - 1; i >= 0; --i)
+        if (!dless(e, ld(T.sandiaE + off + i))) { iv = i; break; }
+    }
+    const double* c = T.sandiaC + 4 * (off + iv);
+    const float inv = 1.f / ef;
+    return inv * (d2f(ld(c)) + inv * (d2f(ld(c + 1)) + inv * (d2f(ld(c + 2)) + inv * d2f(ld(c + 3)))));
+  }
+
+  // HowFar + SelectInteraction + the first part of Perform, as the FP64 stage
+  // (stage_a_gamma_kernel): returns the interaction queue, -1 (no interaction
+  // or on a boundary) or -2 (no interaction: tracking cut); valid if !trip
+  __device__ int stage_a() {
+    const DevGamma& g = T.gm;
+    const DevGamma32& h = T.gm32;
+    if (nonpositive(t.nia[0])) t.nia[0] = f2d(neg_log_u(rng.flat()));
+    const double e = t.e;
+    const float ef = d2f(e), lef = logf(ef);
+    const int imat = ld(&T.couples[t.imc].mat);
+    const bool w2 = dless(g.eMax1, e), w1 = !w2 && dless(g.eMax0, e);
+    float tot, pe = 0.f;
+    int st2 = 0;
+    if (w2) {
+      st2 = imat * g.dataPerMat + g.nData0 + g.nData1;
+      tot = spline_log_9_32(g.nE2, h.mx + st2, ef, lef, h.logEMin2, h.ild2, 1);
+    } else if (w1) {
+      const float* d = h.mx + imat * g.dataPerMat + g.nData0;
+      const int i3 = 3 * bin32(lef, h.logEMin1, h.ild1, g.nE1);
+      const int j3 = i3 + 3;
+      const float x0 = ld(d + i3);
+      const float b = fmx(0.f, fmn(1.f, (ef - x0) / (ld(d + j3) - x0)));
+      tot = fmx(0.f, ld(d + i3 + 1) + b * (ld(d + j3 + 1) - ld(d + i3 + 1)));
+      pe = fmx(0.f, ld(d + i3 + 2) + b * (ld(d + j3 + 2) - ld(d + i3 + 2)));
+    } else {
+      const float* d = h.mx + imat * g.dataPerMat;
+      const int i2 = 2 * bin32(lef, h.logEMin0, h.ild0, g.nE0);
+      const float x1 = ld(d + i2);
+      const float b = fmx(0.f, fmn(1.f, (ef - x1) / (ld(d + i2 + 2) - x1)));
+      const float y1 = ld(d + i2 + 1);
+      pe = fmx(0.f, macxs_pe32(imat, e, ef));
+      tot = y1 + b * (ld(d + i2 + 3) - y1) + pe;
+    }
+    const float mfp = tot > 0.f ? 1.f / tot : kLargeF;
+    const float nia0 = d2f(t.nia[0]);
+    const float gstep = mfp * nia0;
+    t.mfp[0] = f2d(mfp);
+    t.gstep = f2d(gstep);
+    t.pstep = t.gstep;
+    t.edep = 0.0;
+    if (t.onBoundary) {
+      t.nia[0] = f2d(nia0 - gstep / mfp);
+      return -1;
+    }
+    // SelectInteraction
+    const float u = d2f(rng.flat());
+    int winner;
+    if (w2) {
+      float cp = 0.f;
+      int pid = 2;
+      do {
+        const float mx = pid < 5 ? spline_log_9_32(g.nE2, h.mx + st2, ef, lef, h.logEMin2, h.ild2, pid) : 0.f;
+        cp += mx * mfp;
+        near(u, cp);
+        ++pid;
+      } while (pid < 6 && u > cp);
+      winner = pid - 3;
+    } else {
+      near(u, mfp * pe);
+      winner = u > mfp * pe ? 1 : 2;
+    }
+    t.winner = winner;
+    t.peXS = winner == 2 ? gamma_pe_xs64(T, imat, e) : 0.0;
+    // Perform up to the interaction: nia -= gstep / mfp after SelectInteraction set it to -1
+    t.nia[0] = winner == 0 ? -1.0 : f2d(-1.f - gstep / mfp);
+    switch (winner) {
+      case 0: return kQConversion;
+      case 1: return kQCompton;
+      case 2: return kQPhotoelectric;
+      default: return -2;
+    }
+  }
+};
+
 // ---- stage B of the precision form: the costly interaction models ---------------------
 // Bethe-Heitler pair production, Seltzer-Berger and relativistic brem, the
 // modified-Tsai angles, Moller/Bhabha and Klein-Nishina Compton with their

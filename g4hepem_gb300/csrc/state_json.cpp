@@ -526,6 +526,13 @@ StateImage build_state_image(const char* text, size_t len) {
   B.put(T.sb.startPerZ, spz);
   B.put(T.sb.data, sbd);
   B.put(G.mx, mx);
+  T.gm32.logEMin0 = (float)G.logEMin0;
+  T.gm32.ild0 = (float)G.ild0;
+  T.gm32.logEMin1 = (float)G.logEMin1;
+  T.gm32.ild1 = (float)G.ild1;
+  T.gm32.logEMin2 = (float)G.logEMin2;
+  T.gm32.ild2 = (float)G.ild2;
+  B.put32(T.gm32.mx, mx);
   B.put(G.convStart, convStart);
   B.put(G.convGrid, convGrid);
   B.put(G.conv, conv);

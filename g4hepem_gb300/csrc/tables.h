@@ -89,6 +89,13 @@ struct DevElData32 {
   const float* tr1;                 // [2*nLoss*nMats]
 };
 
+// FP32 copy of the gamma macroscopic cross-section table (same layout as
+// DevGamma::mx) with its binning constants
+struct DevGamma32 {
+  float logEMin0, ild0, logEMin1, ild1, logEMin2, ild2;
+  const float* mx;
+};
+
 // FP32 copies of the per-region, per-couple and per-material parameters that
 // the precision form reads (rounded to nearest from the FP64 records)
 struct alignas(16) DevRegion32 {
@@ -126,6 +133,7 @@ struct DevTables {
   const DevRegion32* regions32;
   const DevCouple32* couples32;
   const DevMat32* mats32;
+  DevGamma32 gm32;
 };
 
 }  // namespace hepem

@@ -203,9 +203,11 @@ int  hepem_step_batched_noalloc(const hepem_ctx* ctx, int64_t n, const hepem_tra
 
 /* Precision form of hepem_step_batched: the e+- HowFar and continuous step
  * (step limits, MSC, energy loss and its fluctuations, the delta-interaction
- * test) run from FP32 copies of the tables in FP32 arithmetic; FP64 is kept
- * for the range->energy inversion of the mean loss, the energy and deposit
- * bookkeeping and decisions on exact inputs.  Every discrete decision taken
+ * test), the gamma HowFar and interaction choice, and the interaction models
+ * but the photoelectric effect and annihilation at rest run from FP32 copies
+ * of the tables in FP32 arithmetic; FP64 is kept for the range->energy
+ * inversion of the mean loss, the energy and deposit bookkeeping and
+ * decisions on exact inputs.  Every discrete decision taken
  * on FP32 values is guarded: a track whose FP32 operands of any decision are
  * closer than 2^-12 relative is re-stepped by the FP64 code
  * (counters->fp64_fallback), so discrete outcomes (interaction, rejection

@@ -84,6 +84,7 @@ def compare(st, ref, mix):
     ref_round = 2.2e-16 * r64["pstep"] ** 2 / dz ** 2
     check("disp", dd / np.maximum(np.maximum(dnorm, 1e-3 * r64["pstep"]), 1e-300) / (1.0 + ref_round / TOL))
     check("nia", np.max([rel_err(s32[k], s64[k], 1.0) for k in ("nia0", "nia1", "nia2", "nia3")], axis=0), charged)
+    check("nia_gamma", rel_err(s32["nia0"], s64["nia0"], 1.0), ~charged)
     check("gauss_value", np.abs(s32["gauss_value"] - s64["gauss_value"]), s64["gauss_valid"] == 1)
     check("sec_ekin", rel_err(r32["sec_ekin"], r64["sec_ekin"]), valid)
     check("sec_dir", np.max([np.abs(r32[k] - r64[k]) for k in ("sec_dir_x", "sec_dir_y", "sec_dir_z")], axis=0),
