@@ -313,10 +313,13 @@ def c4_serving(torch, N, args):
     closed loop with 512 requests in flight; then open-loop Poisson arrivals at
     25/50/90% of that peak request rate.  Reported per level: steps/s, p50/p99 request
     latency (submit to result) and p50/p99 batch latency (one server
-    iteration: one batched step over every resident track)."""
+    iteration: one batched step over every resident track).  The server steps
+    in the form of the headline (--form: the precision form by default)."""
     from g4hepem_gb300 import workload as W
     ctx = N.Context(TABLE)
-    srv = N.Server(ctx, memory_budget_bytes=16 << 30, max_steps=1000, max_requests=4096, min_energy=1.0e-3)
+    # the server steps in the bench's form (precision form by default)
+    srv = N.Server(ctx, memory_budget_bytes=16 << 30, max_steps=1000, max_requests=4096, min_energy=1.0e-3,
+                   mixed=args.form == "mixed")
     rng = np.random.Generator(np.random.Philox(41))
     sizes = np.clip(np.round(2000.0 * np.exp(1.5 * rng.standard_normal(256))), 1, 500000).astype(np.int64)
     events = [W.mixed_batch(int(m), seed=1000 + k) for k, m in enumerate(sizes)]
@@ -394,7 +397,8 @@ def c4_serving(torch, N, args):
     return {"workload": "event stream: requests log-normal (median 2k tracks, sigma 1.5, clipped [1, 500k]), "
                         "configuration-2 mix, 16 GB admission budget, resident until < 1 keV or 1000 steps",
             "capacity_tracks": cap, "event_pool": len(events), "event_size_median": int(np.median(sizes)),
-            "event_size_max": int(sizes.max()), "peak": peak, "poisson": levels}
+            "event_size_max": int(sizes.max()), "peak": peak, "poisson": levels,
+            "form": "precision (hepem_server_config.precision = 1)" if args.form == "mixed" else "FP64 batched"}
 
 
 def c5_precision(torch, N, args, n_tracks=1 << 24):
