@@ -649,7 +649,14 @@ __global__ void __launch_bounds__(BS) final_fallback_kernel(const __grid_constan
                                                              hepem_step_counters* counters) {
   const int64_t total = w.counts[kFbCount];
   StepCount cnt = {};
-  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < total; j += (int64_t)gridDim.x * blockDim.x) {
+  // every block takes an equal contiguous share of the list: the few (~1% of
+  // the tracks), long FP64 steps spread over every SM's FP64 pipe instead of
+  // filling the first blocks, and a share holds mostly one kind (the list is
+  // appended kernel by kernel)
+  const int64_t per = (total + gridDim.x - 1) / gridDim.x;
+  const int64_t j0 = (int64_t)blockIdx.x * per;
+  const int64_t j1 = j0 + per < total ? j0 + per : total;
+  for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
     const int32_t i = w.queue[kNumQueues][j];
     const int kind = w.fbKind[j];
     if (kind == kFbGammaA) {
