@@ -734,7 +734,10 @@ def main():
             "frac": achieved / hbm, "traffic": traffic,
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_src == "measured" else "fallback",
             "algorithmic_bytes_per_launch": alg, "ms_per_launch": ms_dom,
-            "note": "HBM is not the limit of this kernel: see roofline_fp64 / roofline_fp32 and profiles/"}
+            "note": ("HBM is not the limit of this kernel: the precision form's stage A is bound by the latency "
+                     "of dependent table and state gathers (profiles/stage_a_charged_mixed_c2_2M.md); traffic is "
+                     "the ncu DRAM bytes per e+- track x the e+- tracks of the step" if args.form == "mixed" else
+                     "HBM is not the limit of this kernel: the FP64 pipe is (roofline_fp64, profiles/)")}
     fp64 = {"bound": "fp64", "kernel": dom, "unit": "TFLOP/s", "peak": None,
             "peak_source": "measured here: cuBLAS DGEMM 4096^3 (MEASURED_PEAKS.json has no FP64 figure)"}
     fp32 = {"bound": "fp32", "kernel": dom, "unit": "TFLOP/s", "peak": None,
