@@ -1170,11 +1170,11 @@ struct MixedB {
   __device__ __forceinline__ const DevElData& eld() const { return t.isEl ? T.el[0] : T.el[1]; }
   __device__ __forceinline__ const DevCouple& couple() const { return T.couples[t.imc]; }
 
-  // modified-Tsai polar angle (G4HepEmInteractionUtils.icc:10-22); 1 - cos in FP32
-  // Near the backward limit u -> umax, 1 + cos = 2 (1 - u/umax)(1 + u/umax)
-  // carries u's relative error times umax / (umax - u): for u/umax > 0.9 the
-  // accepted u is recomputed in FP64, which gives the FP64 value of cos.
-  __device__ double tsai_cost(double E) {
+  // modified-Tsai polar angle (G4HepEmInteractionUtils.icc:10-22) as the pair
+  // 1 - cos = 2 w^2, 1 + cos = 2 (1 - w)(1 + w), w = u / umax, in FP32.  Near the
+  // backward limit w -> 1, 1 + cos carries u's relative error times 1 / (1 - w):
+  // for w > 0.9 the accepted u is recomputed in FP64.
+  __device__ void tsai_pair(double E, float& omc, float& opc) {
     const float umax = 2.0f * (1.0f + d2f(E) * (float)kInvMec2);
     float u;
     double r01;
@@ -1192,10 +1192,26 @@ struct MixedB {
     const float w = u / umax;
     if (w > 0.9f) {
       const double umax64 = 2.0 * (1.0 + E * kInvMec2);
-      const double u64 = -vdt_log(r01) * (low ? 1.6 : 0.533333333);
-      return 1.0 - 2.0 * u64 * u64 / (umax64 * umax64);
+      const double w64 = -vdt_log(r01) * (low ? 1.6 : 0.533333333) / umax64;
+      omc = d2f(2.0 * w64 * w64);
+      opc = d2f(2.0 * (1.0 - w64) * (1.0 + w64));
+      return;
     }
-    return 1.0 - (double)(2.0f * w * w);
+    omc = 2.0f * w * w;
+    opc = 2.0f * (1.0f - w) * (1.0f + w);
+  }
+  // a unit vector at polar angle (1 - cos, 1 + cos) and azimuth pi phiN about the
+  // direction rd (FP64 input), in FP32 (FP64 rotation close to the z axis)
+  __device__ static void dir_about(float omc, float opc, float phiN, const double* rd, double* out) {
+    float sp, cp;
+    sincospif(phiN, &sp, &cp);
+    const float st = sqrtf(fmx(0.f, omc * opc));
+    float v[3] = {st * cp, st * sp, omc < 1.f ? 1.f - omc : opc - 1.f};
+    const float r[3] = {d2f(rd[0]), d2f(rd[1]), d2f(rd[2])};
+    rotate_mixed(v, r, rd);
+    out[0] = f2d(v[0]);
+    out[1] = f2d(v[1]);
+    out[2] = f2d(v[2]);
   }
 
   // The secondaries of an e+- interaction are rotated to the frame of the
@@ -1241,11 +1257,11 @@ struct MixedB {
     const double E = t.e;
     const double cut = couple().elCut;
     const double tmaxE = t.isEl ? 0.5 * E : E;
-    neard(tmaxE, cut);
-    if (tmaxE <= cut) return;
+    near(d2f(tmaxE), d2f(cut));
+    if (!dless(cut, tmaxE)) return;
     frame_guard();
-    const float Ef = (float)E;
-    const float xmin = (float)(cut / E);
+    const float Ef = d2f(E);
+    const float xmin = d2f(cut) / Ef;
     float x, omx = 1.f;
     int it = 0;
     if (t.isEl) {
@@ -1259,10 +1275,10 @@ struct MixedB {
       float dum, g;
       do {
         const double r0 = rng.flat(), r1 = rng.flat();
-        x = xmm / (xmin * (float)(1.0 - r0) + xmax * (float)r0);
+        x = xmm / (xmin * one_minus_u(r0) + xmax * d2f(r0));
         const float xx = 1.0f - x;
         dum = 1.0f - gg * x + x * x * (1.0f - gg + (1.0f - gg * xx) / (xx * xx));
-        g = gf * (float)r1;
+        g = gf * d2f(r1);
         near(g, dum);
         if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
       } while (g > dum);
@@ -1285,37 +1301,31 @@ struct MixedB {
       float dum, g;
       do {
         const double r0 = rng.flat(), r1 = rng.flat();
-        const float den = xmin * (float)(1.0 - r0) + xmax * (float)r0;
+        const float den = xmin * one_minus_u(r0) + xmax * d2f(r0);
         x = xmm / den;
-        omx = (float)r0 * (1.f - xmin) / den;  // 1 - x, xmax = 1
+        omx = d2f(r0) * (1.f - xmin) / den;  // 1 - x, xmax = 1
         const float xx = x * x;
         dum = 1.0f + (xx * xx * c4 - x * xx * c3 + xx * c2 - x * c1) * b2;
-        g = gf * (float)r1;
+        g = gf * d2f(r1);
         near(g, dum);
         if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
       } while (g > dum);
     }
-    const double dE = (double)x * E;
+    const double dE = f2d(x) * E;
     Sec& s = t.addSec(0);
-    // kinematics in FP64 (cos close to 1 at high energy)
+    // the polar angle in FP64 (cos close to 1 at high energy), 1 -+ cos to FP32
     const double eTot = E + kMec2;
     const double pTot = sqrt(E * (eTot + kMec2));
     const double dP = sqrt(dE * (dE + 2.0 * kMec2));
     const double cost = dE * (eTot + kMec2) / (dP * pTot);
     const double ct = dmax_(-1.0, dmin_(cost, 1.0));
-    const double st = sqrt((1.0 - ct) * (1.0 + ct));
-    float sp, cp;
-    sincospif(2.f * d2f(rng.flat()), &sp, &cp);
-    s.dir[0] = st * cp;
-    s.dir[1] = st * sp;
-    s.dir[2] = ct;
-    rotate(s.dir, t.dir);
+    dir_about(d2f(1.0 - ct), d2f(1.0 + ct), 2.f * d2f(rng.flat()), t.dir, s.dir);
     t.dir[0] = pTot * t.dir[0] - dP * s.dir[0];
     t.dir[1] = pTot * t.dir[1] - dP * s.dir[1];
     t.dir[2] = pTot * t.dir[2] - dP * s.dir[2];
     const double nrm = 1.0 / sqrt(t.dir[0] * t.dir[0] + t.dir[1] * t.dir[1] + t.dir[2] * t.dir[2]);
     t.dir[0] *= nrm; t.dir[1] *= nrm; t.dir[2] *= nrm;
-    const double eAfter = !t.isEl && omx < 0.5f ? E * (double)omx : E - dE;
+    const double eAfter = !t.isEl && omx < 0.5f ? E * f2d(omx) : E - dE;
     t.setE(eAfter);
     s.e = E - eAfter;
     if (eAfter * (eAfter + 2.0 * kMec2) < 4.0e-4 * pTot * pTot) set_trip();  // as in brem
@@ -1328,21 +1338,19 @@ struct MixedB {
 
   __device__ void brem(bool sbModel) {
     const double E = t.e;
-    const double le = vdt_log(E);
-    neard(E, couple().gamCut);
-    if (E <= couple().gamCut) return;
+    const double gcut = ld(&couple().gamCut);
+    near(d2f(E), d2f(gcut));
+    if (!dless(gcut, E)) return;
     frame_guard();
     omk = -1.0;
+    // log E: FP64 for the Seltzer-Berger energy bin (a guarded discrete choice),
+    // FP32 for the relativistic model (the target selection only bins with it)
+    const double le = sbModel ? vdt_log(E) : f2d(logf(d2f(E)));
     const double k = sbModel ? sample_sb(E, le) : sample_rb(E, le);
     Sec& s = t.addSec(2);
-    const double cost = tsai_cost(E);
-    const double sint = sqrt((1.0 - cost) * (1.0 + cost));
-    float sp, cp;
-    sincospif(2.f * d2f(rng.flat()), &sp, &cp);
-    s.dir[0] = sint * cp;
-    s.dir[1] = sint * sp;
-    s.dir[2] = cost;
-    rotate(s.dir, t.dir);
+    float omc, opc;
+    tsai_pair(E, omc, opc);
+    dir_about(omc, opc, 2.f * d2f(rng.flat()), t.dir, s.dir);
     const double eTot = E + kMec2;
     const double pTot = sqrt(E * (eTot + kMec2));
     t.dir[0] = pTot * t.dir[0] - k * s.dir[0];
@@ -1358,6 +1366,25 @@ struct MixedB {
     // the electron's new direction is a difference of momenta ~ pTot: its
     // error is the incoming direction's (~1e-7, FP32 MSC) times pTot / p_after
     if (eAfter * (eAfter + 2.0 * kMec2) < 4.0e-4 * pTot * pTot) set_trip();
+  }
+
+  // first index i (a multiple of 3) with v[i] > val, as Physics::lin_search;
+  // these cumulatives and val are >= 0, so their bit patterns order as integers
+  __device__ static int lin_search_bits(const double* v, int size, double val) {
+    int i = 0;
+    const int s3 = 3 * size;
+    while (i + 9 < s3) {
+      if (dless(val, ld(v + i))) return i;
+      if (dless(val, ld(v + i + 3))) return i + 3;
+      if (dless(val, ld(v + i + 6))) return i + 6;
+      if (dless(val, ld(v + i + 9))) return i + 9;
+      i += 12;
+    }
+    while (i < s3) {
+      if (dless(val, ld(v + i))) break;
+      i += 3;
+    }
+    return i;
   }
 
   __device__ double sample_sb(double E, double le) {
@@ -1396,10 +1423,10 @@ struct MixedB {
     const int tst = st + 4 + (ie - minIE) * size1;
     const double minV = ld(sb.data + tst + gci);
     const double* Tb = sb.data + tst + ncut;
-    const float lkt = (float)((lgcut - le) / (lgcut - ld(sb.lelE + ie)));
-    const float Ef = (float)E;
+    const float lkt = d2f(lgcut - le) / d2f(lgcut - ld(sb.lelE + ie));
+    const float Ef = d2f(E);
     const float pe = Ef + (float)kMec2;
-    const float dsc = (float)ld(&md.densityCor) * pe * pe;
+    const float dsc = d2f(ld(&md.densityCor)) * pe * pe;
     // positron correction: the velocity at E - gcut is fixed, the one at E - k
     // is evaluated in FP64 (kinematic end point k -> E)
     double ib1 = 0.0;
@@ -1407,39 +1434,42 @@ struct MixedB {
       const double e1 = E - gcut;
       ib1 = (e1 + kMec2) / sqrt(e1 * (e1 + 2.0 * kMec2));
     }
-    const float zfac = (float)(kAlpha * k2Pi * (double)Z);
+    const float zfac = (float)(kAlpha * k2Pi) * (float)Z;
     double k = 0.0;
-    float sup = 1.0f;
+    float sup = 1.0f, r1f = 0.f;
     double r1;
     int it = 0;
     do {
       const double r0 = rng.flat();
       r1 = rng.flat();
       float kappa = 1.0f;
+      float kf;
       if (!simple) {
         const double cum = r0 * (1.0 - minV) + minV;
-        int i3 = Physics::lin_search(Tb, kNumKappaSB, cum) - 3;
+        int i3 = lin_search_bits(Tb, kNumKappaSB, cum) - 3;
         if (i3 > 3 * (kNumKappaSB - 2)) { i3 = 3 * (kNumKappaSB - 2); t.flags |= kFlagBadIndex; }
         if (i3 < 0) { i3 = 0; t.flags |= kFlagBadIndex; }
         const int i = i3 / 3;
         const double cL = ld(Tb + i3), cH = ld(Tb + i3 + 3);
-        const float pA = (float)ld(Tb + i3 + 1), pB = (float)ld(Tb + i3 + 2);
-        const float lKL = (float)ld(sb.lkappa + i), lKH = (float)ld(sb.lkappa + i + 1);
+        const float pA = d2f(ld(Tb + i3 + 1)), pB = d2f(ld(Tb + i3 + 2));
+        const float lKL = d2f(ld(sb.lkappa + i)), lKH = d2f(ld(sb.lkappa + i + 1));
         // the rational inverse interpolation lk = lKL + m2/m3 (lKH - lKL) written as
-        // lKH - (lKH - lKL)(1 - m1)(1 - pB m1)/m3, exact in the top bin (lKH = 0)
-        const double om1d = (cH - cum) / (cH - cL);
-        const float m1 = (float)(1.0 - om1d), om1 = (float)om1d;
+        // lKH - (lKH - lKL)(1 - m1)(1 - pB m1)/m3, exact in the top bin (lKH = 0);
+        // m1 and 1 - m1 from FP64 differences of the cumulatives
+        const float dc = d2f(cH - cL);
+        const float m1 = d2f(cum - cL) / dc, om1 = d2f(cH - cum) / dc;
         const float m3 = 1.0f + m1 * (pA + pB * m1);
         const float lk = lKH - (lKH - lKL) * om1 * (1.0f - pB * m1) / m3;
         kappa = expf(lk * lkt);
-        k = (double)kappa * E;
-        omk = (double)(-expm1f(lk * lkt));
+        k = f2d(kappa) * E;
+        kf = kappa * Ef;
+        omk = f2d(-expm1f(lk * lkt));
       } else {
         const double om = r0 * (1.0 - gcut / E);
         k = (1.0 - om) * E;
         omk = om;
+        kf = d2f(k);
       }
-      const float kf = (float)k;
       const float ik = 1.0f / kf;
       sup = 1.0f / (1.0f + dsc * ik * ik);
       if (!t.isEl) {
@@ -1449,9 +1479,10 @@ struct MixedB {
         near(dum, -12.f);
         sup = dum > -12.f ? sup * expf(dum) : 0.f;
       }
-      near((float)r1, sup);
+      r1f = d2f(r1);
+      near(r1f, sup);
       if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
-    } while ((float)r1 > sup);
+    } while (r1f > sup);
     return k;
   }
 
@@ -1484,9 +1515,9 @@ struct MixedB {
       val -= il;
       il *= 2;
       il = il < 0 ? 0 : (il > 78 ? 78 : il);
-      const float f0 = (float)kFuncLPM[il], f1 = (float)kFuncLPM[il + 1];
-      gS = ((float)kFuncLPM[il + 2] - f0) * val + f0;
-      phiS = ((float)kFuncLPM[il + 3] - f1) * val + f1;
+      const float f0 = d2f(kFuncLPM[il]), f1 = d2f(kFuncLPM[il + 1]);
+      gS = (d2f(kFuncLPM[il + 2]) - f0) * val + f0;
+      phiS = (d2f(kFuncLPM[il + 3]) - f1) * val + f1;
     } else {
       float ss = 1.0f / (sh * sh);
       ss *= ss;
@@ -1512,23 +1543,26 @@ struct MixedB {
     const double dcor = dens * pte * pte;
     neard(pte, lpmLim);
     const bool lpm = pte > lpmLim;
-    const float zf1 = (float)ld(&el.zFactor1);
+    const float zf1 = d2f(ld(&el.zFactor1));
     const float zf2 = (1.f + 1.f / dZ) / 12.f;
     const float fmax = zf1 + zf2;
-    // photon energy from the kinematic limits: FP64
+    // photon energy k^2 = exp(xmin + r0 xr) - dcor: in the loop in FP32 as
+    // gcut^2 e^y + dcor (e^y - 1), y = r0 xr, without the cancellation of the
+    // difference; the accepted k in FP64 by the reference's own formula
     const double xmin = vdt_log(gcut * gcut + dcor);
     const double xr = vdt_log(E * E + dcor) - xmin;
-    const float ptef = (float)pte, lpmEf = (float)lpmE, dcorf = (float)dcor;
-    const float z23 = (float)ld(&el.Z23), ilS1 = (float)ld(&el.ilVarS1), ilS1c = (float)ld(&el.ilVarS1Cond);
-    const float z13 = (float)ld(&el.Z13), lz = (float)ld(&el.logZ), coul = (float)ld(&el.coulomb);
-    double k, r1;
+    const float xrf = d2f(xr), gcut2f = d2f(gcut * gcut);
+    const float ptef = d2f(pte), lpmEf = d2f(lpmE), dcorf = d2f(dcor);
+    const float z23 = d2f(ld(&el.Z23)), ilS1 = d2f(ld(&el.ilVarS1)), ilS1c = d2f(ld(&el.ilVarS1Cond));
+    const float z13 = d2f(ld(&el.Z13)), lz = d2f(ld(&el.logZ)), coul = d2f(ld(&el.coulomb));
+    double r0, r1;
     float fv, g;
     int it = 0;
     do {
-      const double r0 = rng.flat();
+      r0 = rng.flat();
       r1 = rng.flat();
-      k = sqrt(dmax_(vdt_exp(xmin + r0 * xr) - dcor, 0.0));
-      const float kf = (float)k;
+      const float yk = d2f(r0) * xrf;
+      const float kf = sqrtf(gcut2f * expf(yk) + dcorf * expm1f(yk));
       const float y = kf / ptef;
       const float omy = 1.f - y;
       const float d0 = 0.25f * y * y;
@@ -1542,7 +1576,7 @@ struct MixedB {
         if (Z < 5) {
           fv = d1 * zf1 + omy * zf2;
         } else {
-          const float d2 = y / (float)(pte - k);
+          const float d2 = y / (ptef - kf);
           const float gam = d2 * 100.f * (float)kMec2 / z13;
           const float eps = gam / z13;
           const float g2 = gam * gam;
@@ -1559,11 +1593,11 @@ struct MixedB {
         }
       }
       fv = fmx(0.0f, fv);
-      g = fmax * (float)r1;
+      g = fmax * d2f(r1);
       near(fv, g);
       if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
     } while (fv < g);
-    return k;
+    return sqrt(dmax_(vdt_exp(xmin + r0 * xr) - dcor, 0.0));
   }
 
   // ---- annihilation in flight (G4HepEmPositronInteractionAnnihilation.icc) -----------
@@ -1634,15 +1668,17 @@ struct MixedB {
 
   __device__ void conversion() {
     const double E = t.e;
-    if (E < 2. * kMec2) return;
-    const double le = t.logE();
+    if (dless(E, 2. * kMec2)) return;
     const int imat = couple().mat;
     const DevMat& md = T.mats[imat];
     const int nElem = ld(&md.nElem);
     // the photon energy is exact here (gammas carry no FP32 continuous loss):
     // the FP64 target selection is the reference's own
-    Physics P{T, rng, t};
-    const int ei = nElem > 1 ? P.conv_target(imat, E, le, rng.flat()) : 0;
+    int ei = 0;
+    if (nElem > 1) {
+      Physics P{T, rng, t};
+      ei = P.conv_target(imat, E, t.logE(), rng.flat());
+    }
     const int Z = ld(T.matElemZ + ld(&md.elemOff) + ei);
     const DevElem& el = T.elems[Z < kMaxZ ? Z : kMaxZ];
     // kinematic limits in FP64
@@ -1662,7 +1698,7 @@ struct MixedB {
       const double epsp = 0.5 - 0.5 * sqrt(1. - dmn / dmx);
       const double epsMin = dmax_(eps0, epsp);
       const double epsRange = 0.5 - epsMin;
-      const float dmnf = (float)dmn, FZf = (float)FZ, dff = (float)df;
+      const float dmnf = d2f(dmn), FZf = d2f(FZ), dff = d2f(df);
       float F10, F20;
       if (dmnf > 1.4f) {
         F10 = 42.038f - 8.29f * logf(dmnf + 0.958f);
@@ -1673,32 +1709,25 @@ struct MixedB {
       }
       F10 -= FZf;
       F20 -= FZf;
-      const float epsRf = (float)epsRange;
+      const float epsRf = d2f(epsRange), epsMinf = d2f(epsMin);
       const float N1 = fmx(F10 * epsRf * epsRf, 0.f);
       const float N2 = fmx(1.5f * F20, 0.f);
       const float cond = N1 / (N1 + N2);
       const float iF10 = 1.f / F10, iF20 = 1.f / F20;
-      double r2;
-      float gr;
+      double r1;
+      bool first;
+      float gr, r2f;
       int it = 0;
-      const bool lpmRegime = E >= 100000.0;
-      const float lpmEf = (float)(kLPM * ld(&md.radLength));
-      const float z23 = (float)ld(&el.Z23), il1 = (float)ld(&el.ilVarS1), il1c = (float)ld(&el.ilVarS1Cond);
-      const float Ef = (float)E;
+      const bool lpmRegime = !dless(E, 100000.0);
+      const float lpmEf = d2f(kLPM * ld(&md.radLength));
+      const float z23 = d2f(ld(&el.Z23)), il1 = d2f(ld(&el.ilVarS1)), il1c = d2f(ld(&el.ilVarS1Cond));
+      const float Ef = d2f(E);
       do {
-        const double r0 = rng.flat(), r1 = rng.flat();
-        r2 = rng.flat();
-        const bool first = lt((float)r0, cond);
-        if (first) {
-          const double cr = (double)cbrtf((float)r1);
-          eps = 0.5 - epsRange * cr;
-          // 1 - cbrt(r1) = (1 - r1) / (1 + c + c^2)
-          dlt = (epsMin - eps0) + epsRange * ((1.0 - r1) / (1.0 + cr + cr * cr));
-        } else {
-          eps = epsMin + epsRange * r1;
-          dlt = (epsMin - eps0) + epsRange * r1;
-        }
-        const float ef = (float)eps;
+        const double r0 = rng.flat();
+        r1 = rng.flat();
+        r2f = d2f(rng.flat());
+        first = lt(d2f(r0), cond);
+        const float ef = first ? 0.5f - epsRf * cbrtf(d2f(r1)) : epsMinf + epsRf * d2f(r1);
         const float dd = dff / (ef * (1.f - ef));
         if (!lpmRegime) {
           gr = first ? (screen1(dd) - FZf) * iF10 : (screen2(dd) - FZf) * iF20;
@@ -1709,15 +1738,25 @@ struct MixedB {
           gr = first ? xiS * ((2.f * phiS + gS) * p1 - gS * p2 - phiS * FZf) * iF10
                      : xiS * ((phiS + 0.5f * gS) * p1 + 0.5f * gS * p2 - 0.5f * (gS + phiS) * FZf) * iF20;
         }
-        near(gr, (float)r2);
+        near(gr, r2f);
         if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
-      } while (gr < (float)r2);
+      } while (gr < r2f);
+      // the accepted eps and dlt = eps - eps0 in FP64
+      if (first) {
+        const double cr = f2d(cbrtf(d2f(r1)));
+        eps = 0.5 - epsRange * cr;
+        // 1 - cbrt(r1) = (1 - r1) / (1 + c + c^2)
+        dlt = (epsMin - eps0) + epsRange * ((1.0 - r1) / (1.0 + cr + cr * cr));
+      } else {
+        eps = epsMin + epsRange * r1;
+        dlt = (epsMin - eps0) + epsRange * r1;
+      }
     }
     // kinetic energies: E dlt for the eps lepton, the rest of E - 2 m c^2 for the other
     const double kEps = E * dlt;
     const double kOther = dmax_(0., (E - 2.0 * kMec2) - kEps);
     double eK, pK;
-    if (rng.flat() > 0.5) {
+    if (dless(0.5, rng.flat())) {
       eK = kOther;
       pK = kEps;
     } else {
@@ -1726,16 +1765,13 @@ struct MixedB {
     }
     Sec& se = t.addSec(0);
     Sec& sp = t.addSec(1);
-    float sph, cph;
-    sincospif(2.f * d2f(rng.flat()), &sph, &cph);
-    const double ce = tsai_cost(eK);
-    const double st = sqrt((1.0 - ce) * (1.0 + ce));
-    se.dir[0] = st * cph; se.dir[1] = st * sph; se.dir[2] = ce;
-    rotate(se.dir, t.dir);
-    const double cpo = tsai_cost(pK);
-    const double stp = sqrt((1.0 - cpo) * (1.0 + cpo));
-    sp.dir[0] = -stp * cph; sp.dir[1] = -stp * sph; sp.dir[2] = cpo;
-    rotate(sp.dir, t.dir);
+    // the positron opposite in azimuth: phi + pi
+    const float phiN = 2.f * d2f(rng.flat());
+    float omc, opc;
+    tsai_pair(eK, omc, opc);
+    dir_about(omc, opc, phiN, t.dir, se.dir);
+    tsai_pair(pK, omc, opc);
+    dir_about(omc, opc, phiN + 1.f, t.dir, sp.dir);
     se.e = eK;
     sp.e = pK;
     t.setE(0.0);
@@ -1747,58 +1783,53 @@ struct MixedB {
     const double thr = 0.0001;
     if (E < thr) return;
     const double org[3] = {t.dir[0], t.dir[1], t.dir[2]};
-    const float kappa = (float)(E * kInvMec2);
+    const float kappa = d2f(E) * (float)kInvMec2;
     const float eps0 = 1.f / (1.f + 2.f * kappa);
     const float eps02 = eps0 * eps0;
     const float al1 = log1pf(2.f * kappa);
     const float al2 = al1 + 0.5f * (1.f - eps02);
     // 1 - cos = (1 - eps)/(eps kappa) and 1 + cos = (eps - eps0)(1 + 2 kappa)/(eps kappa)
     // are both formed from differences computed without cancellation
-    float eps, ome, omc, opc, s2, gf;
+    float eps, ome, omc, opc, s2, gf, r2f = 0.f;
     double r2;
     int it = 0;
     do {
       const double r0 = rng.flat(), r1 = rng.flat();
       r2 = rng.flat();
+      const float r1f = d2f(r1), omr1 = one_minus_u(r1);
       float dlt;  // eps - eps0
-      if (lt(al2 * (float)r0, al1)) {
-        eps = expf(-al1 * (float)r1);
-        ome = -expm1f(-al1 * (float)r1);
-        dlt = eps0 * expm1f(al1 * (float)(1.0 - r1));
+      if (lt(al2 * d2f(r0), al1)) {
+        eps = expf(-al1 * r1f);
+        ome = -expm1f(-al1 * r1f);
+        dlt = eps0 * expm1f(al1 * omr1);
       } else {
-        const float eps2 = eps02 + (1.f - eps02) * (float)r1;
+        const float eps2 = eps02 + (1.f - eps02) * r1f;
         eps = sqrtf(eps2);
-        ome = (1.f - eps02) * (float)(1.0 - r1) / (1.f + eps);
-        dlt = (1.f - eps02) * (float)r1 / (eps + eps0);
+        ome = (1.f - eps02) * omr1 / (1.f + eps);
+        dlt = (1.f - eps02) * r1f / (eps + eps0);
       }
       omc = ome / (eps * kappa);
       opc = dlt * (1.f + 2.f * kappa) / (eps * kappa);
       s2 = omc * opc;
       gf = 1.f - eps * s2 / (1.f + eps * eps);
-      near(gf, (float)r2);
+      r2f = d2f(r2);
+      near(gf, r2f);
       if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
-    } while (gf < (float)r2);
-    const double cost = omc < 1.f ? 1.0 - (double)omc : (double)opc - 1.0;
-    const double sint = sqrt((double)fmx(0.f, s2));
-    float sp, cp;
-    sincospif(2.f * d2f(rng.flat()), &sp, &cp);
-    t.dir[0] = sint * cp;
-    t.dir[1] = sint * sp;
-    t.dir[2] = cost;
-    rotate(t.dir, org);
+    } while (gf < r2f);
+    dir_about(omc, opc, 2.f * d2f(rng.flat()), org, t.dir);
     // energies: the smaller share is computed directly, the other by difference
     double post, se;
     if (eps < 0.5f) {
-      post = E * (double)eps;
+      post = E * f2d(eps);
       se = E - post;
     } else {
-      se = E * (double)ome;
+      se = E * f2d(ome);
       post = E - se;
     }
-    neard(se, thr);
-    neard(post, thr);
+    near(d2f(se), 1.0e-4f);
+    near(d2f(post), 1.0e-4f);
     double dep = 0.0;
-    if (se > thr) {
+    if (dless(thr, se)) {
       Sec& s = t.addSec(0);
       s.dir[0] = E * org[0] - post * t.dir[0];
       s.dir[1] = E * org[1] - post * t.dir[1];
@@ -1813,7 +1844,7 @@ struct MixedB {
     } else {
       dep += se;
     }
-    if (post > thr) {
+    if (dless(thr, post)) {
       t.setE(post);
     } else {
       dep += post;
