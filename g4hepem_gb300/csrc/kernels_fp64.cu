@@ -339,13 +339,22 @@ cudaError_t launch_woodcock(const DevTables& T, int64_t n, const hepem_track_sta
   return cudaGetLastError();
 }
 
+// one warp per track, one Philox block per lane: uniforms k and k + 1 (k even)
+// share the counter (k >> 1, id, 0, c), so a lane writes both, and a warp
+// writes the track's row contiguously
 __global__ void fill_uniforms_kernel(int64_t n, const int32_t* __restrict__ id, int nu, uint64_t seed,
                                      double* __restrict__ u) {
-  const int64_t total = n * nu;
-  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < total; j += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = j / nu;
-    const int k = (int)(j - i * nu);
-    u[j] = philox_uniform(seed, id[i], k);
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; i < n; i += warps) {
+    const int32_t tid = id[i];
+    double* row = u + i * nu;
+    for (int k = 2 * lane; k < nu; k += 64) {
+      uint32_t c0 = (uint32_t)k >> 1, c1 = (uint32_t)tid, c2 = 0u, c3 = 0x48455045u;
+      philox4x32_10(c0, c1, c2, c3, (uint32_t)seed, (uint32_t)(seed >> 32));
+      row[k] = u52_to_double(((uint64_t)c0 << 20) | (uint64_t)(c1 >> 12));
+      if (k + 1 < nu) row[k + 1] = u52_to_double(((uint64_t)c2 << 20) | (uint64_t)(c3 >> 12));
+    }
   }
 }
 
@@ -382,7 +391,7 @@ cudaError_t launch_step(const DevTables& T, int64_t n, const hepem_track_state& 
 cudaError_t launch_fill_uniforms(int64_t n, const int32_t* id, int nu, uint64_t seed, double* u, cudaStream_t s,
                                  int sms) {
   if (n <= 0 || nu <= 0) return cudaSuccess;
-  fill_uniforms_kernel<<<grid_for(n * nu, 256, sms), 256, 0, s>>>(n, id, nu, seed, u);
+  fill_uniforms_kernel<<<grid_for(n * 32, 256, sms), 256, 0, s>>>(n, id, nu, seed, u);
   return cudaGetLastError();
 }
 

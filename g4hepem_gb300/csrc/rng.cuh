@@ -9,6 +9,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 
 #include "vdt.cuh"
 
@@ -33,14 +34,33 @@ __host__ __device__ __forceinline__ void philox4x32_10(uint32_t& c0, uint32_t& c
   }
 }
 
+// (bits52 + 0.5) 2^-52 = (2 bits52 + 1) 2^-53 exactly, built from its bits
+// (integer operations only: no integer-to-FP64 conversion, no FP64 multiply)
+__host__ __device__ __forceinline__ double u52_to_double(uint64_t bits52) {
+  const uint64_t v = 2 * bits52 + 1;  // odd, < 2^53
+#ifdef __CUDA_ARCH__
+  const int p = 63 - __clzll((long long)v);
+#else
+  const int p = 63 - __builtin_clzll(v);
+#endif
+  const uint64_t bits = ((uint64_t)(p - 53 + 1023) << 52) | ((v << (52 - p)) & 0xFFFFFFFFFFFFFull);
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)bits);
+#else
+  double d;
+  memcpy(&d, &bits, sizeof d);
+  return d;
+#endif
+}
+
 __host__ __device__ __forceinline__ double philox_uniform(uint64_t seed, int32_t id, int32_t k) {
   uint32_t c0 = (uint32_t)k >> 1, c1 = (uint32_t)id, c2 = 0u, c3 = 0x48455045u;
   philox4x32_10(c0, c1, c2, c3, (uint32_t)seed, (uint32_t)(seed >> 32));
   const uint32_t a = (k & 1) ? c2 : c0;
   const uint32_t b = (k & 1) ? c3 : c1;
-  const uint64_t bits52 = ((uint64_t)a << 20) | (uint64_t)(b >> 12);
-  return ((double)bits52 + 0.5) * (1.0 / 4503599627370496.0);
+  return u52_to_double(((uint64_t)a << 20) | (uint64_t)(b >> 12));
 }
+
 
 struct Rng {
   const double* u;        // this track's buffered stream
