@@ -1033,6 +1033,32 @@ static __device__ __noinline__ double gamma_pe_xs64(const DevTables& T, int imat
   return dmax_(0.0, inv * (ld(c) + inv * (ld(c + 1) + inv * (ld(c + 2) + inv * ld(c + 3)))));
 }
 
+// The FP64 interaction choice of Physics::gamma_select for a drawn uniform u,
+// from the FP64 total cross section (out of line: taken only when the FP32
+// choice is too close to call); leaves the photoelectric cross section in
+// t.peXS as the FP64 path does
+static __device__ __noinline__ int gamma_select64(const DevTables& T, Track& t, Rng& rng, double u) {
+  Physics P{T, rng, t};
+  const double tot = P.gamma_total_xs();
+  const double tmfp = tot > 0. ? 1. / tot : kLarge;
+  const double e = t.e;
+  const DevGamma& g = T.gm;
+  if (e > g.eMax1) {
+    const double le = t.logE();
+    const int st = ld(&T.couples[t.imc].mat) * g.dataPerMat + g.nData0 + g.nData1;
+    double mx = 0.0, cp = 0.0;
+    int pid = 2;
+    do {
+      mx = pid < 5 ? spline_log_9(g.nE2, g.mx + st, e, le, g.logEMin2, g.ild2, pid) : 0.0;
+      cp += mx * tmfp;
+      ++pid;
+    } while (pid < 6 && u > cp);
+    t.peXS = mx;
+    return pid - 3;
+  }
+  return (u > tmfp * t.peXS) ? 1 : 2;
+}
+
 struct MixedG {
   const DevTables& T;
   Rng& rng;
@@ -1107,8 +1133,11 @@ struct MixedG {
       t.nia[0] = f2d(nia0 - gstep / mfp);
       return -1;
     }
-    // SelectInteraction
-    const float u = d2f(rng.flat());
+    // SelectInteraction; a choice whose FP32 operands are too close to call is
+    // made again in FP64 (gamma_select64) instead of sending the track back
+    const double ud = rng.flat();
+    const float u = d2f(ud);
+    bool tie = false;
     int winner;
     if (w2) {
       float cp = 0.f;
@@ -1116,16 +1145,21 @@ struct MixedG {
       do {
         const float mx = pid < 5 ? spline_log_9_32(g.nE2, h.mx + st2, ef, lef, h.logEMin2, h.ild2, pid) : 0.f;
         cp += mx * mfp;
-        near(u, cp);
+        tie = tie || fabsf(u - cp) <= kGuardTol * fmx(fabsf(u), fabsf(cp));
         ++pid;
       } while (pid < 6 && u > cp);
       winner = pid - 3;
     } else {
-      near(u, mfp * pe);
+      tie = fabsf(u - mfp * pe) <= kGuardTol * fmx(fabsf(u), fabsf(mfp * pe));
       winner = u > mfp * pe ? 1 : 2;
     }
+    if (tie) {
+      winner = gamma_select64(T, t, rng, ud);
+      if (winner != 2) t.peXS = 0.0;
+    } else {
+      t.peXS = winner == 2 ? gamma_pe_xs64(T, imat, e) : 0.0;
+    }
     t.winner = winner;
-    t.peXS = winner == 2 ? gamma_pe_xs64(T, imat, e) : 0.0;
     // Perform up to the interaction: nia -= gstep / mfp after SelectInteraction set it to -1
     t.nia[0] = winner == 0 ? -1.0 : f2d(-1.f - gstep / mfp);
     switch (winner) {
