@@ -1260,8 +1260,10 @@ struct MixedB {
     if (x * x + y * y < 0.004f) set_trip();
   }
 
-  // the e+- target element of a brem model: the FP64 interpolation of the
-  // reference selector, guarded because E carries the FP32 continuous loss
+  // the e+- target element of a brem model: the reference selector's
+  // interpolation in FP32, its comparisons with u guarded (E carries the FP32
+  // continuous loss; the interpolated cumulatives are continuous across the
+  // energy knots, so the bin may come from the FP32 log)
   __device__ int select_brem_target(double E, double le, double u, int which) {
     const DevElData& d = eld();
     const int st = ld(d.selStart[which] + t.imc);
@@ -1269,21 +1271,36 @@ struct MixedB {
     const int nd = (int)ld(D);
     const int ne = (int)ld(D + 1);
     const double* x = D + 4;
-    const double xv = dmax_(ld(x), dmin_(ld(x + ne * (nd - 1)), E));
-    // (the interpolated cumulatives are continuous across energy knots: only
-    // the comparisons with u are guarded)
-    const int ie = (int)dmax_(0.0, dmin_((le - ld(D + 2)) * ld(D + 3), nd - 2.0));
+    const double x0 = ld(x), xn = ld(x + ne * (nd - 1));
+    const double xv = dless(E, x0) ? x0 : dless(xn, E) ? xn : E;
+    int ie = (int)((d2f(le) - d2f(ld(D + 2))) * d2f(ld(D + 3)));
+    ie = ie < 0 ? 0 : (ie > nd - 2 ? nd - 2 : ie);
     int i0 = ie * ne, i1 = i0 + ne;
     const double x1 = ld(x + i0++), x2 = ld(x + i1++);
-    const double b = dmax_(0., dmin_(1., (xv - x1) / (x2 - x1)));
+    const float b = fmx(0.f, fmn(1.f, d2f(xv - x1) / d2f(x2 - x1)));
+    const float uf = d2f(u);
     int k = 0;
     while (k < ne - 1) {
-      const double c = ld(x + i0 + k) + b * (ld(x + i1 + k) - ld(x + i0 + k));
-      neard(u, c);
-      if (!(u > c)) break;
+      const float c0 = d2f(ld(x + i0 + k));
+      const float c = c0 + b * (d2f(ld(x + i1 + k)) - c0);
+      near(uf, c);
+      if (!(uf > c)) break;
       ++k;
     }
     return k;
+  }
+
+  // unit vector along a x - b y (a, b >= 0; x, y unit vectors): the difference
+  // in FP64 (it may cancel), its normalisation in FP32; returns |a x - b y|^2
+  __device__ static float unit_diff(double a, const double* x, double b, const double* y, double* out) {
+    const float fx = d2f(a * x[0] - b * y[0]), fy = d2f(a * x[1] - b * y[1]), fz = d2f(a * x[2] - b * y[2]);
+    const float n2 = fx * fx + fy * fy + fz * fz;
+    float inv = rsqrtf(n2);
+    inv = inv * (1.5f - 0.5f * n2 * inv * inv);
+    out[0] = f2d(fx * inv);
+    out[1] = f2d(fy * inv);
+    out[2] = f2d(fz * inv);
+    return n2;
   }
 
   // ---- Moller / Bhabha (G4HepEmElectronInteractionIoni.icc:19-138) ------------------
@@ -1354,11 +1371,7 @@ struct MixedB {
     const double cost = dE * (eTot + kMec2) / (dP * pTot);
     const double ct = dmax_(-1.0, dmin_(cost, 1.0));
     dir_about(d2f(1.0 - ct), d2f(1.0 + ct), 2.f * d2f(rng.flat()), t.dir, s.dir);
-    t.dir[0] = pTot * t.dir[0] - dP * s.dir[0];
-    t.dir[1] = pTot * t.dir[1] - dP * s.dir[1];
-    t.dir[2] = pTot * t.dir[2] - dP * s.dir[2];
-    const double nrm = 1.0 / sqrt(t.dir[0] * t.dir[0] + t.dir[1] * t.dir[1] + t.dir[2] * t.dir[2]);
-    t.dir[0] *= nrm; t.dir[1] *= nrm; t.dir[2] *= nrm;
+    unit_diff(pTot, t.dir, dP, s.dir, t.dir);
     const double eAfter = !t.isEl && omx < 0.5f ? E * f2d(omx) : E - dE;
     t.setE(eAfter);
     s.e = E - eAfter;
@@ -1377,9 +1390,9 @@ struct MixedB {
     if (!dless(gcut, E)) return;
     frame_guard();
     omk = -1.0;
-    // log E: FP64 for the Seltzer-Berger energy bin (a guarded discrete choice),
-    // FP32 for the relativistic model (the target selection only bins with it)
-    const double le = sbModel ? vdt_log(E) : f2d(logf(d2f(E)));
+    // log E in FP32 (error < 2e-6): the target selection only bins with it,
+    // and the Seltzer-Berger energy-bin choice that uses it is guarded by 2e-5
+    const double le = f2d(logf(d2f(E)));
     const double k = sbModel ? sample_sb(E, le) : sample_rb(E, le);
     Sec& s = t.addSec(2);
     float omc, opc;
@@ -1387,11 +1400,7 @@ struct MixedB {
     dir_about(omc, opc, 2.f * d2f(rng.flat()), t.dir, s.dir);
     const double eTot = E + kMec2;
     const double pTot = sqrt(E * (eTot + kMec2));
-    t.dir[0] = pTot * t.dir[0] - k * s.dir[0];
-    t.dir[1] = pTot * t.dir[1] - k * s.dir[1];
-    t.dir[2] = pTot * t.dir[2] - k * s.dir[2];
-    const double nrm = 1.0 / sqrt(t.dir[0] * t.dir[0] + t.dir[1] * t.dir[1] + t.dir[2] * t.dir[2]);
-    t.dir[0] *= nrm; t.dir[1] *= nrm; t.dir[2] *= nrm;
+    unit_diff(pTot, t.dir, k, s.dir, t.dir);
     // the smaller of the two energies is formed directly, the other as the
     // complement, so that E is shared exactly
     const double eAfter = omk >= 0.0 && omk < 0.5 ? E * omk : E - k;
@@ -1438,7 +1447,8 @@ struct MixedB {
       const double val = (le - sb.logMinE) * sb.ildE;
       ie = (int)val;
       double pH = val - ie;
-      if (pH < 1e-6 || pH > 1.0 - 1e-6) set_trip();
+      // le carries the FP32 log's error: pH to ~1e-5 absolute
+      if (pH < 2e-5 || pH > 1.0 - 2e-5) set_trip();
       if (ie < 0 || ie > kNumElEnergySB - 2) { t.flags |= kFlagBadIndex; return E; }
       if (ld(sb.elE + ie) <= gcut) {
         pH = (le - lgcut) / (ld(sb.lelE + ie + 1) - lgcut);
@@ -1446,6 +1456,7 @@ struct MixedB {
       }
       const double u = rng.flat();
       neard(u, pH);
+      if (fabs(u - pH) < 2e-5) set_trip();
       if (u < pH) ++ie;
       else if (corner) simple = true;
     }
@@ -1700,6 +1711,35 @@ struct MixedB {
     }
   }
 
+  // the pair-production target element (Physics::conv_target): interpolation
+  // in FP32, comparisons with u guarded; the energy bin from the FP32 log (the
+  // cumulatives are continuous across the energy knots)
+  __device__ int conv_target32(int imat, double e, double u) {
+    const DevGamma& g = T.gm;
+    const double* D = g.conv + ld(g.convStart + imat);
+    const int nd = g.convN;
+    const int ne = (int)ld(D);
+    const double* x = g.convGrid;
+    const double x0 = ld(x), xn = ld(x + nd - 1);
+    const double xv = dless(e, x0) ? x0 : dless(xn, e) ? xn : e;
+    int ie = (int)((logf(d2f(e)) - d2f(g.convLogMin)) * d2f(g.convILD));
+    ie = ie < 0 ? 0 : (ie > nd - 2 ? nd - 2 : ie);
+    const double x1 = ld(x + ie), x2 = ld(x + ie + 1);
+    const float b = fmx(0.f, fmn(1.f, d2f(xv - x1) / d2f(x2 - x1)));
+    const int i0 = ie * (ne - 1) + 1;
+    const int i1 = i0 + (ne - 1);
+    const float uf = d2f(u);
+    int k = 0;
+    while (k < ne - 1) {
+      const float c0 = d2f(ld(D + i0 + k));
+      const float c = c0 + b * (d2f(ld(D + i1 + k)) - c0);
+      near(uf, c);
+      if (!(uf > c)) break;
+      ++k;
+    }
+    return k;
+  }
+
   __device__ void conversion() {
     const double E = t.e;
     if (dless(E, 2. * kMec2)) return;
@@ -1709,10 +1749,7 @@ struct MixedB {
     // the photon energy is exact here (gammas carry no FP32 continuous loss):
     // the FP64 target selection is the reference's own
     int ei = 0;
-    if (nElem > 1) {
-      Physics P{T, rng, t};
-      ei = P.conv_target(imat, E, t.logE(), rng.flat());
-    }
+    if (nElem > 1) ei = conv_target32(imat, E, rng.flat());
     const int Z = ld(T.matElemZ + ld(&md.elemOff) + ei);
     const DevElem& el = T.elems[Z < kMaxZ ? Z : kMaxZ];
     // kinematic limits in FP64
@@ -1865,15 +1902,11 @@ struct MixedB {
     double dep = 0.0;
     if (dless(thr, se)) {
       Sec& s = t.addSec(0);
-      s.dir[0] = E * org[0] - post * t.dir[0];
-      s.dir[1] = E * org[1] - post * t.dir[1];
-      s.dir[2] = E * org[2] - post * t.dir[2];
-      const double q2 = s.dir[0] * s.dir[0] + s.dir[1] * s.dir[1] + s.dir[2] * s.dir[2];
+      const float q2 = unit_diff(E, org, post, t.dir, s.dir);
       // the electron direction is a difference of ~E-sized vectors built with
       // the FP32 photon angle: its error grows as E / |q|
-      if (q2 < 4.0e-4 * E * E) set_trip();
-      const double nrm = 1.0 / sqrt(q2);
-      s.dir[0] *= nrm; s.dir[1] *= nrm; s.dir[2] *= nrm;
+      const float Ef2 = d2f(E);
+      if (q2 < 4.0e-4f * Ef2 * Ef2) set_trip();
       s.e = se;
     } else {
       dep += se;
