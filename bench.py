@@ -239,7 +239,7 @@ def c3_batching(torch, N, args):
     sub-batch is one call; timed: the plain form, the batched form with the
     default launch configuration, the batched form with the configuration
     chosen by the autotuner, and the latter captured once in a CUDA graph and
-    replayed."""
+    replayed; then the precision form, called and replayed from a graph."""
     from g4hepem_gb300 import workload as W
     table = os.path.join(REPO, "g4hepem_gb300", "data", "random16.json")
     ctx = N.Context(table)
@@ -287,6 +287,15 @@ def c3_batching(torch, N, args):
     with torch.cuda.graph(graph):
         one_pass("batched")
     ms_graph = timed(graph.replay, reps)
+    # the same sub-batches through the precision form, also captured and replayed
+    ms_mixed = timed(lambda: one_pass("mixed"), reps)
+    graph_m = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(side):
+        one_pass("mixed")
+    torch.cuda.current_stream().wait_stream(side)
+    with torch.cuda.graph(graph_m):
+        one_pass("mixed")
+    ms_mixed_graph = timed(graph_m.replay, reps)
     ctx.close()
     return {"workload": "64 sub-batches (log-normal, median 30k, sigma 1.5, clipped [1k, 1M], scaled to "
                         "16,777,216 tracks), 16 random couples, configuration-2 particle/energy mix",
@@ -299,7 +308,12 @@ def c3_batching(torch, N, args):
             "autotuned_config": tuned,
             "batched_graph": {"value": total / (ms_graph / 1e3), "unit": UNIT, "ms_per_pass": ms_graph,
                               "launches_per_pass": LAUNCHES_PER_STEP * len(sizes)},
-            "vs_plain": ms_plain / ms_graph}
+            "vs_plain": ms_plain / ms_graph,
+            "mixed": {"value": total / (ms_mixed / 1e3), "unit": UNIT, "ms_per_pass": ms_mixed,
+                      "entry_point": "hepem_step_mixed"},
+            "mixed_graph": {"value": total / (ms_mixed_graph / 1e3), "unit": UNIT, "ms_per_pass": ms_mixed_graph,
+                            "launches_per_pass": LAUNCHES_PER_STEP_MIXED * len(sizes)},
+            "mixed_vs_plain": ms_plain / ms_mixed_graph}
 
 
 def c4_serving(torch, N, args):
@@ -671,7 +685,8 @@ def main():
             # same results, without moving 8 * NU bytes per track over the link
             N.check(host_fn(ctx.h, n, C.byref(sin_h), C.byref(sout_h), None, 0, SEED, C.byref(sres_h),
                             C.byref(hcnt), stream.cuda_stream))
-        host_step()
+        for _ in range(3):
+            host_step()
         barrier()
         t0 = time.perf_counter()
         for _ in range(ctx_steps):

@@ -292,9 +292,11 @@ def test_batched_equals_plain_bitwise(native, gpu_ctx, table, nc, emin, emax):
     assert np.array_equal(a_cnt, b_cnt), (a_cnt, b_cnt)
 
 
-def test_batched_step_replays_from_a_cuda_graph(native, gpu_ctx):
-    """The batched entry point is stream-capturable (its workspace is a
-    stream-ordered allocation): capture once, replay, same results."""
+@pytest.mark.parametrize("form", ["batched", "mixed"])
+def test_batched_step_replays_from_a_cuda_graph(native, gpu_ctx, form):
+    """The batched entry points (FP64 and precision form) are stream-capturable
+    (their workspace is a stream-ordered allocation): capture once, replay,
+    same results."""
     torch = _torch()
     st = W.mixed_batch(100000, seed=71)
     n = len(st["ekin"])
@@ -302,16 +304,16 @@ def test_batched_step_replays_from_a_cuda_graph(native, gpu_ctx):
     sin = native.state_to_torch(st)
     u = native.fill_uniforms(sin["id"], 64, 9)
     ref_out, ref_res = native.empty_state_torch(n), native.alloc_out_torch(n)
-    ctx.step(sin, ref_out, u, 64, 9, ref_res, form="batched")
+    ctx.step(sin, ref_out, u, 64, 9, ref_res, form=form)
     g_out, g_res = native.empty_state_torch(n), native.alloc_out_torch(n)
     side = torch.cuda.Stream()
     side.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(side):
-        ctx.step(sin, g_out, u, 64, 9, g_res, form="batched")
+        ctx.step(sin, g_out, u, 64, 9, g_res, form=form)
     torch.cuda.current_stream().wait_stream(side)
     graph = torch.cuda.CUDAGraph()
     with torch.cuda.graph(graph):
-        ctx.step(sin, g_out, u, 64, 9, g_res, form="batched")
+        ctx.step(sin, g_out, u, 64, 9, g_res, form=form)
     for v in list(g_out.values()) + list(g_res.values()):
         v.zero_()
     graph.replay()
