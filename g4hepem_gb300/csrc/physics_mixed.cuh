@@ -1,23 +1,29 @@
-// physics_mixed.cuh -- the e+- stage A (HowFar, continuous step, MSC, energy
-// loss fluctuations, delta-interaction test) of the precision form.
+// physics_mixed.cuh -- the precision form: the e+- stage A (HowFar,
+// continuous step, MSC, energy loss fluctuations, delta-interaction test;
+// MixedEl), the gamma stage A (HowFar and interaction choice; MixedG) and the
+// FP32 interaction models (MixedB).
 //
-// The same algorithm as Physics::el_howfar + el_perform_until_discrete
-// (physics.cuh, G4HepEmElectronManager.icc:35-483, UMSC and fluctuation
+// The same algorithms as Physics (physics.cuh; G4HepEmElectronManager.icc:35-483,
+// G4HepEmGammaManager.icc:27-130, the UMSC, fluctuation and interaction
 // models), with the table lookups and the sampling arithmetic in FP32 from
-// FP32 tables (DevElData32).  FP64 is kept for: the decisions on exact inputs
-// (energy against table thresholds), the range->energy inversion of the mean
-// energy loss, the polar-method acceptance of Gaussian samples, the sum of the
-// fluctuation terms, and the energy / deposit bookkeeping.
+// FP32 tables (DevElData32, DevGamma32) and FP32 parameter records.  FP64 is
+// kept for: the decisions on exact inputs (energy against table thresholds,
+// compared as integer bit patterns), the range->energy inversion of the mean
+// energy loss, the polar-method acceptance of Gaussian samples, the accepted
+// photon energy / epsilon of the relativistic brem and pair production, the
+// kinematic limits, and the energy / deposit bookkeeping.  Conversions between
+// FP64 and FP32 are integer bit operations (d2f, f2d): on this GPU they would
+// otherwise run on the FP64 pipe.
 //
 // Guarded decisions.  Every branch that changes a discrete outcome (the
 // winning process, whether MSC limits the step or scatters, Gaussian or
-// Poisson sampling, Poisson counts, rejection-loop acceptances, the
-// delta-interaction test, the tracking cut) compares FP32 values that carry a
-// relative error of ~1e-6.  A comparison whose operands are closer than
-// kGuardTol (relative) sets `trip`: the caller then discards the track's FP32
-// result and steps it again with the FP64 code (Physics), which gives the
-// FP64 outcome bit for bit.  So the discrete outcomes of the precision form
-// are those of the FP64 path; the tripped fraction is reported.
+// Poisson sampling, Poisson counts, rejection-loop acceptances, target
+// elements, the delta-interaction test, the tracking cut) compares FP32 values
+// that carry a relative error of ~1e-6.  A comparison whose operands are
+// closer than kGuardTol (relative) sets `trip`: the caller then discards the
+// track's FP32 result and steps it again with the FP64 code (Physics), which
+// gives the FP64 outcome bit for bit.  So the discrete outcomes of the
+// precision form are those of the FP64 path; the tripped fraction is reported.
 #pragma once
 
 #include "physics.cuh"
