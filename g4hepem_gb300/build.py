@@ -22,9 +22,12 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 # (source, extra nvcc flags)
 UNITS = [
     ("kernels_fp64.cu", ["-fmad=false"]),
-    # single-precision division and square root to ~2 ulp (the precision form's
-    # FP32 stages; FP64 arithmetic is not affected by these two flags)
-    ("kernels_batched.cu", ["-fmad=false", "-prec-div=false", "-prec-sqrt=false"]),
+    ("kernels_batched.cu", ["-fmad=false"]),
+    # the precision form's FP32 stage kernels: FMA contraction on, single-precision
+    # division and square root to ~2 ulp (FP64 arithmetic is not affected by
+    # these two flags; its exact decisions do not rest on contraction-sensitive
+    # expressions, see physics_mixed.cuh)
+    ("kernels_batched_mixed.cu", ["-prec-div=false", "-prec-sqrt=false"]),
     ("api.cu", ["-fmad=false"]),
     ("noalloc.cu", []),
     ("server.cu", ["-fmad=false"]),

@@ -28,13 +28,24 @@
 #include "physics_mixed.cuh"
 #include "step_io.cuh"
 
+// This file is compiled twice.  As itself (the FP64 unit, -fmad=false: the
+// FP64 path is bit-exact only without contraction) it holds the sort, the
+// FP64 stage kernels, the FP64 fallback and the host side.  Included by
+// kernels_batched_mixed.cu with HEPEM_MIXED_UNIT defined, it holds the FP32
+// stage kernels of the precision form, compiled with contraction (FFMA) on.
+#ifdef HEPEM_MIXED_UNIT
+#define HEPEM_FP64_UNIT 0
+#else
+#define HEPEM_FP64_UNIT 1
+#endif
+
 namespace hepem {
 
 // Diagnostics build only (-DHEPEM_TRIP_SITES): count, per source line of
 // physics_mixed.cuh, the guards that sent a track of the precision form to
 // its FP64 fallback (read with hepem_debug_trip_sites).
 #ifdef HEPEM_TRIP_SITES
-__device__ unsigned long long g_tripSites[4096];
+static __device__ unsigned long long g_tripSites[4096];
 #define HEPEM_COUNT_TRIP(line) atomicAdd(&g_tripSites[(line) & 4095], 1ull)
 #else
 #define HEPEM_COUNT_TRIP(line) ((void)0)
@@ -67,6 +78,7 @@ __device__ __forceinline__ uint64_t key_of(const Work& w, int64_t i, uint64_t se
   return w.seeds ? w.seeds[i] : seed;
 }
 
+#if HEPEM_FP64_UNIT
 const char* stage_name(int i) {
   static const char* names[kNumStageEvents - 1] = {
       "sort", "stage_a_charged", "stage_a_gamma", "ioni_e-", "ioni_e+", "brem_sb", "brem_rb",
@@ -270,6 +282,8 @@ __global__ void __launch_bounds__(256) sort_scatter_kernel(const __grid_constant
     __syncthreads();
   }
 }
+
+#endif  // HEPEM_FP64_UNIT
 
 // ---- 2. stage A -----------------------------------------------------------------------
 // copy of the mutable pre-step state of track i (precision form, in-place steps)
@@ -567,6 +581,7 @@ __device__ __forceinline__ void interaction_fp64(Physics& P) {
   if (Q == kQAnnihRest) P.annihilate_at_rest();
 }
 
+#if HEPEM_FP64_UNIT
 __device__ void charged_full_step(const DevTables& T, const hepem_track_state& in, const hepem_track_state& out,
                                   const double* uniforms, int nu, uint64_t seed, const hepem_step_out& res,
                                   const Work& w, int32_t i, bool fromStageA, StepCount& cnt) {
@@ -674,6 +689,8 @@ __global__ void __launch_bounds__(BS) final_fallback_kernel(const __grid_constan
   add_counters(cnt, counters);
 }
 
+#endif  // HEPEM_FP64_UNIT
+
 // ---- host side -------------------------------------------------------------------------------
 // The eleven stage kernels share one signature; each exists for 128, 256 and
 // 512 threads per block, and the launch configuration picks one of them and
@@ -714,6 +731,16 @@ static void mixed_table(StageFn* m) {
   m[2 + kQCompton] = stage_b_kernel<kQCompton, BS, kStageMixed>;
 }
 
+#if !HEPEM_FP64_UNIT
+// the precision form's stage kernels of this unit, for the FP64 unit's table
+void mixed_stage_table(int b, StageFn* m) {
+  if (b == 0) mixed_table<128>(m);
+  else if (b == 2) mixed_table<512>(m);
+  else mixed_table<256>(m);
+}
+#else
+void mixed_stage_table(int b, StageFn* m);  // kernels_batched_mixed.cu
+
 struct StageKernels {
   StageFn fn[3][kNumStageKernels];
   int occ[3][kNumStageKernels];  // resident CTAs per SM
@@ -736,9 +763,9 @@ static const StageKernels& stage_kernels() {
     stage_table<128>(r.fn[0]);
     stage_table<256>(r.fn[1]);
     stage_table<512>(r.fn[2]);
-    mixed_table<128>(r.mixed[0]);
-    mixed_table<256>(r.mixed[1]);
-    mixed_table<512>(r.mixed[2]);
+    mixed_stage_table(0, r.mixed[0]);
+    mixed_stage_table(1, r.mixed[1]);
+    mixed_stage_table(2, r.mixed[2]);
     r.final_[0] = final_fallback_kernel<128>;
     r.final_[1] = final_fallback_kernel<256>;
     r.final_[2] = final_fallback_kernel<512>;
@@ -929,10 +956,13 @@ cudaError_t launch_sample(const DevTables& T, int model, int mixed, int64_t n, d
     sample_kernel<false><<<g, 256, 0, s>>>(T, model, n, ekin, imc, seed, out, nFallback);
   return cudaGetLastError();
 }
+#endif  // HEPEM_FP64_UNIT
 
 }  // namespace hepem
 
-#ifdef HEPEM_TRIP_SITES
+// diagnostics exports: the trip counters of the precision form's kernels live
+// in the FP32 unit, the trace rows in both (FP64 row 0 here, row 1 there)
+#if defined(HEPEM_TRIP_SITES) && !HEPEM_FP64_UNIT
 extern "C" int hepem_debug_trip_sites(unsigned long long* out, int reset) {
   cudaError_t e = cudaMemcpyFromSymbol(out, hepem::g_tripSites, sizeof(unsigned long long) * 4096);
   if (e == cudaSuccess && reset) {
@@ -944,7 +974,11 @@ extern "C" int hepem_debug_trip_sites(unsigned long long* out, int reset) {
 #endif
 
 #ifdef HEPEM_TRACE
+#if HEPEM_FP64_UNIT
 extern "C" int hepem_debug_trace(int id, double* out128) {
+#else
+extern "C" int hepem_debug_trace_mixed(int id, double* out128) {
+#endif
   if (id >= -1) {
     static const double zero[128] = {};
     if (cudaMemcpyToSymbol(hepem::g_trace, zero, sizeof(zero)) != cudaSuccess) return 3;

@@ -367,9 +367,11 @@ struct MixedEl {
     int it = 0;
     do {
       const double a = rng.flat(), b = rng.flat();
-      v1 = 2. * a - 1.;
-      v2 = 2. * b - 1.;
-      r = v1 * v1 + v2 * v2;
+      // the acceptance r > 1 is the FP64 path's decision: evaluated with its
+      // rounding (no contraction into FMA)
+      v1 = __dsub_rn(__dmul_rn(2., a), 1.);
+      v2 = __dsub_rn(__dmul_rn(2., b), 1.);
+      r = __dadd_rn(__dmul_rn(v1, v1), __dmul_rn(v2, v2));
       if (++it >= kMaxIter) { t.flags |= kFlagLoopCap; break; }
     } while (dless(1.0, r));
     const float rf = d2f(r);
