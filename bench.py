@@ -1,11 +1,14 @@
 """Benchmark of the G4HepEmRun stepping-physics path on GB300.
 
-Workload (BASELINE configuration 2): 4,194,304 tracks, 45% gamma / 45% e- /
+Workload (the 4M mixed-track step): 4,194,304 tracks, 45% gamma / 45% e- /
 10% e+, kinetic energies log-uniform in [1 MeV, 10 GeV], couples uniform over
 G4_PbWO4 / G4_lAr / G4_Pb at 0.7 mm (synthetic G4HepEmState tables), isotropic
 directions, first-step track state, 64 Philox uniforms per track.  One "step"
-= one HowFar + Perform of every track (plain FP64 path, bit-exact with the
-reference CPU functions).  Each timed step reads the same input state and
+= one HowFar + Perform of every track.  `--form mixed` (default) steps it with
+the precision form (hepem_step_mixed: FP32 bulk, FP64 where the error budget
+needs it, discrete outcomes identical to the FP64 path); `--form batched` with
+the FP64 batched form (bit-exact with the reference CPU functions).  The plain
+FP64 form (hepem_step, bit-exact) is timed beside either.  Each timed step reads the same input state and
 writes separate outputs, so every step does identical work; the inputs
 (~2.7 GB) are larger than L2.
 
@@ -13,11 +16,13 @@ writes separate outputs, so every step does identical work; the inputs
 
 Prints one JSON line (rank 0).  `value` is device-resident throughput
 (steps/s over all ranks); `e2e` is the same metric through the host-buffer
-C-ABI entry point hepem_step_host with the host<->device copies of the track
-state inside the timed region (the uniforms are drawn on the device from the
+C-ABI entry point of the form (hepem_step_host_mixed, or hepem_step_host for
+--form batched) with the host<->device copies of the track state inside the
+timed region (the uniforms are drawn on the device from the
 same counter-based stream, n_uniform = 0).  `--impl reference` times the reference algorithm on the host
-cores: the CPU port of the oracle (the reference build itself cannot exist on
-the GPU host), all host threads, same workload and metric.
+cores: the CPU port of the oracle (the reference build needs the reference
+sources, which only the development host has), all host threads, same workload
+and metric.
 """
 from __future__ import annotations
 
@@ -44,7 +49,7 @@ LAUNCHES_PER_STEP = 14  # 3 sort kernels, 2 stage-A kernels, 9 interaction kerne
 LAUNCHES_PER_STEP_MIXED = 15
 METRIC = "mixed e±/γ physics steps/s (1 GB300) vs plain FP64 path; p50/p99 batch latency"
 UNIT = "steps/s"
-CONFIG = {"workload": "plain FP64 full step, 4,194,304 mixed tracks (45% gamma, 45% e-, 10% e+), "
+CONFIG = {"workload": "full physics step (HowFar + Perform), 4,194,304 mixed tracks (45% gamma, 45% e-, 10% e+), "
                       "1 MeV-10 GeV log-uniform, 3 couples (G4_PbWO4, G4_lAr, G4_Pb @0.7 mm), "
                       "64 Philox uniforms/track",
           "tracks_per_step": N_TRACKS, "uniforms_per_track": NU, "table": "three_couples_0.7mm.json",
@@ -198,7 +203,7 @@ def profile_summary(name):
 
 
 def c1_lookups(torch, N, ctx, stream, args, hbm):
-    """BASELINE configuration 1: 2^20 e- with energies log-uniform in
+    """Electron lookups: 2^20 e- with energies log-uniform in
     [1 keV, 100 TeV] over the 3 couples; restricted ionisation and brem cross
     sections, dE/dx, range and inverse range at half the range per track
     (hepem_electron_lookup).  Inputs 12 B + outputs 40 B per track; the
@@ -232,9 +237,9 @@ def c1_lookups(torch, N, ctx, stream, args, hbm):
 
 
 def c3_batching(torch, N, args):
-    """BASELINE configuration 3: 64 sub-batches of log-normal sizes (median 30k
+    """Uneven batching: 64 sub-batches of log-normal sizes (median 30k
     before scaling, sigma 1.5, clipped to [1k, 1M], scaled to 16,777,216 tracks
-    in total), the configuration-2 particle and energy mix, 16 random couples
+    in total), the particle and energy mix of the 4M-track step, 16 random couples
     (1-4 elements, Z in 1..82, 1-12 g/cm3, cuts 0.1/0.7/1.0 mm).  Each
     sub-batch is one call; timed: the plain form, the batched form with the
     default launch configuration, the batched form with the configuration
@@ -298,7 +303,7 @@ def c3_batching(torch, N, args):
     ms_mixed_graph = timed(graph_m.replay, reps)
     ctx.close()
     return {"workload": "64 sub-batches (log-normal, median 30k, sigma 1.5, clipped [1k, 1M], scaled to "
-                        "16,777,216 tracks), 16 random couples, configuration-2 particle/energy mix",
+                        "16,777,216 tracks), 16 random couples, the particle/energy mix of the 4M-track step",
             "subbatch_min": int(sizes.min()), "subbatch_median": int(np.median(sizes)),
             "subbatch_max": int(sizes.max()),
             "plain": {"value": total / (ms_plain / 1e3), "unit": UNIT, "ms_per_pass": ms_plain},
@@ -317,10 +322,10 @@ def c3_batching(torch, N, args):
 
 
 def c4_serving(torch, N, args):
-    """BASELINE configuration 4: an event stream through the serving form
+    """Serving: an event stream through the serving form
     (hepem_server_*).  A request is one event's track batch, log-normal in size
     (median 2k tracks, sigma 1.5, clipped to [1, 500k]), with the
-    configuration-2 particle / energy / couple mix; 256 distinct event batches
+    particle / energy / couple mix of the 4M-track step; 256 distinct event batches
     are drawn once and re-submitted with fresh seeds (new uniform streams).
     Memory admission budget 16 GB; tracks stay resident until they fall below
     1 keV or the request reaches 1000 steps.  First the sustained peak: a
@@ -409,18 +414,18 @@ def c4_serving(torch, N, args):
     srv.close()
     ctx.close()
     return {"workload": "event stream: requests log-normal (median 2k tracks, sigma 1.5, clipped [1, 500k]), "
-                        "configuration-2 mix, 16 GB admission budget, resident until < 1 keV or 1000 steps",
+                        "mix of the 4M-track step, 16 GB admission budget, resident until < 1 keV or 1000 steps",
             "capacity_tracks": cap, "event_pool": len(events), "event_size_median": int(np.median(sizes)),
             "event_size_max": int(sizes.max()), "peak": peak, "poisson": levels,
             "form": "precision (hepem_server_config.precision = 1)" if args.form == "mixed" else "FP64 batched"}
 
 
 def c5_precision(torch, N, args, n_tracks=1 << 24):
-    """BASELINE configuration 5: the precision form (hepem_step_mixed) on a
-    16,777,216-track batch with the configuration-2 mix, against the FP64
+    """Precision: the precision form (hepem_step_mixed) on a
+    16,777,216-track batch with the mix of the 4M-track step, against the FP64
     batched form on identical uniforms: steps/s of both, the FP64 fallback
     fraction, discrete mismatches (must be 0) and per-quantity max / RMS
-    relative errors; the configuration-1 lookups from the FP32 tables against
+    relative errors; the 2^20-track electron lookups from the FP32 tables against
     the FP64 ones; and chi2 of 1e8 Seltzer-Berger brem draws at 999 MeV in G4_Pb
     (just below the 1 GeV switch to the relativistic model) and 1e8
     Klein-Nishina draws at 1 MeV in G4_lAr, FP32 models against FP64 models."""
@@ -474,7 +479,7 @@ def c5_precision(torch, N, args, n_tracks=1 << 24):
             "dir_abs_max": float(max((b_s[k] - a_s[k]).abs().max() for k in ("dir_x", "dir_y", "dir_z")))}
     del outs, ress, a_s, b_s, a_r, b_r
     torch.cuda.empty_cache()
-    # configuration-1 lookups, FP32 tables against FP64
+    # the 2^20-track electron lookups, FP32 tables against FP64
     e_np, i_np = W.electron_lookup_batch(1 << 20, seed=11)
     ekin = torch.from_numpy(e_np).cuda()
     imc = torch.from_numpy(i_np).cuda()
@@ -524,7 +529,7 @@ def c5_precision(torch, N, args, n_tracks=1 << 24):
                      "fp64_fallback_draws": fb_total, "draws_per_s": tms}
     ctx.close()
     c = cnts["mixed"].cpu().numpy()
-    return {"workload": f"{n} mixed tracks (configuration-2 mix), 64 Philox uniforms/track, identical streams",
+    return {"workload": f"{n} mixed tracks (mix of the 4M-track step), 64 Philox uniforms/track, identical streams",
             "mixed": {"value": n / (ms["mixed"] / 1e3), "unit": UNIT, "ms_per_step": ms["mixed"],
                       "entry_point": "hepem_step_mixed"},
             "fp64_batched": {"value": n / (ms["batched"] / 1e3), "unit": UNIT, "ms_per_step": ms["batched"]},
@@ -750,7 +755,7 @@ def main():
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_src == "measured" else "fallback",
             "algorithmic_bytes_per_launch": alg, "ms_per_launch": ms_dom,
             "note": ("HBM is not the limit of this kernel: the precision form's stage A is bound by the latency "
-                     "of dependent table and state gathers (profiles/stage_a_charged_mixed_c2_2M.md); traffic is "
+                     "of dependent table and state gathers (profiles/stage_a_charged_mixed_2M_tracks.md); traffic is "
                      "the ncu DRAM bytes per e+- track x the e+- tracks of the step" if args.form == "mixed" else
                      "HBM is not the limit of this kernel: the FP64 pipe is (roofline_fp64, profiles/)")}
     fp64 = {"bound": "fp64", "kernel": dom, "unit": "TFLOP/s", "peak": None,

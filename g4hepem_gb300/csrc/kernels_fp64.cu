@@ -2,10 +2,10 @@
 // --fmad=false: no contracted multiply-adds, so the arithmetic is the
 // reference's operation by operation).
 //
-//  lookup_kernel  : BASELINE configuration 1, the reference functions
+//  lookup_kernel  : the electron table lookups, the reference functions
 //                   GetRestMacXSec / GetRestDEDX / GetRestRange / GetInvRange
 //                   (G4HepEm/G4HepEmRun/include/G4HepEmElectronManager.icc:486-532)
-//  step_kernel    : one HowFar + Perform per track (configuration 2)
+//  step_kernel    : one HowFar + Perform per track
 //  fill_uniforms  : the per-track Philox streams of the C-ABI contract
 #include <cstdint>
 

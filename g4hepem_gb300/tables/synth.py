@@ -720,14 +720,14 @@ class StateBuilder:
 
 
 def three_couple_state(range_cut=0.7):
-    """G4_PbWO4, G4_lAr and G4_Pb at one range cut (BASELINE configurations 1, 2, 5)."""
+    """G4_PbWO4, G4_lAr and G4_Pb at one range cut (the lookup, step and precision workloads)."""
     mats = [NAMED["G4_PbWO4"](), NAMED["G4_lAr"](), NAMED["G4_Pb"]()]
     return StateBuilder(mats, [Couple(i, range_cut) for i in range(3)]).state()
 
 
 def random_couple_state(n_couples=16, seed=1234, regions=None):
     """n random materials of 1-4 elements, Z in 1..82, density U[1,12] g/cm3,
-    cut in {0.1, 0.7, 1.0} mm (BASELINE configuration 3)."""
+    cut in {0.1, 0.7, 1.0} mm (the uneven-batching workload)."""
     rng = np.random.default_rng(seed)
     mats, couples = [], []
     for i in range(n_couples):

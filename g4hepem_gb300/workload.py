@@ -118,7 +118,7 @@ def electron_lookup_batch(n: int, n_couples: int = 3, seed: int = 11, emin=1e-3,
 
 def subbatch_sizes(total: int = 1 << 24, n_sub: int = 64, median: float = 30000.0, sigma: float = 1.5,
                    lo: int = 1000, hi: int = 1 << 20, seed: int = 3) -> np.ndarray:
-    """Uneven sub-batch sizes of BASELINE configuration 3: log-normal with the
+    """Uneven sub-batch sizes of the batching workload: log-normal with the
     given median and sigma, scaled so that the clipped sizes sum to `total`
     (the scale factor is found by bisection; the last size absorbs rounding)."""
     rng = np.random.Generator(np.random.Philox(seed))

@@ -6,7 +6,7 @@
  * operand order of the reference so that results agree bit for bit where the
  * reference itself is deterministic (log/exp by the VDT/Cephes Pade method,
  * no contracted multiply-adds; sin/cos/pow/sqrt from the host libm).
- * It is the checker of the GPU path on hosts without the reference sources and
+ * It is the oracle of the GPU path on hosts without the reference sources and
  * the timed CPU baseline; it is pinned against the reference itself by
  * tests/golden (vectors written by oracle/_ref) and by tests that run both.
  *

@@ -109,7 +109,7 @@ void ref_vdt_pow(int64_t n, const double* x, const double* a, double* y) {
   for (int64_t i = 0; i < n; ++i) y[i] = G4HepEmPow(x[i], a[i]);
 }
 
-// Table lookups of the electron tables (BASELINE configuration 1).
+// Table lookups of the electron tables (2^20-track lookup workload).
 void ref_electron_lookup(void* st, int64_t n, int is_positron, const double* ekin,
                          const int32_t* imc, double* xs_ioni, double* xs_brem,
                          double* dedx, double* range, double* invrange_half) {

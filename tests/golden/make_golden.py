@@ -6,7 +6,7 @@ Usage (where the reference sources are present):
 It builds oracle/_ref/libhepem_ref.so from the reference sources (oracle/Makefile),
 loads the committed synthetic tables through the reference's own
 G4HepEmStateFromJson, and records inputs and outputs of the reference
-functions: VDT log/exp, the configuration-1 lookups, step-limit cross
+functions: VDT log/exp, the electron table lookups, step-limit cross
 sections, target-element selectors, gamma cross sections and interaction
 selection, and full HowFar+Perform steps (fresh tracks, a second step that
 carries MSC/Gauss/RNG state, boundary and safety variants, and a 16-couple
@@ -78,7 +78,7 @@ def main():
     xe = np.concatenate([r.uniform(-720, 720, 3000), r.uniform(-1, 1, 1000), [0.0, -0.0, 708.0, -708.0]])
     save("vdt.npz", x_log=xl, y_log=ref.vdt_log(xl), x_exp=xe, y_exp=ref.vdt_exp(xe))
 
-    # configuration-1 lookups + step-limit cross sections
+    # electron table lookups + step-limit cross sections
     ekin, imc = W.electron_lookup_batch(8192, seed=11)
     d = dict(ekin=ekin, imc=imc)
     for pos in (0, 1):
@@ -103,7 +103,7 @@ def main():
             d[f"brem_p{pos}_sb{sb}"] = ref.brem_select_target(es, np.zeros(8192, np.int32), us, bool(pos), bool(sb))
     save("selectors_3couples.npz", **d)
 
-    # full steps, three couples: BASELINE mix, a second step, a wide-range batch
+    # full steps, three couples: the 45/45/10 mix, a second step, a wide-range batch
     st = W.mixed_batch(8192, seed=7)
     d1, out1 = step_fixture(ref, st, SEED, prefix="s1_")
     # second step: continue the same tracks (alive ones keep their state)

@@ -202,7 +202,7 @@ def test_bad_track_inputs_are_flagged_not_faulted(native, gpu_ctx):
     assert not np.any(res["flags"][ok] & 4)
 
 
-# ---- full-size properties (BASELINE configuration 2: 4M mixed tracks) --------------------
+# ---- full-size properties (the 4M mixed-track step) -----------------------------------
 @pytest.fixture(scope="module")
 def full_batch(native, gpu_ctx):
     n = 1 << 22
