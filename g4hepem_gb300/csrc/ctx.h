@@ -16,6 +16,10 @@ struct hepem_ctx {
   void* arena = nullptr;
   size_t arenaBytes = 0;
   hepem::DevTables tables;
+  // L2 access-policy window over the arena for the batched forms' stage
+  // kernels (hepem_set_table_l2_window); tableWindow 0: none
+  size_t tableWindow = 0;
+  float tableHitRatio = 0.0f;
   // launch configuration of the batched form (hepem_set_launch_config / hepem_autotune)
   hepem::LaunchCfg launch = hepem::default_launch_cfg();
   // copy/compute pipeline of hepem_step_host (grow-only buffers, serialised by mu)
@@ -41,4 +45,12 @@ namespace hepem {
 int set_error(int code, const std::string& msg);
 bool valid_state(const hepem_track_state* s);
 bool valid_out(const hepem_step_out* r);
+// the context's table window, as options of a batched step
+inline void apply_table_window(const hepem_ctx* c, BatchOpts& o) {
+  o.tableBase = c->arena;
+  o.tableBytes = c->tableWindow;
+  o.tableHitRatio = c->tableHitRatio;
+}
+// set (enable != 0) or clear the window; see hepem_set_table_l2_window
+int set_table_window(hepem_ctx* c, int enable);
 }  // namespace hepem

@@ -45,6 +45,12 @@ struct BatchOpts {
   // of the mutable fields (immutable fields pointing to the input), see
   // mixed_pre_state_bytes; null for out-of-place steps
   const hepem_track_state* preState = nullptr;
+  // L2 access-policy window over the table arena (tableBytes 0: none): the
+  // stage kernels mark that fraction of their table gathers persisting, so the
+  // streamed track state does not evict the tables from L2
+  const void* tableBase = nullptr;
+  size_t tableBytes = 0;
+  float tableHitRatio = 0.0f;
 };
 // bytes of the pre-step copy of an in-place precision-form step (n tracks)
 size_t mixed_pre_state_bytes(int64_t n);

@@ -841,33 +841,57 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
   const int gS = (int)(tiles < (int64_t)sms * 8 ? tiles : (int64_t)sms * 8);
   sort_scatter_kernel<<<gS, 256, nkeys * sizeof(uint32_t), s>>>(T, n, o.active, in, w, ncb, neb);
   mark();
+  // the stage kernels: with a table window, launched with it as a launch
+  // attribute (the caller's stream is left as it is)
+  cudaError_t le = cudaSuccess;
+  auto stage = [&](StageFn f, int grid, int block) {
+    if (o.tableBytes == 0) {
+      f<<<grid, block, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+      return;
+    }
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
+    attr[0].val.accessPolicyWindow.base_ptr = const_cast<void*>(o.tableBase);
+    attr[0].val.accessPolicyWindow.num_bytes = o.tableBytes;
+    attr[0].val.accessPolicyWindow.hitRatio = o.tableHitRatio;
+    attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(grid);
+    lc.blockDim = dim3(block);
+    lc.dynamicSmemBytes = 0;
+    lc.stream = s;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    const cudaError_t x = cudaLaunchKernelEx(&lc, f, T, in, out, uniforms, nu, seed, res, w, counters);
+    if (le == cudaSuccess) le = x;
+  };
   for (int q = 0; q < kNumStageKernels; ++q) {
     const int b = bs_index(cfg.block[q]);
     if (o.mixed && K.mixed[b][q]) {
       // precision form: the FP32 kernel (its FP64 fallbacks run after the last stage)
       const int om = K.occMixed[b][q];
       const int pm = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < om ? cfg.ctasPerSM[q] : om;
-      K.mixed[b][q]<<<sms * pm, kBlockSizes[b], 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
-      if (q == kNumStageKernels - 1) {
-        K.final_[1]<<<sms * K.occFinal[1], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
-      }
+      stage(K.mixed[b][q], sms * pm, kBlockSizes[b]);
+      if (q == kNumStageKernels - 1) stage(K.final_[1], sms * K.occFinal[1], 256);
       mark();
       continue;
     }
     if (o.mixed && q == kNumStageKernels - 1) {
       const int occ = K.occ[b][q];
       const int per = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < occ ? cfg.ctasPerSM[q] : occ;
-      K.fn[b][q]<<<sms * per, kBlockSizes[b], 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
-      K.final_[1]<<<sms * K.occFinal[1], 256, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+      stage(K.fn[b][q], sms * per, kBlockSizes[b]);
+      stage(K.final_[1], sms * K.occFinal[1], 256);
       mark();
       continue;
     }
     const int occ = K.occ[b][q];
     const int per = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < occ ? cfg.ctasPerSM[q] : occ;
-    K.fn[b][q]<<<sms * per, kBlockSizes[b], 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+    stage(K.fn[b][q], sms * per, kBlockSizes[b]);
     mark();
   }
-  return cudaGetLastError();
+  const cudaError_t e2 = cudaGetLastError();
+  return le != cudaSuccess ? le : e2;
 }
 
 // ---- 4. per-model sampling (interaction unit tests and distribution checks) -------------

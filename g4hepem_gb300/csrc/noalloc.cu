@@ -82,6 +82,7 @@ extern "C" int hepem_step_batched_noalloc(const hepem_ctx* c, int64_t n, const h
   if (rc != HEPEM_OK) return rc;
   hepem::BatchOpts o;
   o.cfg = &c->launch;
+  hepem::apply_table_window(c, o);
   const cudaError_t e = hepem::launch_step_batched(c->tables, n, *in, *out, uniforms, nu, seed, *res, counters, ws,
                                                    (cudaStream_t)stream, c->sms, o);
   if (e != cudaSuccess)

@@ -299,6 +299,7 @@ cudaError_t hepem_server::iterate() {
     o.active = active;
     o.seeds = seeds;
     o.cfg = &ctx->launch;
+    hepem::apply_table_window(ctx, o);
     hepem_track_state preState;
     if (cfg.precision) {
       o.mixed = true;

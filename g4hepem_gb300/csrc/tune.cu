@@ -59,12 +59,53 @@ struct Scratch {
 
 }  // namespace
 
+namespace hepem {
+int set_table_window(hepem_ctx* c, int enable) {
+  c->tableWindow = 0;
+  c->tableHitRatio = 0.0f;
+  if (!enable) return HEPEM_OK;
+  int maxPersist = 0, maxWindow = 0;
+  if (cudaDeviceGetAttribute(&maxPersist, cudaDevAttrMaxPersistingL2CacheSize, c->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&maxWindow, cudaDevAttrMaxAccessPolicyWindowSize, c->device) != cudaSuccess) {
+    cudaGetLastError();
+    return HEPEM_OK;  // no window on this device
+  }
+  if (maxPersist <= 0 || maxWindow <= 0) return HEPEM_OK;
+  const size_t window = std::min(c->arenaBytes, (size_t)maxWindow);
+  const size_t want = std::min(window, (size_t)maxPersist);
+  // the persisting set-aside is a limit of this process's context: raise it
+  // (never lower what another context of the process asked for)
+  size_t have = 0;
+  if (cudaDeviceGetLimit(&have, cudaLimitPersistingL2CacheSize) != cudaSuccess) {
+    cudaGetLastError();
+    return HEPEM_OK;
+  }
+  if (have < want) {
+    if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) != cudaSuccess) {
+      cudaGetLastError();
+      return HEPEM_OK;
+    }
+    have = want;
+  }
+  c->tableWindow = window;
+  c->tableHitRatio = window > 0 ? (float)std::min(1.0, (double)have / (double)window) : 0.0f;
+  return HEPEM_OK;
+}
+}  // namespace hepem
+
 extern "C" {
 
 int hepem_get_launch_config(const hepem_ctx* c, hepem_launch_config* out) {
   if (!c || !out) return hepem::set_error(HEPEM_BAD_ARG, "null argument");
   to_public(c->launch, nullptr, out);
   return HEPEM_OK;
+}
+
+int hepem_set_table_l2_window(hepem_ctx* c, int enable, int64_t* window_bytes) {
+  if (!c) return hepem::set_error(HEPEM_BAD_ARG, "null context");
+  const int rc = hepem::set_table_window(c, enable);
+  if (window_bytes) *window_bytes = (int64_t)c->tableWindow;
+  return rc;
 }
 
 int hepem_set_launch_config(hepem_ctx* c, const hepem_launch_config* cfg) {
@@ -112,6 +153,7 @@ int hepem_autotune(hepem_ctx* c, int64_t n, const hepem_track_state* in, const d
     hepem::BatchOpts o;
     o.ev = sc.ev;
     o.cfg = &cfg;
+    hepem::apply_table_window(c, o);
     for (int k = 0; k < hepem::kNumStageKernels; ++k) stage[k] = 1e30f;
     *total = 1e30f;
     for (int r = 0; r < reps; ++r) {

@@ -92,7 +92,8 @@ EXPORTED = ["hepem_create", "hepem_create_from_file", "hepem_image_from_json", "
             "hepem_philox_uniform", "hepem_fill_uniforms", "hepem_profile_stages", "hepem_stage_times",
             "hepem_server_create", "hepem_server_capacity", "hepem_server_submit", "hepem_server_poll",
             "hepem_server_wait", "hepem_server_cancel", "hepem_server_get_stats", "hepem_server_reset_stats",
-            "hepem_server_destroy", "hepem_sample_model", "hepem_stack_secondaries", "hepem_woodcock_gamma", "hepem_get_launch_config", "hepem_set_launch_config", "hepem_autotune"]
+            "hepem_server_destroy", "hepem_sample_model", "hepem_stack_secondaries", "hepem_woodcock_gamma", "hepem_get_launch_config", "hepem_set_launch_config", "hepem_autotune",
+            "hepem_set_table_l2_window"]
 STATUS_CANCELLED, STATUS_TIMEOUT, STATUS_OOM_ADMISSION = 8, 5, 6
 
 
@@ -146,6 +147,7 @@ def lib():
                                         C.POINTER(C.c_int32)]
         L.hepem_get_launch_config.argtypes = [_vp, C.POINTER(LaunchConfig)]
         L.hepem_set_launch_config.argtypes = [_vp, C.POINTER(LaunchConfig)]
+        L.hepem_set_table_l2_window.argtypes = [_vp, C.c_int, C.POINTER(C.c_int64)]
         L.hepem_autotune.argtypes = [_vp, C.c_int64, C.POINTER(TrackState), _vp, C.c_int32, C.c_uint64, C.c_int,
                                      C.POINTER(LaunchConfig), _vp]
         L.hepem_server_create.argtypes = [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]
@@ -316,6 +318,13 @@ class Context:
             c.ctas_per_sm[k] = cfg["ctas_per_sm"][k]
         c.sort_energy_bins = cfg["sort_energy_bins"]
         check(lib().hepem_set_launch_config(self.h, C.byref(c)))
+
+    def set_table_l2_window(self, enable: bool) -> int:
+        """Sets or clears the L2 persisting window over the tables of the
+        batched forms' stage kernels; returns the window's size in bytes."""
+        w = C.c_int64(0)
+        check(lib().hepem_set_table_l2_window(self.h, int(bool(enable)), C.byref(w)))
+        return w.value
 
     def autotune(self, state_in: dict, uniforms, n_uniform: int, seed: int, apply=True, stream=None) -> dict:
         """Times the batched step on this batch under every launch candidate;

@@ -328,6 +328,20 @@ int  hepem_get_launch_config(const hepem_ctx* ctx, hepem_launch_config* out);
 /* cfg NULL restores the default (256 threads, occupancy grid, 32 bins).  Set
  * it before the context is shared between threads. */
 int  hepem_set_launch_config(hepem_ctx* ctx, const hepem_launch_config* cfg);
+/* L2 residency of the tables for the batched forms (hepem_step_batched,
+ * hepem_step_mixed, the host-buffer steps, the server): enable != 0 sets an
+ * L2 access-policy window over the context's table arena on every stage
+ * kernel launch (table gathers persisting, up to the device's persisting L2
+ * set-aside, which this raises for the process's context to the arena size
+ * at most), so the streamed track state does not evict the tables; 0 clears
+ * it.  New contexts start without it: on a GB300 it made the precision-form
+ * step 4-5% slower and left the FP64 batched step unchanged (the tables, a
+ * few hundred KB to a few MB, stay cached without it).  *window_bytes (may be NULL) = the window's size (0: none, e.g. the device
+ * has no persisting L2).  Results do not depend on it.  Set it before the
+ * context is shared between threads.  No reference counterpart: the
+ * reference reads its tables through the ordinary caches
+ * (G4HepEm/G4HepEmData/src/G4HepEmData.cc:78-101 copies them to the device). */
+int  hepem_set_table_l2_window(hepem_ctx* ctx, int enable, int64_t* window_bytes);
 /* Times the batched step on the caller's batch (device pointers; the batch is
  * read, outputs go to scratch) under every candidate configuration and returns
  * the fastest in `out`; apply != 0 also makes it the context's configuration.

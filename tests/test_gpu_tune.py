@@ -73,3 +73,35 @@ def test_bad_launch_config_is_rejected(native, gpu_ctx):
             ctx.set_launch_config(bad)
         assert e.value.code == 1
     assert ctx.launch_config() == good
+
+
+@pytest.mark.parametrize("form", ["batched", "mixed"])
+def test_table_l2_window_does_not_change_results(native, gpu_ctx, form):
+    """The L2 persisting window over the tables changes where the table lines
+    live, never a value: steps with and without it are bit-identical."""
+    import torch
+    ctx = gpu_ctx(T16)
+    n = 1 << 17
+    st = W.mixed_batch(n, n_couples=16, seed=73)
+    sin = native.state_to_torch(st)
+    u = native.fill_uniforms(sin["id"], NU, SEED)
+
+    def run():
+        sout = native.empty_state_torch(n)
+        res = native.alloc_out_torch(n)
+        cnt = torch.zeros(13, dtype=torch.int64, device="cuda")
+        ctx.step(sin, sout, u, NU, SEED, res, counters=cnt, form=form)
+        torch.cuda.synchronize()
+        return native.to_numpy(sout), native.to_numpy(res), cnt.cpu().numpy()
+
+    try:
+        on = ctx.set_table_l2_window(True)
+        assert on >= 0
+        with_w = run()
+        assert ctx.set_table_l2_window(False) == 0
+        without = run()
+    finally:
+        ctx.set_table_l2_window(False)
+    _same(with_w[0], without[0])
+    _same(with_w[1], without[1])
+    assert np.array_equal(with_w[2], without[2])
