@@ -54,13 +54,14 @@ static __device__ unsigned long long g_tripSites[4096];
 // Tracks are ordered by a sort key (particle, couple bin, energy bin) with a
 // counting sort, so that the warps of a stage hold tracks of one particle in
 // one material at similar energies and take the same branches (FP64 form; the
-// precision form sorts by particle only, see launch_step_batched).
+// precision form only splits e+- from gammas, see launch_step_batched).
 constexpr int kMaxSortEBins = 32;   // log2(E) bins over 1 keV - 100 TeV (the launch configuration picks 8..32)
 constexpr int kSortCoupleBins = 64; // couples beyond 64 share bins (imc % 64)
 constexpr int kMaxSortKeys = 3 * kSortCoupleBins * kMaxSortEBins;
 
 struct Work {
-  uint32_t* counts;               // [0..2] e-, e+, gamma tracks, [3..3+kNumQueues] queues + FP64 fallback
+  uint32_t* counts;               // [0..2] e-, e+, gamma tracks (oneChargedKey: e+-, 0, gamma),
+                                  // [3..3+kNumQueues] queues + FP64 fallback
   uint32_t* hist;                 // [kMaxSortKeys] tracks per sort key
   uint32_t* cursor;               // [kMaxSortKeys] scatter cursors
   int32_t* perm;                  // [n] valid tracks in sort-key order
@@ -72,6 +73,8 @@ struct Work {
   // in-place steps a copy that stage A takes of the e+- tracks it queues)
   hepem_track_state pre;
   bool preCopy;
+  // precision form: e- and e+ share one sort key (one list in batch order)
+  bool oneChargedKey;
 };
 
 __device__ __forceinline__ uint64_t key_of(const Work& w, int64_t i, uint64_t seed) {
@@ -129,6 +132,7 @@ hepem_track_state carve_pre_state(void* mem, int64_t n, const hepem_track_state&
 static Work carve(void* ws, int64_t n) {
   uint8_t* p = static_cast<uint8_t*>(ws);
   Work w;
+  w.oneChargedKey = false;
   w.counts = reinterpret_cast<uint32_t*>(p);
   p += rnd(64 * sizeof(uint32_t));
   w.hist = reinterpret_cast<uint32_t*>(p);
@@ -147,10 +151,13 @@ static Work carve(void* ws, int64_t n) {
   return w;
 }
 
-__device__ __forceinline__ int sort_key(int type, int imc, double e, int ncb, int neb) {
+__device__ __forceinline__ int sort_key(int type, int imc, double e, int ncb, int neb, bool oneChargedKey) {
   // Gammas keep their batch order (one key): their stage is light on FP64 and
   // latency bound, so coalesced loads matter more there than branch coherence.
   if (type == 2) return 2 * ncb * neb;
+  // the precision form (ncb = neb = 1) keeps e- and e+ in one list: the e+
+  // alone are too sparse in the batch for their loads to share sectors
+  if (oneChargedKey) return 0;
   // log2(1 keV / MeV) = -9.9658, log2(100 TeV / 1 keV) = 36.5412
   int eb = (int)((__log2f((float)e) + 9.965784f) * ((float)neb / 36.541209f));
   eb = eb < 0 ? 0 : (eb >= neb ? neb - 1 : eb);
@@ -187,7 +194,7 @@ __global__ void __launch_bounds__(256) sort_hist_kernel(const __grid_constant__ 
         res.n_sec[i] = 0;
         cnt.steps += 1;
       } else {
-        key = sort_key(type, imc, e, ncb, neb);
+        key = sort_key(type, imc, e, ncb, neb, w.oneChargedKey);
       }
     }
     // warp-aggregated: one shared atomic per distinct key in the warp
@@ -260,7 +267,7 @@ __global__ void __launch_bounds__(256) sort_scatter_kernel(const __grid_constant
         const int type = in.type[i];
         const int imc = in.imc[i];
         const double e = in.ekin[i];
-        if (!track_input_bad(T, type, imc, e)) key[it] = sort_key(type, imc, e, ncb, neb);
+        if (!track_input_bad(T, type, imc, e)) key[it] = sort_key(type, imc, e, ncb, neb, w.oneChargedKey);
       }
       // warp-aggregated: one shared atomic per distinct key in the warp
       const unsigned same = __match_any_sync(0xFFFFFFFFu, key[it]);
@@ -361,7 +368,7 @@ __global__ void __launch_bounds__(BS, MODE == kStageMixed ? HEPEM_MIXED_A_WARPS 
     bool tripped = false;
     if (j < total) {
       idx = w.perm[j];
-      const int type = j < nEm ? 0 : 1;
+      const int type = w.oneChargedKey ? (int)in.type[idx] : (j < nEm ? 0 : 1);
       Track t;
       Rng rng;
       load_track(in, idx, t, rng, uniforms, nu, key_of(w, idx, seed), type);
@@ -813,6 +820,7 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
   w.seeds = o.seeds;
   w.pre = in;
   w.preCopy = false;
+  w.oneChargedKey = o.mixed;
   if (o.mixed && o.preState) {
     w.pre = *o.preState;
     w.preCopy = true;
@@ -821,7 +829,9 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
   // couple and energy range; the precision form's stages are bound by the
   // latency of their state gathers and gain more from keeping each particle
   // list in batch order (neighbouring tracks share memory sectors: stage A
-  // of e+- takes 2.2x less time): it sorts by particle type only.
+  // of e+- takes 2.2x less time): it sorts into two lists only, e+- (e- and
+  // e+ together: the step 4% faster than with an e+ list of its own) and
+  // gammas.
   const int ncb = o.mixed ? 1 : (T.nCouples < kSortCoupleBins ? T.nCouples : kSortCoupleBins);
   const int neb = o.mixed ? 1 : cfg.sortEBins;
   const int nkeys = 3 * ncb * neb;
