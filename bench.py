@@ -56,6 +56,29 @@ CONFIG = {"workload": "full physics step (HowFar + Perform), 4,194,304 mixed tra
           "l2": "inputs larger than L2 (2.7 GB per step), no flush"}
 
 
+def shard_id0(rank: int, n: int) -> int:
+    """First track id of a rank's batch: ranks step disjoint id ranges of
+    independent tracks (replicas; no collective on the data path)."""
+    return rank * n
+
+
+def max_over_ranks(torch, value: float, ws: int) -> float:
+    """The largest per-rank time: the slowest replica sets the whole-job time
+    (on the device of the process group's backend: CUDA for NCCL)."""
+    if ws <= 1:
+        return value
+    dist = torch.distributed
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(ws: int, n: int, steps: int, seconds: float) -> float:
+    """Steps/s of all ranks together: every rank steps n tracks per step."""
+    return ws * n * steps / seconds
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -559,8 +582,8 @@ def run_reference(args, ws, rank):
         return
     from g4hepem_gb300 import workload as W
     threads = os.cpu_count() or 1
-    st = W.mixed_batch(N_TRACKS, seed=WORKLOAD_SEED)
-    n_sample = N_TRACKS
+    n_sample = args.n
+    st = W.mixed_batch(n_sample, seed=WORKLOAD_SEED)
     rates = []
     for i in range(args.warmup + args.steps):
         r, _ = cpu_port_rate(st, threads, n_sample)
@@ -585,7 +608,9 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--n", type=int, default=N_TRACKS)
+    # tracks per step and rank (--tracks: the same, for launches under torchrun,
+    # whose own parser would take --n for an abbreviation of its options)
+    ap.add_argument("--n", "--tracks", dest="n", type=int, default=N_TRACKS)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-c3", action="store_true")
@@ -613,7 +638,7 @@ def main():
 
     n = args.n
     ctx = N.Context(TABLE)
-    st_np = W.mixed_batch(n, seed=WORKLOAD_SEED, id0=rank * n)
+    st_np = W.mixed_batch(n, seed=WORKLOAD_SEED, id0=shard_id0(rank, n))
     sin = N.state_to_torch(st_np)
     sout = N.empty_state_torch(n)
     res = N.alloc_out_torch(n)
@@ -645,11 +670,7 @@ def main():
         ev1.record(stream)
         torch.cuda.synchronize()
         barrier()
-        t = ev0.elapsed_time(ev1)
-        if ws > 1:
-            tt = torch.tensor([t], device="cuda")
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            t = float(tt.item())
+        t = max_over_ranks(torch, ev0.elapsed_time(ev1), ws)
         return t / steps
 
     # the plain form (one thread per track) is the denominator of the target;
@@ -662,7 +683,7 @@ def main():
     time.sleep(0.3)
     ms_step = timed(args.form, args.steps)
     clk = clocks.stop()
-    value = ws * n / (ms_step / 1e3)
+    value = whole_job_rate(ws, n, 1, ms_step / 1e3)
     fcnt = torch.zeros(13, dtype=torch.int64, device="cuda")
     ctx.step(sin, sout, u, NU, SEED, res, counters=fcnt, form="mixed")
     torch.cuda.synchronize()
@@ -696,17 +717,13 @@ def main():
         t0 = time.perf_counter()
         for _ in range(ctx_steps):
             host_step()
-        t_e2e = time.perf_counter() - t0
-        if ws > 1:
-            tt = torch.tensor([t_e2e], device="cuda")
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            t_e2e = float(tt.item())
+        t_e2e = max_over_ranks(torch, time.perf_counter() - t0, ws)
         h2d = sum(v.numel() * v.element_size() for v in h_in.values())
         d2h = sum(h_out[k].numel() * h_out[k].element_size() for k in N.STATE_OUT_FIELDS)
         d2h += sum(v.numel() * v.element_size() for v in h_res.values())
         link = host_link_gbs(torch)
         moved = (h2d + d2h) / (t_e2e / ctx_steps) / 1e9
-        e2e = {"value": ws * n * ctx_steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+        e2e = {"value": whole_job_rate(ws, n, ctx_steps, t_e2e), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "steps": ctx_steps, "ms_per_step": 1e3 * t_e2e / ctx_steps,
                "host_link": {"achieved_gbs": moved, "measured_gbs": link, "frac": moved / link,
                              "note": "e2e is bound by the host<->device copies: measured = concurrent pinned "
@@ -789,10 +806,10 @@ def main():
                      "1e-5" if args.form == "mixed" else
                      "batched FP64 (hepem_step_batched): bit-identical to the plain FP64 path"),
             "fp64_fallback_per_step": fallback,
-            "plain_fp64": {"value": ws * n / (ms_plain / 1e3), "unit": UNIT, "ms_per_step": ms_plain,
+            "plain_fp64": {"value": whole_job_rate(ws, n, 1, ms_plain / 1e3), "unit": UNIT, "ms_per_step": ms_plain,
                            "entry_point": "hepem_step"},
             ("batched_fp64" if other == "batched" else "mixed"): {
-                "value": ws * n / (ms_other / 1e3), "unit": UNIT, "ms_per_step": ms_other,
+                "value": whole_job_rate(ws, n, 1, ms_other / 1e3), "unit": UNIT, "ms_per_step": ms_other,
                 "entry_point": "hepem_step_batched" if other == "batched" else "hepem_step_mixed"},
             "vs_plain_fp64": ms_plain / ms_step, "roofline": roof, "roofline_fp64": fp64, "roofline_fp32": fp32,
             "stage_ms": stages, "c1_lookup": c1, "c3_batching": c3, "c4_serving": c4, "c5_precision": c5,
