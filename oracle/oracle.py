@@ -273,6 +273,24 @@ class PortLib(_Lib):
             raise RuntimeError(f"step failed rc={rc}")
         return out_state, res
 
+    def step_mt_fn(self, state: dict, out_state: dict, res: dict, uniforms, n_uniform, seed, threads):
+        """A function of no arguments that steps `state` into `out_state` and
+        `res` on `threads` host threads; the argument structs are built once,
+        so a timing loop times the port's step alone."""
+        n = len(state["ekin"])
+        sin, sout, sres = make_state_struct(state), make_state_struct(out_state), make_out_struct(res)
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        up = _ptr(u, _dp)
+
+        def run():
+            rc = self.lib.port_step_mt(self.st, n, C.byref(sin), C.byref(sout), up, n_uniform, seed,
+                                       C.byref(sres), threads)
+            if rc != 0:
+                raise RuntimeError(f"step failed rc={rc}")
+
+        run.keep = (state, out_state, res, u, sin, sout, sres)  # the arrays stay alive with the function
+        return run
+
     def fill_uniforms(self, ids, n_uniform, seed):
         ids = np.ascontiguousarray(ids, dtype=np.int32)
         u = np.empty(len(ids) * n_uniform)
