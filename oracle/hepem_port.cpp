@@ -1804,6 +1804,74 @@ void port_electron_lookup(void* st, int64_t n, int is_pos, const double* ekin, c
   }
 }
 
+// Step-limit cross sections of HowFarToDiscreteInteraction and the transport
+// mean free path (G4HepEmElectronManager.icc:534-599), per (E, couple).
+void port_electron_xs_stepping(void* st, int64_t n, int is_pos, const double* ekin, const int32_t* imc,
+                               double* xi, double* xb, double* xa, double* xn, double* tr) {
+  const port::State& S = *static_cast<port::State*>(st);
+  const port::ElData& d = S.el[is_pos ? 1 : 0];
+  using St = port::Step;
+  for (int64_t i = 0; i < n; ++i) {
+    const double e = ekin[i], le = port::vlog(e);
+    const int imat = S.couples[imc[i]].mat;
+    xi[i] = St::restMacXSStepping(d, imc[i], e, le, true);
+    xb[i] = St::restMacXSStepping(d, imc[i], e, le, false);
+    xa[i] = is_pos ? St::annihXS(0.8 * e, S.mats[imat].elDensity) : 0.0;
+    xn[i] = St::nucMacXS(d, imat, e, le);
+    tr[i] = St::transportMFP(d, imat, e, le);
+  }
+}
+
+// Target element of Seltzer-Berger (is_sb) or relativistic brem for a given
+// uniform (G4HepEmElectronInteractionBrem.icc SelectTargetAtom); 0 for
+// single-element materials, where the reference draws nothing.
+void port_brem_select_target(void* st, int64_t n, int is_pos, int is_sb, const double* ekin, const int32_t* imc,
+                             const double* urnd, int32_t* elem) {
+  const port::State& S = *static_cast<port::State*>(st);
+  for (int64_t i = 0; i < n; ++i) {
+    if (S.mats[S.couples[imc[i]].mat].elems.size() < 2) { elem[i] = 0; continue; }
+    port::Rng rng{&urnd[i], 1, 0, 0, 0, false, false, 0.0};
+    port::Step P(S, rng);
+    P.t.imc = imc[i];
+    P.t.charge = is_pos ? 1.0 : -1.0;
+    elem[i] = P.selectBremTarget(ekin[i], port::vlog(ekin[i]), urnd[i], is_sb != 0);
+  }
+}
+
+// Gamma total macroscopic cross section and the interaction chosen with a
+// given uniform (G4HepEmGammaManager.icc:108-219, the pair the reference's
+// gamma cross-section test checks); PE cross section when the winner is PE.
+void port_gamma_xs(void* st, int64_t n, const double* ekin, const int32_t* imc, const double* urnd,
+                   double* xs_tot, double* xs_pe, int32_t* winner) {
+  const port::State& S = *static_cast<port::State*>(st);
+  for (int64_t i = 0; i < n; ++i) {
+    port::Rng rng{&urnd[i], 1, 0, 0, 0, false, false, 0.0};
+    port::Step P(S, rng);
+    P.t.imc = imc[i];
+    P.t.setE(ekin[i]);
+    const double tot = P.gammaTotalXS();
+    xs_tot[i] = tot;
+    P.t.mfp[0] = tot > 0. ? 1. / tot : port::kLarge;
+    P.gammaSelect();
+    winner[i] = P.t.winner;
+    xs_pe[i] = P.t.winner == 2 ? P.t.peXS : 0.0;
+  }
+}
+
+// Target element of gamma conversion for a given uniform
+// (G4HepEmGammaInteractionConversion.icc SelectTargetAtom).
+void port_conv_select_target(void* st, int64_t n, const double* ekin, const int32_t* imc, const double* urnd,
+                             int32_t* elem) {
+  const port::State& S = *static_cast<port::State*>(st);
+  for (int64_t i = 0; i < n; ++i) {
+    const int imat = S.couples[imc[i]].mat;
+    if (S.mats[imat].elems.size() < 2) { elem[i] = 0; continue; }
+    port::Rng rng{&urnd[i], 1, 0, 0, 0, false, false, 0.0};
+    port::Step P(S, rng);
+    elem[i] = P.convTarget(imat, ekin[i], port::vlog(ekin[i]), urnd[i]);
+  }
+}
+
 int port_step(void* st, int64_t n, const hepem_track_state* in, hepem_track_state* out, const double* u,
               int32_t nu, uint64_t seed, hepem_step_out* res) {
   return port::step_range(*static_cast<port::State*>(st), 0, n, in, out, u, nu, seed, res);

@@ -112,6 +112,11 @@ class _Lib:
         getattr(L, p + "step").argtypes = [C.c_void_p, C.c_int64, C.POINTER(TrackState), C.POINTER(TrackState),
                                            _dp, C.c_int32, C.c_uint64, C.POINTER(StepOut)]
         getattr(L, p + "step").restype = C.c_int
+        getattr(L, p + "electron_xs_stepping").argtypes = [C.c_void_p, C.c_int64, C.c_int, _dp, _ip] + [_dp] * 5
+        getattr(L, p + "brem_select_target").argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, _dp, _ip, _dp,
+                                                         _ip]
+        getattr(L, p + "gamma_xs").argtypes = [C.c_void_p, C.c_int64, _dp, _ip, _dp, _dp, _dp, _ip]
+        getattr(L, p + "conv_select_target").argtypes = [C.c_void_p, C.c_int64, _dp, _ip, _dp, _ip]
         self.st = None
 
     def _f(self, name):
@@ -137,6 +142,46 @@ class _Lib:
                                    *[_ptr(o, _dp) for o in outs])
         return dict(zip(["xs_ioni", "xs_brem", "dedx", "range", "invrange_half"], outs))
 
+    def electron_xs_stepping(self, ekin, imc, positron=False):
+        n = len(ekin)
+        ekin = np.ascontiguousarray(ekin, dtype=np.float64)
+        imc = np.ascontiguousarray(imc, dtype=np.int32)
+        outs = [np.empty(n) for _ in range(5)]
+        self._f("electron_xs_stepping")(self.st, n, int(positron), _ptr(ekin, _dp), _ptr(imc, _ip),
+                                        *[_ptr(o, _dp) for o in outs])
+        return dict(zip(["xs_ioni", "xs_brem", "xs_annih", "xs_nuc", "tr_mfp"], outs))
+
+    def brem_select_target(self, ekin, imc, urnd, positron=False, sb=True):
+        n = len(ekin)
+        ekin = np.ascontiguousarray(ekin, dtype=np.float64)
+        imc = np.ascontiguousarray(imc, dtype=np.int32)
+        urnd = np.ascontiguousarray(urnd, dtype=np.float64)
+        out = np.empty(n, dtype=np.int32)
+        self._f("brem_select_target")(self.st, n, int(positron), int(sb), _ptr(ekin, _dp), _ptr(imc, _ip),
+                                      _ptr(urnd, _dp), _ptr(out, _ip))
+        return out
+
+    def gamma_xs(self, ekin, imc, urnd):
+        n = len(ekin)
+        ekin = np.ascontiguousarray(ekin, dtype=np.float64)
+        imc = np.ascontiguousarray(imc, dtype=np.int32)
+        urnd = np.ascontiguousarray(urnd, dtype=np.float64)
+        tot, pe = np.empty(n), np.empty(n)
+        win = np.empty(n, dtype=np.int32)
+        self._f("gamma_xs")(self.st, n, _ptr(ekin, _dp), _ptr(imc, _ip), _ptr(urnd, _dp), _ptr(tot, _dp),
+                            _ptr(pe, _dp), _ptr(win, _ip))
+        return dict(xs_tot=tot, xs_pe=pe, winner=win)
+
+    def conv_select_target(self, ekin, imc, urnd):
+        n = len(ekin)
+        ekin = np.ascontiguousarray(ekin, dtype=np.float64)
+        imc = np.ascontiguousarray(imc, dtype=np.int32)
+        urnd = np.ascontiguousarray(urnd, dtype=np.float64)
+        out = np.empty(n, dtype=np.int32)
+        self._f("conv_select_target")(self.st, n, _ptr(ekin, _dp), _ptr(imc, _ip), _ptr(urnd, _dp),
+                                      _ptr(out, _ip))
+        return out
+
     def step(self, state: dict, uniforms: np.ndarray, n_uniform: int, seed: int, in_place=False):
         n = len(state["ekin"])
         out_state = state if in_place else copy_state(state)
@@ -161,10 +206,6 @@ class RefLib(_Lib):
         L.ref_vdt_log.argtypes = [C.c_int64, _dp, _dp]
         L.ref_vdt_exp.argtypes = [C.c_int64, _dp, _dp]
         L.ref_vdt_pow.argtypes = [C.c_int64, _dp, _dp, _dp]
-        L.ref_electron_xs_stepping.argtypes = [C.c_void_p, C.c_int64, C.c_int, _dp, _ip] + [_dp] * 5
-        L.ref_brem_select_target.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_int, _dp, _ip, _dp, _ip]
-        L.ref_gamma_xs.argtypes = [C.c_void_p, C.c_int64, _dp, _ip, _dp, _dp, _dp, _ip]
-        L.ref_conv_select_target.argtypes = [C.c_void_p, C.c_int64, _dp, _ip, _dp, _ip]
         L.ref_num_couples.argtypes = [C.c_void_p]
 
     def vdt_log(self, x):
@@ -178,47 +219,6 @@ class RefLib(_Lib):
         y = np.empty_like(x)
         self.lib.ref_vdt_exp(len(x), _ptr(x, _dp), _ptr(y, _dp))
         return y
-
-    def electron_xs_stepping(self, ekin, imc, positron=False):
-        n = len(ekin)
-        ekin = np.ascontiguousarray(ekin, dtype=np.float64)
-        imc = np.ascontiguousarray(imc, dtype=np.int32)
-        outs = [np.empty(n) for _ in range(5)]
-        self.lib.ref_electron_xs_stepping(self.st, n, int(positron), _ptr(ekin, _dp), _ptr(imc, _ip),
-                                          *[_ptr(o, _dp) for o in outs])
-        return dict(zip(["xs_ioni", "xs_brem", "xs_annih", "xs_nuc", "tr_mfp"], outs))
-
-    def brem_select_target(self, ekin, imc, urnd, positron=False, sb=True):
-        n = len(ekin)
-        ekin = np.ascontiguousarray(ekin, dtype=np.float64)
-        imc = np.ascontiguousarray(imc, dtype=np.int32)
-        urnd = np.ascontiguousarray(urnd, dtype=np.float64)
-        out = np.empty(n, dtype=np.int32)
-        self.lib.ref_brem_select_target(self.st, n, int(positron), int(sb), _ptr(ekin, _dp), _ptr(imc, _ip),
-                                        _ptr(urnd, _dp), _ptr(out, _ip))
-        return out
-
-    def gamma_xs(self, ekin, imc, urnd):
-        n = len(ekin)
-        ekin = np.ascontiguousarray(ekin, dtype=np.float64)
-        imc = np.ascontiguousarray(imc, dtype=np.int32)
-        urnd = np.ascontiguousarray(urnd, dtype=np.float64)
-        tot, pe = np.empty(n), np.empty(n)
-        win = np.empty(n, dtype=np.int32)
-        self.lib.ref_gamma_xs(self.st, n, _ptr(ekin, _dp), _ptr(imc, _ip), _ptr(urnd, _dp), _ptr(tot, _dp),
-                              _ptr(pe, _dp), _ptr(win, _ip))
-        return dict(xs_tot=tot, xs_pe=pe, winner=win)
-
-    def conv_select_target(self, ekin, imc, urnd):
-        n = len(ekin)
-        ekin = np.ascontiguousarray(ekin, dtype=np.float64)
-        imc = np.ascontiguousarray(imc, dtype=np.int32)
-        urnd = np.ascontiguousarray(urnd, dtype=np.float64)
-        out = np.empty(n, dtype=np.int32)
-        self.lib.ref_conv_select_target(self.st, n, _ptr(ekin, _dp), _ptr(imc, _ip), _ptr(urnd, _dp),
-                                        _ptr(out, _ip))
-        return out
-
 
 class PortLib(_Lib):
     prefix = "port_"

@@ -7,8 +7,9 @@ It builds oracle/_ref/libhepem_ref.so from the reference sources (oracle/Makefil
 loads the committed synthetic tables through the reference's own
 G4HepEmStateFromJson, and records inputs and outputs of the reference
 functions: VDT log/exp, the electron table lookups, step-limit cross
-sections, target-element selectors, gamma cross sections and interaction
-selection, and full HowFar+Perform steps (fresh tracks, a second step that
+sections, target-element selectors (brem SB/RB for e- and e+, conversion),
+gamma cross sections and interaction selection, on three and on sixteen
+couples, and full HowFar+Perform steps (fresh tracks, a second step that
 carries MSC/Gauss/RNG state, boundary and safety variants, and a 16-couple
 table with two regions).  Uniform streams are not stored: they are the Philox
 streams of the C-ABI contract and are regenerated from (seed, id).
@@ -85,7 +86,7 @@ def main():
         for k, v in ref.electron_lookup(ekin, imc, bool(pos)).items():
             d[f"p{pos}_{k}"] = v
         for k, v in ref.electron_xs_stepping(ekin, imc, bool(pos)).items():
-            d[f"p{pos}_{k}"] = v
+            d[f"p{pos}_step_{k}"] = v
     save("lookup_3couples.npz", **d)
 
     # selectors and gamma interaction choice
@@ -124,6 +125,24 @@ def main():
     ekin, imc = W.electron_lookup_batch(4096, n_couples=16, seed=12)
     lk = {f"l_{k}": v for k, v in ref16.electron_lookup(ekin, imc).items()}
     save("step_16couples.npz", seed=np.array([SEED + 3]), nu=np.array([NU]), l_ekin=ekin, l_imc=imc, **lk, **d4)
+
+    # selectors, gamma cross sections and step-limit cross sections over the
+    # sixteen couples (1-4 elements each, random couple per input)
+    rr = np.random.default_rng(6)
+    n16 = 16384
+    eg = np.exp(rr.uniform(np.log(1e-3), np.log(1e8), n16))
+    es = np.exp(rr.uniform(np.log(0.1), np.log(1e8), n16))
+    ic = rr.integers(0, 16, n16).astype(np.int32)
+    u = rr.random(n16)
+    gx = ref16.gamma_xs(eg, ic, u)
+    d = dict(g_ekin=eg, s_ekin=es, imc=ic, u=u, g_xs_tot=gx["xs_tot"], g_xs_pe=gx["xs_pe"],
+             g_winner=gx["winner"], conv=ref16.conv_select_target(es, ic, u))
+    for pos in (0, 1):
+        for sb in (0, 1):
+            d[f"brem_p{pos}_sb{sb}"] = ref16.brem_select_target(es, ic, u, bool(pos), bool(sb))
+        for k, v in ref16.electron_xs_stepping(es, ic, bool(pos)).items():
+            d[f"p{pos}_step_{k}"] = v
+    save("selectors_16couples.npz", **d)
 
 
 if __name__ == "__main__":

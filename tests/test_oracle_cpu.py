@@ -74,6 +74,46 @@ def test_port_steps_match_reference_golden(port, prefix, table):
     assert ok, rep
 
 
+def test_port_step_limit_cross_sections_match_reference_golden(port):
+    """The HowFarToDiscreteInteraction inputs: restricted ioni and brem cross
+    sections for stepping, e+ annihilation, e-nuclear and the transport mean
+    free path (the reference's TestXSectionData quantities)."""
+    for name, table, ekin_key in (("lookup_3couples.npz", T3, "ekin"), ("selectors_16couples.npz", T16, "s_ekin")):
+        g = load_golden(name)
+        p = port(table)
+        for pos in (0, 1):
+            got = p.electron_xs_stepping(g[ekin_key], g["imc"], bool(pos))
+            for k, v in got.items():
+                assert np.array_equal(v, g[f"p{pos}_step_{k}"]), (name, pos, k)
+
+
+@pytest.mark.parametrize("name,table", [("selectors_3couples.npz", T3), ("selectors_16couples.npz", T16)])
+def test_port_selectors_match_reference_golden(port, name, table):
+    """Target-element selection for Seltzer-Berger and relativistic brem (e-
+    and e+) and for conversion, and the gamma total cross section with the
+    interaction it selects for a given uniform (the reference's
+    TestElemSelectorData, TestGammaElemSelectorData and TestGammaXSectionData
+    quantities), bit for bit."""
+    g = load_golden(name)
+    p = port(table)
+    if "u" in g:
+        g_imc, s_imc, gu, su = g["imc"], g["imc"], g["u"], g["u"]
+    else:
+        g_imc, s_imc, gu, su = g["g_imc"], np.zeros(len(g["s_ekin"]), np.int32), g["g_u"], g["s_u"]
+    gx = p.gamma_xs(g["g_ekin"], g_imc, gu)
+    assert np.array_equal(gx["xs_tot"], g["g_xs_tot"])
+    assert np.array_equal(gx["winner"], g["g_winner"])
+    assert np.array_equal(gx["xs_pe"], g["g_xs_pe"])
+    assert np.array_equal(p.conv_select_target(g["s_ekin"], s_imc, su), g["conv"])
+    for pos in (0, 1):
+        for sb in (0, 1):
+            got = p.brem_select_target(g["s_ekin"], s_imc, su, bool(pos), bool(sb))
+            assert np.array_equal(got, g[f"brem_p{pos}_sb{sb}"]), (pos, sb)
+    # every branch is exercised: each interaction and several target elements
+    assert set(np.unique(g["g_winner"])) >= {0, 1, 2}
+    assert len(np.unique(g["conv"])) >= 2
+
+
 def test_golden_steps_conserve_energy():
     g = load_golden("step_3couples.npz")
     for prefix in ("s1_", "w_"):
