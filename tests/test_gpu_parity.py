@@ -105,6 +105,36 @@ def test_step_matches_port_200k(native, gpu_ctx, port, table, nc):
     assert cnt[3] == int(res["n_sec"].astype(np.int64).sum())
 
 
+@pytest.mark.parametrize("form", ["plain", "batched", "mixed"])
+def test_ragged_and_empty_batches(native, gpu_ctx, port, form):
+    """Batch sizes that fill no warp, block or sort tile evenly (1 to 2,049
+    tracks), and the empty batch, through every device form: the FP64 forms
+    bit-exact with the port, the precision form with the port's discrete
+    outcomes and energies within 1e-5."""
+    ctx = gpu_ctx(T3)
+    p = port(T3)
+    for n in (1, 3, 31, 33, 257, 2049):
+        st = W.mixed_batch(n, seed=100 + n)
+        u = p.fill_uniforms(st["id"], 64, 77)
+        ref_out, ref_res = p.step(st, u, 64, 77)
+        out, res, cnt = gpu_step(native, ctx, st, 77, 64, form=form)
+        if form == "mixed":
+            for f in ("rng_cursor", "gauss_valid", "msc_first_step"):
+                assert np.array_equal(ref_out[f], out[f]), (n, f)
+            for f in ("winner", "n_sec", "flags"):
+                assert np.array_equal(ref_res[f], res[f]), (n, f)
+            a, b = ref_out["ekin"], out["ekin"]
+            r = np.abs(a - b) / np.maximum(np.abs(a), 1e-300)
+            assert np.all((a == b) | (r <= 1e-5)), (n, float(r.max()))
+        else:
+            rep, ok = compare_steps(ref_out, ref_res, out, res)
+            assert ok, (n, rep)
+        assert int(cnt[0]) == n
+    st = W.mixed_batch(0, seed=1)
+    out, res, cnt = gpu_step(native, ctx, st, 77, 64, form=form)
+    assert len(out["ekin"]) == 0 and len(res["winner"]) == 0 and int(cnt[0]) == 0
+
+
 def test_step_wide_energy_range_matches_port(native, gpu_ctx, port):
     """1 keV - 100 TeV: LPM brem/pair, RB brem, tracking cuts, at-rest annihilation."""
     st = W.mixed_batch(100000, seed=5, emin=1e-3, emax=1e8, frac=(0.4, 0.3, 0.3))
