@@ -172,6 +172,7 @@ int hepem_destroy(hepem_ctx* c) {
     if (sl.s) cudaStreamDestroy(sl.s);
   }
   if (c->start) cudaEventDestroy(c->start);
+  if (c->splitBuf) cudaFree(c->splitBuf);
   if (c->stageEvReady)
     for (auto& e2 : c->stageEv) cudaEventDestroy(e2);
   delete c;
@@ -446,6 +447,171 @@ int hepem_step_host_mixed(const hepem_ctx* c, int64_t n, const hepem_track_state
                           const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res,
                           hepem_step_counters* counters, void* stream) {
   return step_host(c, n, in, out, uniforms, nu, seed, res, counters, stream, true);
+}
+
+// ---- HowFar and Perform as two calls ----------------------------------------------------
+int64_t hepem_step_limit_bytes(int64_t n) { return n < 0 ? 0 : (int64_t)hepem::limits_bytes(n); }
+
+namespace {
+// one phase of the split step over device buffers (in == out for an in-place Perform)
+int split_device(const hepem_ctx* c, int form, int phase, int64_t n, const hepem_track_state* in,
+                 hepem_track_state* out, double* gstep, void* limits, const double* uniforms, int32_t nu,
+                 uint64_t seed, hepem_step_out* res, hepem_step_counters* counters, cudaStream_t s) {
+  const hepem::Limits L = hepem::carve_limits(limits, n);
+  if (form == HEPEM_FORM_PLAIN) {
+    if (phase == hepem::kPhaseHowFar)
+      HEPEM_CUDA(hepem::launch_howfar(c->tables, n, *in, uniforms, nu, seed, gstep, L, counters, s, c->sms));
+    else
+      HEPEM_CUDA(hepem::launch_perform(c->tables, n, *in, *out, gstep, L, uniforms, nu, seed, *res, counters, s,
+                                       c->sms));
+    return HEPEM_OK;
+  }
+  const bool mixed = form == HEPEM_FORM_MIXED;
+  const bool preCopy = mixed && phase == hepem::kPhasePerform && in->ekin == out->ekin;
+  const size_t wsBytes = hepem::batched_workspace_bytes(n);
+  void* ws = nullptr;
+  HEPEM_CUDA(cudaMallocAsync(&ws, wsBytes + (preCopy ? hepem::mixed_pre_state_bytes(n) : 0), s));
+  hepem::BatchOpts o;
+  o.ev = c->profile ? const_cast<cudaEvent_t*>(c->stageEv) : nullptr;
+  o.cfg = &c->launch;
+  o.mixed = mixed;
+  o.phase = phase;
+  o.gstep = gstep;
+  o.limits = L;
+  hepem::apply_table_window(c, o);
+  hepem_track_state pre;
+  if (preCopy) {
+    pre = hepem::carve_pre_state(static_cast<uint8_t*>(ws) + wsBytes, n, *in);
+    o.preState = &pre;
+  }
+  // HowFar writes no track state and no results: `out` and `res` are not used
+  hepem_step_out none;
+  memset(&none, 0, sizeof(none));
+  cudaError_t e = hepem::launch_step_batched(c->tables, n, *in, out ? *out : *in, uniforms, nu, seed,
+                                             res ? *res : none, counters, ws, s, c->sms, o);
+  cudaError_t f = cudaFreeAsync(ws, s);
+  if (e != cudaSuccess) return cuda_fail(e, "split step launch");
+  if (f != cudaSuccess) return cuda_fail(f, "cudaFreeAsync");
+  return HEPEM_OK;
+}
+
+int split_check(const hepem_ctx* c, int form, int64_t n, int32_t nu, const hepem_track_state* in,
+                const hepem_track_state* out, const void* gstep, const void* limits, const double* uniforms,
+                const hepem_step_out* res, bool perform) {
+  if (!c || n < 0 || nu < 0) return fail(HEPEM_BAD_ARG, "bad context or size");
+  if (form != HEPEM_FORM_PLAIN && form != HEPEM_FORM_BATCHED && form != HEPEM_FORM_MIXED)
+    return fail(HEPEM_BAD_ARG, "form must be HEPEM_FORM_PLAIN, HEPEM_FORM_BATCHED or HEPEM_FORM_MIXED");
+  if (n == 0) return HEPEM_OK;
+  if (!state_ok(in) || (perform && (!state_ok(out) || !out_ok(res))) || !gstep || !limits ||
+      (nu > 0 && !uniforms))
+    return fail(HEPEM_BAD_ARG, "null array in track batch");
+  if (n > (int64_t)INT32_MAX * 2 / 3) return fail(HEPEM_BAD_ARG, "batch too large");
+  return HEPEM_OK;
+}
+
+// host-buffer split step: inputs to one device buffer, the phase, outputs back
+int split_host(const hepem_ctx* cc, int form, int phase, int64_t n, const hepem_track_state* in,
+               hepem_track_state* out, double* gstep, void* limits, const double* uniforms, int32_t nu,
+               uint64_t seed, hepem_step_out* res, hepem_step_counters* counters, cudaStream_t s) {
+  hepem_ctx* c = const_cast<hepem_ctx*>(cc);
+  std::lock_guard<std::mutex> lock(c->mu);
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t m = (size_t)n;
+  const size_t limBytes = hepem::limits_bytes(n);
+  size_t need = al(sizeof(double) * m) + al(limBytes) + al(sizeof(double) * m * nu) + al(sizeof(hepem_step_counters));
+  for (size_t b : kStateSizes) need += al(b * m);
+  if (phase == hepem::kPhasePerform)
+    for (size_t b : kOutSizes) need += al(b * m);
+  if (need > c->splitBytes) {
+    if (c->splitBuf) HEPEM_CUDA(cudaFree(c->splitBuf));
+    c->splitBuf = nullptr;
+    c->splitBytes = 0;
+    HEPEM_CUDA(cudaMalloc(&c->splitBuf, need));
+    c->splitBytes = need;
+  }
+  uint8_t* p = static_cast<uint8_t*>(c->splitBuf);
+  double* dg = reinterpret_cast<double*>(p);
+  p += al(sizeof(double) * m);
+  void* dlim = p;
+  p += al(limBytes);
+  double* du = reinterpret_cast<double*>(p);
+  p += al(sizeof(double) * m * nu);
+  hepem_step_counters* dcnt = reinterpret_cast<hepem_step_counters*>(p);
+  p += al(sizeof(hepem_step_counters));
+  void* dstate[20];
+  void* dout[14] = {};
+  for (int k = 0; k < 20; ++k) { dstate[k] = p; p += al(kStateSizes[k] * m); }
+  if (phase == hepem::kPhasePerform)
+    for (int k = 0; k < 14; ++k) { dout[k] = p; p += al(kOutSizes[k] * m); }
+  void* const* hin = reinterpret_cast<void* const*>(in);
+  for (int k = 0; k < 20; ++k)
+    HEPEM_CUDA(cudaMemcpyAsync(dstate[k], hin[k], kStateSizes[k] * m, cudaMemcpyHostToDevice, s));
+  if (nu > 0) HEPEM_CUDA(cudaMemcpyAsync(du, uniforms, sizeof(double) * m * nu, cudaMemcpyHostToDevice, s));
+  if (counters) HEPEM_CUDA(cudaMemsetAsync(dcnt, 0, sizeof(*dcnt), s));
+  hepem_track_state ds;
+  hepem_step_out dr;
+  memcpy(&ds, dstate, sizeof(ds));
+  memcpy(&dr, dout, sizeof(dr));
+  if (phase == hepem::kPhasePerform) {
+    HEPEM_CUDA(cudaMemcpyAsync(dg, gstep, sizeof(double) * m, cudaMemcpyHostToDevice, s));
+    HEPEM_CUDA(cudaMemcpyAsync(dlim, limits, limBytes, cudaMemcpyHostToDevice, s));
+  }
+  const int rc = split_device(c, form, phase, n, &ds, phase == hepem::kPhasePerform ? &ds : nullptr, dg, dlim,
+                              nu > 0 ? du : nullptr, nu, seed, phase == hepem::kPhasePerform ? &dr : nullptr,
+                              counters ? dcnt : nullptr, s);
+  if (rc != HEPEM_OK) return rc;
+  if (phase == hepem::kPhaseHowFar) {
+    HEPEM_CUDA(cudaMemcpyAsync(gstep, dg, sizeof(double) * m, cudaMemcpyDeviceToHost, s));
+    HEPEM_CUDA(cudaMemcpyAsync(limits, dlim, limBytes, cudaMemcpyDeviceToHost, s));
+  } else {
+    void* const* hout = reinterpret_cast<void* const*>(out);
+    void* const* hres = reinterpret_cast<void* const*>(res);
+    for (int k = 0; k < 20; ++k)
+      HEPEM_CUDA(cudaMemcpyAsync(hout[k], dstate[k], kStateSizes[k] * m, cudaMemcpyDeviceToHost, s));
+    for (int k = 0; k < 14; ++k)
+      HEPEM_CUDA(cudaMemcpyAsync(hres[k], dout[k], kOutSizes[k] * m, cudaMemcpyDeviceToHost, s));
+  }
+  if (counters) HEPEM_CUDA(cudaMemcpyAsync(counters, dcnt, sizeof(*counters), cudaMemcpyDeviceToHost, s));
+  HEPEM_CUDA(cudaStreamSynchronize(s));
+  return HEPEM_OK;
+}
+}  // namespace
+
+int hepem_howfar(const hepem_ctx* c, int form, int64_t n, const hepem_track_state* tracks, const double* uniforms,
+                 int32_t nu, uint64_t seed, double* gstep, void* limits, hepem_step_counters* counters,
+                 void* stream) {
+  const int rc = split_check(c, form, n, nu, tracks, nullptr, gstep, limits, uniforms, nullptr, false);
+  if (rc != HEPEM_OK || n == 0) return rc;
+  return split_device(c, form, hepem::kPhaseHowFar, n, tracks, nullptr, gstep, limits, uniforms, nu, seed, nullptr,
+                      counters, (cudaStream_t)stream);
+}
+
+int hepem_perform(const hepem_ctx* c, int form, int64_t n, const hepem_track_state* in, hepem_track_state* out,
+                  const double* gstep, const void* limits, const double* uniforms, int32_t nu, uint64_t seed,
+                  hepem_step_out* res, hepem_step_counters* counters, void* stream) {
+  const int rc = split_check(c, form, n, nu, in, out, gstep, limits, uniforms, res, true);
+  if (rc != HEPEM_OK || n == 0) return rc;
+  return split_device(c, form, hepem::kPhasePerform, n, in, out, const_cast<double*>(gstep),
+                      const_cast<void*>(limits), uniforms, nu, seed, res, counters, (cudaStream_t)stream);
+}
+
+int hepem_howfar_host(const hepem_ctx* c, int form, int64_t n, const hepem_track_state* tracks,
+                      const double* uniforms, int32_t nu, uint64_t seed, double* gstep, void* limits,
+                      hepem_step_counters* counters, void* stream) {
+  const int rc = split_check(c, form, n, nu, tracks, nullptr, gstep, limits, uniforms, nullptr, false);
+  if (rc != HEPEM_OK || n == 0) return rc;
+  return split_host(c, form, hepem::kPhaseHowFar, n, tracks, nullptr, gstep, limits, uniforms, nu, seed, nullptr,
+                    counters, (cudaStream_t)stream);
+}
+
+int hepem_perform_host(const hepem_ctx* c, int form, int64_t n, const hepem_track_state* in,
+                       hepem_track_state* out, const double* gstep, const void* limits, const double* uniforms,
+                       int32_t nu, uint64_t seed, hepem_step_out* res, hepem_step_counters* counters,
+                       void* stream) {
+  const int rc = split_check(c, form, n, nu, in, out, gstep, limits, uniforms, res, true);
+  if (rc != HEPEM_OK || n == 0) return rc;
+  return split_host(c, form, hepem::kPhasePerform, n, in, out, const_cast<double*>(gstep),
+                    const_cast<void*>(limits), uniforms, nu, seed, res, counters, (cudaStream_t)stream);
 }
 
 int hepem_profile_stages(hepem_ctx* c, int enable) {

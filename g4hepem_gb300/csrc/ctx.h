@@ -34,6 +34,10 @@ struct hepem_ctx {
   Slot slot[kSlots];
   cudaEvent_t start = nullptr;
   bool slotsReady = false;
+  // device buffer of the host-buffer split step (hepem_howfar_host /
+  // hepem_perform_host; grow-only, serialised by mu)
+  void* splitBuf = nullptr;
+  size_t splitBytes = 0;
   // per-stage timing of the batched form (hepem_profile_stages)
   bool profile = false;
   bool stageEvReady = false;

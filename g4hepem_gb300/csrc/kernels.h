@@ -10,6 +10,75 @@
 
 namespace hepem {
 
+// ---- the step-limit record between hepem_howfar and hepem_perform -------------------
+// What the reference keeps in the thread-local primary track between
+// G4HepEm{Electron,Gamma}Manager::HowFar and ::Perform (G4HepEmTrack,
+// G4HepEmElectronTrack, G4HepEmMSCTrackData, G4HepEmGammaTrack fields and the
+// RNG state after HowFar), SoA over n tracks in one caller buffer of
+// limits_bytes(n) bytes.  HowFar leaves the caller's track state unchanged and
+// writes everything it changed here; Perform reads the state (with the
+// direction and boundary status transport left) and this record.
+enum {
+  kLProposed = 0,  // the geometrical step HowFar proposed
+  kLPstep,         // e+-: the proposed true step length
+  kLRange,         // e+-: range at the pre-step energy
+  kLMfp0,          // mean free paths [4] (gamma: total, in [0])
+  kLNia0 = kLMfp0 + 4,  // numbers of interaction lengths left after HowFar [4]
+  kLPeXS = kLNia0 + 4,  // gamma: photoelectric macroscopic cross section
+  kLLambtr1,            // e+- MSC: transport mean free path, true and geometrical
+  kLTrueStep,           //   lengths, conversion parameters, and the persistent
+  kLZPath,              //   step-limit state after HowFar
+  kLPar1,
+  kLPar2,
+  kLPar3,
+  kLInitRange,
+  kLDynFactor,
+  kLTlimitMin,
+  kLDelta,              // precision form: trueStep - zPath without cancellation
+  kLGauss,              // the cached Gaussian after HowFar
+  kLimDoubles
+};
+constexpr uint32_t kLimMscActive = 1u << 0, kLimMscDisplace = 1u << 1, kLimFirstStep = 1u << 2,
+                   kLimGaussValid = 1u << 3, kLimFp32 = 1u << 4, kLimPreBoundary = 1u << 5;
+constexpr int kLimProvShift = 8;    // bits 8..15: provenance bits of an FP32 record (physics_mixed.cuh)
+constexpr int kLimFlagsShift = 16;  // bits 16..23: the track flags HowFar raised (kFlag*)
+struct Limits {
+  double* d[kLimDoubles];
+  int32_t* cursor;  // RNG cursor after HowFar
+  int8_t* winner;   // process that limited the proposed step
+  uint32_t* bits;
+};
+inline size_t limits_align(size_t b) { return (b + 255) / 256 * 256; }
+inline size_t limits_bytes(int64_t n) {
+  const size_t m = n > 0 ? (size_t)n : 0;
+  return kLimDoubles * limits_align(8 * m) + limits_align(4 * m) + limits_align(m) + limits_align(4 * m);
+}
+inline Limits carve_limits(void* base, int64_t n) {
+  const size_t m = n > 0 ? (size_t)n : 0;
+  uint8_t* p = static_cast<uint8_t*>(base);
+  Limits L;
+  for (int k = 0; k < kLimDoubles; ++k) {
+    L.d[k] = reinterpret_cast<double*>(p);
+    p += limits_align(8 * m);
+  }
+  L.cursor = reinterpret_cast<int32_t*>(p);
+  p += limits_align(4 * m);
+  L.winner = reinterpret_cast<int8_t*>(p);
+  p += limits_align(m);
+  L.bits = reinterpret_cast<uint32_t*>(p);
+  return L;
+}
+
+// the split of the step: phase of a launch (kPhaseStep: HowFar + Perform)
+enum { kPhaseStep = 0, kPhaseHowFar = 1, kPhasePerform = 2 };
+
+cudaError_t launch_howfar(const DevTables& T, int64_t n, const hepem_track_state& in, const double* uniforms, int nu,
+                          uint64_t seed, double* gstep, const Limits& L, hepem_step_counters* counters,
+                          cudaStream_t s, int sms);
+cudaError_t launch_perform(const DevTables& T, int64_t n, const hepem_track_state& in, const hepem_track_state& out,
+                           const double* gstep, const Limits& L, const double* uniforms, int nu, uint64_t seed,
+                           const hepem_step_out& res, hepem_step_counters* counters, cudaStream_t s, int sms);
+
 cudaError_t launch_lookup(const DevTables& T, int64_t n, int pos, const double* ekin, const int32_t* imc, double* xi,
                           double* xb, double* dedx, double* range, double* invr, cudaStream_t s, int sms);
 
@@ -51,6 +120,12 @@ struct BatchOpts {
   const void* tableBase = nullptr;
   size_t tableBytes = 0;
   float tableHitRatio = 0.0f;
+  // split step: kPhaseHowFar writes the proposed steps to gstep and the step
+  // limits to limits (out unused); kPhasePerform reads them (gstep: the
+  // steps transport made)
+  int phase = kPhaseStep;
+  double* gstep = nullptr;
+  Limits limits = {};
 };
 // bytes of the pre-step copy of an in-place precision-form step (n tracks)
 size_t mixed_pre_state_bytes(int64_t n);

@@ -75,6 +75,11 @@ struct Work {
   bool preCopy;
   // precision form: e- and e+ share one sort key (one list in batch order)
   bool oneChargedKey;
+  // the split step (kPhaseHowFar / kPhasePerform): the geometrical steps
+  // (proposed / made) and the step-limit record
+  double* gstep;
+  Limits limits;
+  int phase;
 };
 
 __device__ __forceinline__ uint64_t key_of(const Work& w, int64_t i, uint64_t seed) {
@@ -133,6 +138,9 @@ static Work carve(void* ws, int64_t n) {
   uint8_t* p = static_cast<uint8_t*>(ws);
   Work w;
   w.oneChargedKey = false;
+  w.gstep = nullptr;
+  w.limits = Limits{};
+  w.phase = kPhaseStep;
   w.counts = reinterpret_cast<uint32_t*>(p);
   p += rnd(64 * sizeof(uint32_t));
   w.hist = reinterpret_cast<uint32_t*>(p);
@@ -185,14 +193,25 @@ __global__ void __launch_bounds__(256) sort_hist_kernel(const __grid_constant__ 
       const int imc = in.imc[i];
       const double e = in.ekin[i];
       if (track_input_bad(T, type, imc, e)) {
-        // pass the track through unchanged, flagged
-        Track t;
-        Rng rng;
-        load_track(in, i, t, rng, nullptr, 0, 0, 2);
-        t.flags = kFlagBadInput;
-        store_track(in, out, res, i, t, rng, 2, true);
-        res.n_sec[i] = 0;
-        cnt.steps += 1;
+        if (w.phase == kPhaseHowFar) {
+          // no step limit: flagged in the record, passed through by Perform
+          w.gstep[i] = 0.0;
+          w.limits.d[kLProposed][i] = 0.0;
+          w.limits.bits[i] = (uint32_t)kFlagBadInput << kLimFlagsShift;
+        } else {
+          // pass the track through unchanged, flagged
+          Track t;
+          Rng rng;
+          load_track(in, i, t, rng, nullptr, 0, 0, 2);
+          t.flags = kFlagBadInput;
+          if (w.phase == kPhasePerform) {
+            t.gstep = w.gstep[i];
+            t.pstep = t.gstep;
+          }
+          store_track(in, out, res, i, t, rng, 2, true);
+          res.n_sec[i] = 0;
+          cnt.steps += 1;
+        }
       } else {
         key = sort_key(type, imc, e, ncb, neb, w.oneChargedKey);
       }
@@ -292,6 +311,89 @@ __global__ void __launch_bounds__(256) sort_scatter_kernel(const __grid_constant
 
 #endif  // HEPEM_FP64_UNIT
 
+// ---- the FP32 step-limit record of the precision form's split step -------------------
+// The values of ElLimit32 / GammaLimit32 widened to FP64 (exactly) in the
+// record of kernels.h, with kLimFp32 set and the provenance bits of
+// ElLimit32 in bits kLimProvShift...
+__device__ __forceinline__ void store_limits32(const Limits& L, int64_t i, const ElLimit32& h, const Track& t,
+                                               const Rng& rng, double* gstep) {
+  gstep[i] = f2d(h.gstep);
+  L.d[kLProposed][i] = f2d(h.gstep);
+  L.d[kLPstep][i] = f2d(h.pstep);
+  L.d[kLRange][i] = f2d(h.range);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    L.d[kLMfp0 + k][i] = f2d(h.mfp[k]);
+    L.d[kLNia0 + k][i] = f2d(h.nia[k]);
+  }
+  L.d[kLLambtr1][i] = f2d(h.lambtr1);
+  L.d[kLTrueStep][i] = f2d(h.trueStep);
+  L.d[kLZPath][i] = f2d(h.zPath);
+  L.d[kLDelta][i] = f2d(h.delta);
+  L.d[kLInitRange][i] = f2d(h.initRange);
+  L.d[kLDynFactor][i] = f2d(h.dynFactor);
+  L.d[kLTlimitMin][i] = f2d(h.tlimitMin);
+  L.d[kLGauss][i] = rng.gaussValue;
+  L.cursor[i] = rng.cursor;
+  L.winner[i] = (int8_t)h.winner;
+  L.bits[i] = kLimFp32 | (rng.gaussValid ? kLimGaussValid : 0u) | (t.onBoundary ? kLimPreBoundary : 0u) |
+              (h.bits << kLimProvShift) |
+              ((uint32_t)(t.flags | (rng.overflow ? kFlagRngOverflow : 0)) << kLimFlagsShift);
+}
+
+__device__ __forceinline__ void load_limits32(const Limits& L, int64_t i, ElLimit32& h, Track& t, Rng& rng) {
+  const uint32_t b = L.bits[i];
+  h.gstep = d2f(L.d[kLProposed][i]);
+  h.pstep = d2f(L.d[kLPstep][i]);
+  h.range = d2f(L.d[kLRange][i]);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    h.mfp[k] = d2f(L.d[kLMfp0 + k][i]);
+    h.nia[k] = d2f(L.d[kLNia0 + k][i]);
+  }
+  h.lambtr1 = d2f(L.d[kLLambtr1][i]);
+  h.trueStep = d2f(L.d[kLTrueStep][i]);
+  h.zPath = d2f(L.d[kLZPath][i]);
+  h.delta = d2f(L.d[kLDelta][i]);
+  h.initRange = d2f(L.d[kLInitRange][i]);
+  h.dynFactor = d2f(L.d[kLDynFactor][i]);
+  h.tlimitMin = d2f(L.d[kLTlimitMin][i]);
+  h.winner = L.winner[i];
+  h.bits = (b >> kLimProvShift) & 0xFFu;
+  rng.cursor = L.cursor[i];
+  rng.gaussValid = (b & kLimGaussValid) != 0;
+  rng.gaussValue = L.d[kLGauss][i];
+  t.flags |= (uint8_t)((b >> kLimFlagsShift) & 0xFFu);
+}
+
+__device__ __forceinline__ void store_glimits32(const Limits& L, int64_t i, const GammaLimit32& q, const Track& t,
+                                                const Rng& rng, double* gstep) {
+  gstep[i] = f2d(q.gstep);
+  L.d[kLProposed][i] = f2d(q.gstep);
+  L.d[kLPstep][i] = f2d(q.gstep);
+  L.d[kLMfp0][i] = f2d(q.mfp);
+  L.d[kLNia0][i] = f2d(q.nia0);
+  L.d[kLPeXS][i] = f2d(q.pe);
+  L.d[kLGauss][i] = rng.gaussValue;
+  L.cursor[i] = rng.cursor;
+  L.winner[i] = -1;
+  L.bits[i] = kLimFp32 | (rng.gaussValid ? kLimGaussValid : 0u) | (t.onBoundary ? kLimPreBoundary : 0u) |
+              ((uint32_t)(t.flags | (rng.overflow ? kFlagRngOverflow : 0)) << kLimFlagsShift);
+}
+
+__device__ __forceinline__ void load_glimits32(const Limits& L, int64_t i, GammaLimit32& q, Track& t, Rng& rng) {
+  const uint32_t b = L.bits[i];
+  q.gstep = d2f(L.d[kLProposed][i]);
+  q.mfp = d2f(L.d[kLMfp0][i]);
+  q.nia0 = d2f(L.d[kLNia0][i]);
+  q.pe = d2f(L.d[kLPeXS][i]);
+  t.nia[0] = L.d[kLNia0][i];
+  rng.cursor = L.cursor[i];
+  rng.gaussValid = (b & kLimGaussValid) != 0;
+  rng.gaussValue = L.d[kLGauss][i];
+  t.flags |= (uint8_t)((b >> kLimFlagsShift) & 0xFFu);
+}
+
 // ---- 2. stage A -----------------------------------------------------------------------
 // copy of the mutable pre-step state of track i (precision form, in-place steps)
 __device__ __forceinline__ void save_pre(const hepem_track_state& in, const hepem_track_state& pre, int64_t i) {
@@ -351,7 +453,10 @@ __device__ __forceinline__ void fb_push(bool trip, int32_t idx, uint8_t kind, co
 #ifndef HEPEM_MIXED_B_WARPS
 #define HEPEM_MIXED_B_WARPS 24
 #endif
-template <int BS, int MODE>
+// PHASE kPhaseStep: HowFar and Perform up to the interaction (the fused step);
+// kPhaseHowFar: HowFar only, into the step-limit record (nothing queued);
+// kPhasePerform: Perform from the record with the caller's geometrical step.
+template <int BS, int MODE, int PHASE = kPhaseStep>
 __global__ void __launch_bounds__(BS, MODE == kStageMixed ? HEPEM_MIXED_A_WARPS * 32 / BS : 1)
     stage_a_charged_kernel(const __grid_constant__ DevTables T,
                                                               const hepem_track_state in, const hepem_track_state out,
@@ -372,18 +477,49 @@ __global__ void __launch_bounds__(BS, MODE == kStageMixed ? HEPEM_MIXED_A_WARPS 
       Track t;
       Rng rng;
       load_track(in, idx, t, rng, uniforms, nu, key_of(w, idx, seed), type);
-      const int32_t c0 = rng.cursor;
+      int32_t c0 = rng.cursor;
       if (MODE == kStageMixed) {
         MixedEl M{T, rng, t, false};
-        key = M.stage_a();
+        if (PHASE == kPhaseStep) {
+          key = M.stage_a();
+        } else if (PHASE == kPhaseHowFar) {
+          ElLimit32 h;
+          M.howfar(h);
+          if (!M.trip) store_limits32(w.limits, idx, h, t, rng, w.gstep);
+        } else {
+          ElLimit32 h;
+          load_limits32(w.limits, idx, h, t, rng);
+          c0 = rng.cursor;
+          // an FP64 record (its HowFar tripped), or a step that transport
+          // shortened (the geometrical -> true conversion): the FP64 code
+          if (!(w.limits.bits[idx] & kLimFp32) || w.gstep[idx] != f2d(h.gstep))
+            M.set_trip();
+          else
+            key = M.perform(h);
+        }
         tripped = M.trip;
         if (tripped) HEPEM_COUNT_TRIP(M.tripLine);
       } else {
         Physics P{T, rng, t};
-        P.el_howfar();
-        key = P.el_perform_until_discrete();
+        if (PHASE == kPhaseStep) {
+          P.el_howfar();
+          key = P.el_perform_until_discrete();
+        } else if (PHASE == kPhaseHowFar) {
+          P.el_howfar();
+          store_limits64(w.limits, idx, t, rng, type, w.gstep);
+        } else {
+          load_limits64(w.limits, idx, t, rng, type, w.gstep);
+          c0 = rng.cursor;
+          key = P.el_perform_until_discrete();
+        }
       }
-      if (tripped) {
+      if (PHASE == kPhaseHowFar) {
+        key = -1;
+        if (!tripped) {
+          cnt.uniforms += (uint32_t)(rng.cursor - c0);
+          cnt.overflow += rng.overflow;
+        }
+      } else if (tripped) {
         key = -1;
       } else {
         if (MODE == kStageMixed && w.preCopy && key >= 0 && key != kQAnnihRest) save_pre(in, w.pre, idx);
@@ -403,7 +539,7 @@ __global__ void __launch_bounds__(BS, MODE == kStageMixed ? HEPEM_MIXED_A_WARPS 
 
 // MODE kStageMixed: HowFar and the interaction choice from the FP32 table
 // (MixedG); a tripped gamma is not stored but goes to the fallback list.
-template <int BS, int MODE>
+template <int BS, int MODE, int PHASE = kPhaseStep>
 __global__ void __launch_bounds__(BS) stage_a_gamma_kernel(const __grid_constant__ DevTables T,
                                                             const hepem_track_state in, const hepem_track_state out,
                                                             const double* __restrict__ uniforms, int nu,
@@ -422,11 +558,25 @@ __global__ void __launch_bounds__(BS) stage_a_gamma_kernel(const __grid_constant
       Track t;
       Rng rng;
       load_track(in, idx, t, rng, uniforms, nu, key_of(w, idx, seed), 2);
-      const int32_t c0 = rng.cursor;
+      int32_t c0 = rng.cursor;
       t.isEl = false;
       if (MODE == kStageMixed) {
         MixedG G{T, rng, t, false};
-        key = G.stage_a();
+        if (PHASE == kPhaseStep) {
+          key = G.stage_a();
+        } else if (PHASE == kPhaseHowFar) {
+          GammaLimit32 q;
+          G.howfar(q);
+          store_glimits32(w.limits, idx, q, t, rng, w.gstep);
+        } else {
+          GammaLimit32 q;
+          load_glimits32(w.limits, idx, q, t, rng);
+          c0 = rng.cursor;
+          const double g = w.gstep[idx];
+          key = G.perform(q, d2f(g));
+          t.gstep = g;
+          t.pstep = g;
+        }
         tripped = G.trip;
         if (tripped) {
           HEPEM_COUNT_TRIP(G.tripLine);
@@ -434,16 +584,30 @@ __global__ void __launch_bounds__(BS) stage_a_gamma_kernel(const __grid_constant
         }
       } else {
         Physics P{T, rng, t};
-        P.gamma_howfar();
-        if (t.onBoundary) {
-          t.nia[0] -= t.gstep / t.mfp[0];
+        if (PHASE == kPhaseHowFar) {
+          P.gamma_howfar();
+          store_limits64(w.limits, idx, t, rng, 2, w.gstep);
         } else {
-          P.gamma_select();
-          key = P.gamma_perform_until_interaction();
+          if (PHASE == kPhaseStep) {
+            P.gamma_howfar();
+          } else {
+            load_limits64(w.limits, idx, t, rng, 2, w.gstep);
+            c0 = rng.cursor;
+          }
+          if (t.onBoundary) {
+            t.nia[0] -= t.gstep / t.mfp[0];
+          } else {
+            P.gamma_select();
+            key = P.gamma_perform_until_interaction();
+          }
+          t.pstep = t.gstep;
         }
-        t.pstep = t.gstep;
       }
-      if (!tripped) {
+      if (PHASE == kPhaseHowFar) {
+        key = -1;
+        cnt.uniforms += (uint32_t)(rng.cursor - c0);
+        cnt.overflow += rng.overflow;
+      } else if (!tripped) {
         if (key == -2) {
           Physics P{T, rng, t};
           P.gamma_tracking_cut();
@@ -589,6 +753,13 @@ __device__ __forceinline__ void interaction_fp64(Physics& P) {
 }
 
 #if HEPEM_FP64_UNIT
+// PHASE kPhaseHowFar: the FP64 HowFar of a track whose FP32 HowFar tripped,
+// into the step-limit record.  kPhasePerform: the whole step again in FP64:
+// HowFar from the pre-step state with the pre-step boundary status (the state
+// is the pre-step one: HowFar left it unchanged), then the caller's transport
+// (its geometrical step, unless it is the proposed one, the direction and the
+// post-step boundary status in the state), then Perform.
+template <int PHASE>
 __device__ void charged_full_step(const DevTables& T, const hepem_track_state& in, const hepem_track_state& out,
                                   const double* uniforms, int nu, uint64_t seed, const hepem_step_out& res,
                                   const Work& w, int32_t i, bool fromStageA, StepCount& cnt) {
@@ -598,9 +769,28 @@ __device__ void charged_full_step(const DevTables& T, const hepem_track_state& i
   Rng rng;
   load_track(src, i, t, rng, uniforms, nu, key_of(w, i, seed), type);
   Physics P{T, rng, t};
-  const int32_t c0 = rng.cursor;
-  P.el_howfar();
+  int32_t c0 = rng.cursor;
+  if (PHASE == kPhaseHowFar) {
+    P.el_howfar();
+    store_limits64(w.limits, i, t, rng, type, w.gstep);
+    cnt.uniforms += (uint32_t)(rng.cursor - c0);
+    cnt.overflow += rng.overflow;
+    cnt.fallback += 1;
+    return;
+  }
+  if (PHASE == kPhasePerform) {
+    const bool post = t.onBoundary;
+    t.onBoundary = (w.limits.bits[i] & kLimPreBoundary) != 0;
+    P.el_howfar();
+    const double g = w.gstep[i];
+    if (g != w.limits.d[kLProposed][i]) t.gstep = g;
+    t.onBoundary = post;
+    c0 = rng.cursor;
+  } else {
+    P.el_howfar();
+  }
   const int key = P.el_perform_until_discrete();
+  if (PHASE == kPhasePerform) t.gstep = w.gstep[i];
   const int32_t cA = rng.cursor;
   const uint32_t ovA = rng.overflow;
   switch (key) {
@@ -663,7 +853,7 @@ __device__ void gamma_full_step(const DevTables& T, const hepem_track_state& in,
   cnt.fallback += 1;
 }
 
-template <int BS>
+template <int BS, int PHASE = kPhaseStep>
 __global__ void __launch_bounds__(BS) final_fallback_kernel(const __grid_constant__ DevTables T,
                                                              const hepem_track_state in, const hepem_track_state out,
                                                              const double* __restrict__ uniforms, int nu,
@@ -684,7 +874,7 @@ __global__ void __launch_bounds__(BS) final_fallback_kernel(const __grid_constan
     if (kind == kFbGammaA) {
       gamma_full_step(T, in, out, uniforms, nu, seed, res, w, i, cnt);
     } else if (kind == 0 || charged_model(kind - 1)) {
-      charged_full_step(T, in, out, uniforms, nu, seed, res, w, i, kind == 0, cnt);
+      charged_full_step<PHASE>(T, in, out, uniforms, nu, seed, res, w, i, kind == 0, cnt);
     } else {
       if (kind - 1 == kQConversion)
         stage_b_one<kQConversion, false>(T, in, out, uniforms, nu, seed, res, w, i, -1, cnt);
@@ -738,6 +928,15 @@ static void mixed_table(StageFn* m) {
   m[2 + kQCompton] = stage_b_kernel<kQCompton, BS, kStageMixed>;
 }
 
+// the stage A kernels of the split step (256 threads): [phase - 1][0 e+-, 1 gamma]
+template <int MODE>
+static void split_table(StageFn (*f)[2]) {
+  f[0][0] = stage_a_charged_kernel<256, MODE, kPhaseHowFar>;
+  f[0][1] = stage_a_gamma_kernel<256, MODE, kPhaseHowFar>;
+  f[1][0] = stage_a_charged_kernel<256, MODE, kPhasePerform>;
+  f[1][1] = stage_a_gamma_kernel<256, MODE, kPhasePerform>;
+}
+
 #if !HEPEM_FP64_UNIT
 // the precision form's stage kernels of this unit, for the FP64 unit's table
 void mixed_stage_table(int b, StageFn* m) {
@@ -745,8 +944,10 @@ void mixed_stage_table(int b, StageFn* m) {
   else if (b == 2) mixed_table<512>(m);
   else mixed_table<256>(m);
 }
+void mixed_split_table(StageFn (*m)[2]) { split_table<kStageMixed>(m); }
 #else
 void mixed_stage_table(int b, StageFn* m);  // kernels_batched_mixed.cu
+void mixed_split_table(StageFn (*m)[2]);
 
 struct StageKernels {
   StageFn fn[3][kNumStageKernels];
@@ -755,6 +956,10 @@ struct StageKernels {
   int occMixed[3][kNumStageKernels];
   StageFn final_[3];                   // precision form: the FP64 fallback kernel
   int occFinal[3];
+  // the split step (256 threads per block): stage A of HowFar / Perform,
+  // [phase - 1][0 e+-, 1 gamma], FP64 and FP32; the fallback of each phase
+  StageFn split[2][2], splitMixed[2][2], finalSplit[2];
+  int occSplit[2][2], occSplitMixed[2][2], occFinalSplit[2];
 };
 
 static int occupancy_of(StageFn f, int bs) {
@@ -782,6 +987,17 @@ static const StageKernels& stage_kernels() {
         r.occMixed[b][k] = r.mixed[b][k] ? occupancy_of(r.mixed[b][k], kBlockSizes[b]) : 0;
       }
       r.occFinal[b] = occupancy_of(r.final_[b], kBlockSizes[b]);
+    }
+    split_table<kStageFp64>(r.split);
+    mixed_split_table(r.splitMixed);
+    r.finalSplit[0] = final_fallback_kernel<256, kPhaseHowFar>;
+    r.finalSplit[1] = final_fallback_kernel<256, kPhasePerform>;
+    for (int ph = 0; ph < 2; ++ph) {
+      for (int q = 0; q < 2; ++q) {
+        r.occSplit[ph][q] = occupancy_of(r.split[ph][q], 256);
+        r.occSplitMixed[ph][q] = occupancy_of(r.splitMixed[ph][q], 256);
+      }
+      r.occFinalSplit[ph] = occupancy_of(r.finalSplit[ph], 256);
     }
     return r;
   }();
@@ -825,6 +1041,9 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
     w.pre = *o.preState;
     w.preCopy = true;
   }
+  w.phase = o.phase;
+  w.gstep = o.gstep;
+  w.limits = o.limits;
   // The FP64 stages are bound by the FP64 pipe and gain from warps of one
   // couple and energy range; the precision form's stages are bound by the
   // latency of their state gathers and gain more from keeping each particle
@@ -876,14 +1095,32 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
     const cudaError_t x = cudaLaunchKernelEx(&lc, f, T, in, out, uniforms, nu, seed, res, w, counters);
     if (le == cudaSuccess) le = x;
   };
-  for (int q = 0; q < kNumStageKernels; ++q) {
+  if (o.phase != kPhaseStep) {
+    // the split step: its stage A kernels (256 threads, occupancy grids)
+    const int ph = o.phase - 1;
+    for (int q = 0; q < 2; ++q) {
+      if (o.mixed)
+        stage(K.splitMixed[ph][q], sms * K.occSplitMixed[ph][q], 256);
+      else
+        stage(K.split[ph][q], sms * K.occSplit[ph][q], 256);
+      mark();
+    }
+    if (o.phase == kPhaseHowFar) {
+      if (o.mixed) stage(K.finalSplit[0], sms * K.occFinalSplit[0], 256);
+      const cudaError_t e3 = cudaGetLastError();
+      return le != cudaSuccess ? le : e3;
+    }
+  }
+  for (int q = o.phase == kPhaseStep ? 0 : 2; q < kNumStageKernels; ++q) {
     const int b = bs_index(cfg.block[q]);
+    StageFn const finalFn = o.phase == kPhasePerform ? K.finalSplit[1] : K.final_[1];
+    const int finalOcc = o.phase == kPhasePerform ? K.occFinalSplit[1] : K.occFinal[1];
     if (o.mixed && K.mixed[b][q]) {
       // precision form: the FP32 kernel (its FP64 fallbacks run after the last stage)
       const int om = K.occMixed[b][q];
       const int pm = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < om ? cfg.ctasPerSM[q] : om;
       stage(K.mixed[b][q], sms * pm, kBlockSizes[b]);
-      if (q == kNumStageKernels - 1) stage(K.final_[1], sms * K.occFinal[1], 256);
+      if (q == kNumStageKernels - 1) stage(finalFn, sms * finalOcc, 256);
       mark();
       continue;
     }
@@ -891,7 +1128,7 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
       const int occ = K.occ[b][q];
       const int per = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < occ ? cfg.ctasPerSM[q] : occ;
       stage(K.fn[b][q], sms * per, kBlockSizes[b]);
-      stage(K.final_[1], sms * K.occFinal[1], 256);
+      stage(finalFn, sms * finalOcc, 256);
       mark();
       continue;
     }

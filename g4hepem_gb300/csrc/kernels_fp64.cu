@@ -169,6 +169,101 @@ __global__ void __launch_bounds__(256) step_kernel(const __grid_constant__ DevTa
   if (counters) add_counters(cnt, counters);
 }
 
+// ---- the step split at the geometry: HowFar, then Perform ----------------------------
+// howfar_kernel: G4HepEmElectronManager::HowFar / G4HepEmGammaManager::HowFar
+// (G4HepEmElectronManager.icc:35-169, G4HepEmGammaManager.icc:27-48) per track;
+// the proposed geometrical step to gstep, the rest of what Perform needs to the
+// step-limit record; the track state is left as it was.
+__global__ void __launch_bounds__(256) howfar_kernel(const __grid_constant__ DevTables T, int64_t n,
+                                                     const hepem_track_state in, const double* __restrict__ uniforms,
+                                                     int nu, uint64_t seed, double* __restrict__ gstep,
+                                                     const Limits L, hepem_step_counters* counters) {
+  StepCount cnt = {};
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    if (i >= n) continue;
+    const int type = in.type[i];
+    Track t;
+    Rng rng;
+    const bool bad = track_input_bad(T, type, in.imc[i], in.ekin[i]);
+    load_track(in, i, t, rng, uniforms, nu, seed, bad ? 2 : type);
+    if (bad) {
+      t.flags |= kFlagBadInput;
+      t.mfp[0] = kLarge;
+      t.peXS = 0.0;
+      store_limits64(L, i, t, rng, 2, gstep);
+      continue;
+    }
+    Physics P{T, rng, t};
+    if (type == 2) {
+      t.isEl = false;
+      P.gamma_howfar();
+    } else {
+      P.el_howfar();
+    }
+    store_limits64(L, i, t, rng, type, gstep);
+    cnt.uniforms += (uint32_t)(rng.cursor - in.rng_cursor[i]);
+    cnt.overflow += rng.overflow;
+  }
+  if (counters) add_counters(cnt, counters);
+}
+
+// perform_kernel: the rest of the step with the geometrical step gstep[i]
+// that transport made, the direction and the post-step boundary status in
+// the state: e+- G4HepEmElectronManager::Perform (.icc:171-483, with
+// UpdatePStepLength's geometrical -> true conversion); gamma on a boundary
+// UpdateNumIALeft only, else SelectInteraction + Perform, as the reference
+// client (apps/examples/TestEm3/src/G4HepEmProcess.cc:160-197).
+__global__ void __launch_bounds__(256) perform_kernel(const __grid_constant__ DevTables T, int64_t n,
+                                                      const hepem_track_state in, const hepem_track_state out,
+                                                      const double* __restrict__ gstep, const Limits L,
+                                                      const double* __restrict__ uniforms, int nu, uint64_t seed,
+                                                      const hepem_step_out res, hepem_step_counters* counters) {
+  StepCount cnt = {};
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    if (i >= n) continue;
+    const int type = in.type[i];
+    Track t;
+    Rng rng;
+    const bool bad = track_input_bad(T, type, in.imc[i], in.ekin[i]);
+    load_track(in, i, t, rng, uniforms, nu, seed, bad ? 2 : type);
+    if (bad) {
+      t.flags |= kFlagBadInput;
+      t.gstep = gstep[i];
+      t.pstep = t.gstep;
+      store_track(in, out, res, i, t, rng, 2, true);
+      res.n_sec[i] = 0;
+      cnt.steps += 1;
+      continue;
+    }
+    load_limits64(L, i, t, rng, type, gstep);
+    const int32_t c0 = rng.cursor;
+    Physics P{T, rng, t};
+    if (type == 2) {
+      t.isEl = false;
+      if (t.onBoundary) {
+        t.nia[0] -= t.gstep / t.mfp[0];
+      } else {
+        P.gamma_select();
+        P.gamma_perform();
+      }
+      t.pstep = t.gstep;
+    } else {
+      P.el_perform();
+    }
+    store_track(in, out, res, i, t, rng, type, false);
+    store_secondaries(res, i, t, 0);
+    const int ns = t.nsec > 2 ? 2 : t.nsec;
+    cnt.steps += 1;
+    cnt.uniforms += (uint32_t)(rng.cursor - c0);
+    cnt.overflow += rng.overflow;
+    cnt.secondaries += ns;
+    if (t.winner >= 0 && t.winner < 4) count_inter(cnt, (type == 2 ? 4 : 0) + t.winner);
+  }
+  if (counters) add_counters(cnt, counters);
+}
+
 // the same lookups from the FP32 tables of the precision form (FP32 arithmetic)
 __global__ void __launch_bounds__(256) lookup_mixed_kernel(const __grid_constant__ DevTables T, int64_t n, int pos,
                                                            const double* __restrict__ ekin,
@@ -385,6 +480,22 @@ cudaError_t launch_step(const DevTables& T, int64_t n, const hepem_track_state& 
                         hepem_step_counters* counters, cudaStream_t s, int sms) {
   if (n <= 0) return cudaSuccess;
   step_kernel<<<grid_for(n, 256, sms), 256, 0, s>>>(T, n, in, out, uniforms, nu, seed, res, counters);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_howfar(const DevTables& T, int64_t n, const hepem_track_state& in, const double* uniforms, int nu,
+                          uint64_t seed, double* gstep, const Limits& L, hepem_step_counters* counters,
+                          cudaStream_t s, int sms) {
+  if (n <= 0) return cudaSuccess;
+  howfar_kernel<<<grid_for(n, 256, sms), 256, 0, s>>>(T, n, in, uniforms, nu, seed, gstep, L, counters);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_perform(const DevTables& T, int64_t n, const hepem_track_state& in, const hepem_track_state& out,
+                           const double* gstep, const Limits& L, const double* uniforms, int nu, uint64_t seed,
+                           const hepem_step_out& res, hepem_step_counters* counters, cudaStream_t s, int sms) {
+  if (n <= 0) return cudaSuccess;
+  perform_kernel<<<grid_for(n, 256, sms), 256, 0, s>>>(T, n, in, out, gstep, L, uniforms, nu, seed, res, counters);
   return cudaGetLastError();
 }
 

@@ -328,6 +328,19 @@ __device__ __forceinline__ float annih_macxs32(float e, float ne) {
 }
 
 // ---- the e+- stage A in FP32 ------------------------------------------------------------
+// The step limits that the FP32 HowFar of MixedEl leaves for its Perform:
+// lengths, mean free paths and interaction lengths left in FP32, the MSC
+// state, and the provenance of values equal by construction (kL32*), which
+// Perform's comparisons decide exactly.
+constexpr uint32_t kL32FirstStep = 1u << 0, kL32Active = 1u << 1, kL32Displace = 1u << 2, kL32StepFn = 1u << 3,
+                   kL32PIsRange = 1u << 4, kL32TsIsP = 1u << 5, kL32TsIsTlm = 1u << 6, kL32AtRange = 1u << 7;
+struct ElLimit32 {
+  float range, pstep, gstep, trueStep, zPath, lambtr1, delta, initRange, dynFactor, tlimitMin;
+  float mfp[4], nia[4];
+  int winner;
+  uint32_t bits;
+};
+
 struct MixedEl {
   const DevTables& T;
   Rng& rng;
@@ -630,9 +643,12 @@ struct MixedEl {
   }
 
   // ---- the stage: HowFar + Perform up to the pending discrete interaction ------------
-  // Returns the interaction queue of the pending interaction or -1 (as
-  // Physics::el_perform_until_discrete).  Valid only if !trip on return.
-  __device__ int stage_a() {
+  // stage_a() returns the interaction queue of the pending interaction or -1 (as
+  // Physics::el_perform_until_discrete); valid only if !trip on return.  Its two
+  // halves are howfar(), the step limits of G4HepEmElectronManager::HowFar in FP32
+  // (kept in an ElLimit32), and perform(), Perform from those limits; the split
+  // entry points run them as two kernels.
+  __device__ void howfar(ElLimit32& h) {
     const DevElData& d = eld();
     const DevElData32& f = elf();
     const int nL = d.nLoss;
@@ -825,6 +841,52 @@ struct MixedEl {
       // the geometry-shortened case of the reference is left to the FP64 code
       if (gstep < zPath) set_trip();
     }
+    h.range = range;
+    h.pstep = pstep;
+    h.gstep = gstep;
+    h.trueStep = trueStep;
+    h.zPath = zPath;
+    h.lambtr1 = lambtr1;
+    h.delta = delta;
+    h.initRange = initRange;
+    h.dynFactor = dynFactor;
+    h.tlimitMin = tlimitMin;
+#pragma unroll
+    for (int ip = 0; ip < 4; ++ip) {
+      h.mfp[ip] = mfp[ip];
+      h.nia[ip] = nia[ip];
+    }
+    h.winner = winner;
+    h.bits = (firstStep ? kL32FirstStep : 0u) | (active ? kL32Active : 0u) | (displace ? kL32Displace : 0u) |
+             (stepFn ? kL32StepFn : 0u) | (pIsRange ? kL32PIsRange : 0u) | (tsIsP ? kL32TsIsP : 0u) |
+             (tsIsTlm ? kL32TsIsTlm : 0u) | (atRange ? kL32AtRange : 0u);
+  }
+
+  __device__ int perform(const ElLimit32& h) {
+    const DevElData& d = eld();
+    const DevElData32& f = elf();
+    const int nL = d.nLoss;
+    const int imc = t.imc;
+    const int cMat = ld(&T.couples[imc].mat), cRegion = ld(&T.couples[imc].region);
+    const DevRegion32& reg = T.regions32[cRegion];
+    const DevMat32& md = T.mats32[cMat];
+    const double e = t.e;
+    const float ef = d2f(e), lef = logf(ef);
+    const float range = h.range;
+    float pstep = h.pstep, gstep = h.gstep, trueStep = h.trueStep, zPath = h.zPath, lambtr1 = h.lambtr1;
+    const float delta = h.delta;
+    const float initRange = h.initRange, dynFactor = h.dynFactor, tlimitMin = h.tlimitMin;
+    float mfp[4], nia[4];
+#pragma unroll
+    for (int ip = 0; ip < 4; ++ip) {
+      mfp[ip] = h.mfp[ip];
+      nia[ip] = h.nia[ip];
+    }
+    const int winner = h.winner;
+    const bool firstStep = h.bits & kL32FirstStep;
+    bool active = h.bits & kL32Active;
+    const bool displace = h.bits & kL32Displace, stepFn = h.bits & kL32StepFn, pIsRange = h.bits & kL32PIsRange;
+    const bool tsIsP = h.bits & kL32TsIsP, tsIsTlm = h.bits & kL32TsIsTlm, atRange = h.bits & kL32AtRange;
     t.winner = winner;
     t.gstep = f2d(gstep);
     t.msc.initRange = f2d(initRange);
@@ -991,6 +1053,12 @@ struct MixedEl {
       default: return -1;
     }
   }
+
+  __device__ int stage_a() {
+    ElLimit32 h;
+    howfar(h);
+    return perform(h);
+  }
 };
 
 // ---- the gamma stage A in FP32 ---------------------------------------------------------
@@ -1067,6 +1135,11 @@ static __device__ __noinline__ int gamma_select64(const DevTables& T, Track& t, 
   return (u > tmfp * t.peXS) ? 1 : 2;
 }
 
+// What the FP32 HowFar of MixedG leaves for its Perform.
+struct GammaLimit32 {
+  float mfp, pe, nia0, gstep;
+};
+
 struct MixedG {
   const DevTables& T;
   Rng& rng;
@@ -1099,8 +1172,17 @@ struct MixedG {
 
   // HowFar + SelectInteraction + the first part of Perform, as the FP64 stage
   // (stage_a_gamma_kernel): returns the interaction queue, -1 (no interaction
-  // or on a boundary) or -2 (no interaction: tracking cut); valid if !trip
+  // or on a boundary) or -2 (no interaction: tracking cut); valid if !trip.
+  // howfar() is the HowFar half (total cross section, mean free path and the
+  // proposed step in FP32, kept in a GammaLimit32), perform() the rest with
+  // the geometrical step gstep (the proposed one in stage_a).
   __device__ int stage_a() {
+    GammaLimit32 q;
+    howfar(q);
+    return perform(q, q.gstep);
+  }
+
+  __device__ void howfar(GammaLimit32& q) {
     const DevGamma& g = T.gm;
     const DevGamma32& h = T.gm32;
     if (nonpositive(t.nia[0])) t.nia[0] = f2d(neg_log_u(rng.flat()));
@@ -1109,9 +1191,8 @@ struct MixedG {
     const int imat = ld(&T.couples[t.imc].mat);
     const bool w2 = dless(g.eMax1, e), w1 = !w2 && dless(g.eMax0, e);
     float tot, pe = 0.f;
-    int st2 = 0;
     if (w2) {
-      st2 = imat * g.dataPerMat + g.nData0 + g.nData1;
+      const int st2 = imat * g.dataPerMat + g.nData0 + g.nData1;
       tot = spline_log_9_32(g.nE2, h.mx + st2, ef, lef, h.logEMin2, h.ild2, 1);
     } else if (w1) {
       const float* d = h.mx + imat * g.dataPerMat + g.nData0;
@@ -1130,9 +1211,22 @@ struct MixedG {
       pe = fmx(0.f, macxs_pe32(imat, e, ef));
       tot = y1 + b * (ld(d + i2 + 3) - y1) + pe;
     }
-    const float mfp = tot > 0.f ? 1.f / tot : kLargeF;
-    const float nia0 = d2f(t.nia[0]);
-    const float gstep = mfp * nia0;
+    q.mfp = tot > 0.f ? 1.f / tot : kLargeF;
+    q.pe = pe;
+    q.nia0 = d2f(t.nia[0]);
+    q.gstep = q.mfp * q.nia0;
+  }
+
+  // gstep: the geometrical step made (FP32)
+  __device__ int perform(const GammaLimit32& q, float gstep) {
+    const DevGamma& g = T.gm;
+    const DevGamma32& h = T.gm32;
+    const double e = t.e;
+    const float ef = d2f(e), lef = logf(ef);
+    const int imat = ld(&T.couples[t.imc].mat);
+    const bool w2 = dless(g.eMax1, e);
+    const int st2 = w2 ? imat * g.dataPerMat + g.nData0 + g.nData1 : 0;
+    const float mfp = q.mfp, pe = q.pe, nia0 = q.nia0;
     t.mfp[0] = f2d(mfp);
     t.gstep = f2d(gstep);
     t.pstep = t.gstep;

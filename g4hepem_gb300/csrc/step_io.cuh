@@ -5,6 +5,7 @@
 #include <cstdint>
 
 #include "g4hepem_gb300.h"
+#include "kernels.h"
 #include "physics.cuh"
 
 namespace hepem {
@@ -148,6 +149,88 @@ __device__ __forceinline__ void store_track(const hepem_track_state& in, const h
   res.disp_y[i] = charged ? t.msc.disp[1] : 0.0;
   res.disp_z[i] = charged ? t.msc.disp[2] : 0.0;
   res.flags[i] = t.flags | (rng.overflow ? kFlagRngOverflow : 0);
+}
+
+// ---- the step-limit record (kernels.h: Limits) ----------------------------------------
+// After the FP64 HowFar of track i (Physics::el_howfar / gamma_howfar):
+// the proposed geometrical step to gstep[i], everything else Perform needs to
+// the record.  preBoundary: the pre-step boundary status HowFar used.
+__device__ __forceinline__ void store_limits64(const Limits& L, int64_t i, const Track& t, const Rng& rng, int type,
+                                               double* gstep) {
+  const bool charged = type != 2;
+  gstep[i] = t.gstep;
+  L.d[kLProposed][i] = t.gstep;
+  L.d[kLPstep][i] = t.pstep;
+  L.d[kLMfp0][i] = t.mfp[0];
+  L.d[kLNia0][i] = t.nia[0];
+  L.d[kLGauss][i] = rng.gaussValue;
+  L.cursor[i] = rng.cursor;
+  L.winner[i] = (int8_t)t.winner;
+  uint32_t b = (rng.gaussValid ? kLimGaussValid : 0u) | (t.onBoundary ? kLimPreBoundary : 0u) |
+               ((uint32_t)(t.flags | (rng.overflow ? kFlagRngOverflow : 0)) << kLimFlagsShift);
+  if (charged) {
+    const Msc& m = t.msc;
+    L.d[kLRange][i] = t.range;
+#pragma unroll
+    for (int k = 1; k < 4; ++k) {
+      L.d[kLMfp0 + k][i] = t.mfp[k];
+      L.d[kLNia0 + k][i] = t.nia[k];
+    }
+    L.d[kLLambtr1][i] = m.lambtr1;
+    L.d[kLTrueStep][i] = m.trueStep;
+    L.d[kLZPath][i] = m.zPath;
+    L.d[kLPar1][i] = m.par1;
+    L.d[kLPar2][i] = m.par2;
+    L.d[kLPar3][i] = m.par3;
+    L.d[kLInitRange][i] = m.initRange;
+    L.d[kLDynFactor][i] = m.dynFactor;
+    L.d[kLTlimitMin][i] = m.tlimitMin;
+    b |= (m.active ? kLimMscActive : 0u) | (m.displace ? kLimMscDisplace : 0u) | (m.firstStep ? kLimFirstStep : 0u);
+  } else {
+    L.d[kLPeXS][i] = t.peXS;
+  }
+  L.bits[i] = b;
+}
+
+// Before the FP64 Perform of track i: the caller's geometrical step and the
+// record over the state that load_track read (the state keeps the direction
+// and the post-step boundary status that transport left).
+__device__ __forceinline__ void load_limits64(const Limits& L, int64_t i, Track& t, Rng& rng, int type,
+                                              const double* gstep) {
+  const uint32_t b = L.bits[i];
+  t.gstep = gstep[i];
+  t.pstep = L.d[kLPstep][i];
+  t.mfp[0] = L.d[kLMfp0][i];
+  t.nia[0] = L.d[kLNia0][i];
+  t.winner = L.winner[i];
+  t.flags |= (uint8_t)((b >> kLimFlagsShift) & 0xFFu);
+  rng.cursor = L.cursor[i];
+  rng.gaussValid = (b & kLimGaussValid) != 0;
+  rng.gaussValue = L.d[kLGauss][i];
+  if (type != 2) {
+    Msc& m = t.msc;
+    t.range = L.d[kLRange][i];
+#pragma unroll
+    for (int k = 1; k < 4; ++k) {
+      t.mfp[k] = L.d[kLMfp0 + k][i];
+      t.nia[k] = L.d[kLNia0 + k][i];
+    }
+    m.lambtr1 = L.d[kLLambtr1][i];
+    m.trueStep = L.d[kLTrueStep][i];
+    m.zPath = L.d[kLZPath][i];
+    m.par1 = L.d[kLPar1][i];
+    m.par2 = L.d[kLPar2][i];
+    m.par3 = L.d[kLPar3][i];
+    m.initRange = L.d[kLInitRange][i];
+    m.dynFactor = L.d[kLDynFactor][i];
+    m.tlimitMin = L.d[kLTlimitMin][i];
+    m.active = (b & kLimMscActive) != 0;
+    m.displace = (b & kLimMscDisplace) != 0;
+    m.firstStep = (b & kLimFirstStep) != 0;
+    m.noScatter = false;
+  } else {
+    t.peXS = L.d[kLPeXS][i];
+  }
 }
 
 __device__ __forceinline__ void store_secondaries(const hepem_step_out& res, int64_t i, const Track& t, int first) {

@@ -93,7 +93,9 @@ EXPORTED = ["hepem_create", "hepem_create_from_file", "hepem_image_from_json", "
             "hepem_server_create", "hepem_server_capacity", "hepem_server_submit", "hepem_server_poll",
             "hepem_server_wait", "hepem_server_cancel", "hepem_server_get_stats", "hepem_server_reset_stats",
             "hepem_server_destroy", "hepem_sample_model", "hepem_stack_secondaries", "hepem_woodcock_gamma", "hepem_get_launch_config", "hepem_set_launch_config", "hepem_autotune",
-            "hepem_set_table_l2_window"]
+            "hepem_set_table_l2_window", "hepem_step_limit_bytes", "hepem_howfar", "hepem_perform",
+            "hepem_howfar_host", "hepem_perform_host"]
+FORMS = {"plain": 0, "batched": 1, "mixed": 2}
 STATUS_CANCELLED, STATUS_TIMEOUT, STATUS_OOM_ADMISSION = 8, 5, 6
 
 
@@ -150,6 +152,14 @@ def lib():
         L.hepem_set_table_l2_window.argtypes = [_vp, C.c_int, C.POINTER(C.c_int64)]
         L.hepem_autotune.argtypes = [_vp, C.c_int64, C.POINTER(TrackState), _vp, C.c_int32, C.c_uint64, C.c_int,
                                      C.POINTER(LaunchConfig), _vp]
+        L.hepem_step_limit_bytes.argtypes = [C.c_int64]
+        L.hepem_step_limit_bytes.restype = C.c_int64
+        L.hepem_howfar.argtypes = [_vp, C.c_int, C.c_int64, C.POINTER(TrackState), _vp, C.c_int32, C.c_uint64,
+                                   _vp, _vp, _vp, _vp]
+        L.hepem_howfar_host.argtypes = L.hepem_howfar.argtypes
+        L.hepem_perform.argtypes = [_vp, C.c_int, C.c_int64, C.POINTER(TrackState), C.POINTER(TrackState), _vp,
+                                    _vp, _vp, C.c_int32, C.c_uint64, C.POINTER(StepOut), _vp, _vp]
+        L.hepem_perform_host.argtypes = L.hepem_perform.argtypes
         L.hepem_server_create.argtypes = [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]
         L.hepem_server_capacity.argtypes = [_vp, C.POINTER(C.c_int64)]
         L.hepem_server_submit.argtypes = [_vp, C.c_int64, C.POINTER(TrackState), C.c_uint64, C.POINTER(C.c_int64)]
@@ -258,7 +268,57 @@ class Context:
         check(fn(self.h, n, C.byref(sin), C.byref(sout), _ptr(uniforms), n_uniform, seed, C.byref(sres),
                  _ptr(counters) if counters is not None else None, _stream_ptr(stream)))
 
-    # -- host-buffer entry point (numpy arrays) ----------------------------------
+    # -- HowFar and Perform as two calls (the caller's transport between them) -----
+    def howfar(self, state: dict, uniforms, n_uniform: int, seed: int, gstep=None, limits=None, counters=None,
+               stream=None, form="plain"):
+        """hepem_howfar on device tensors: returns (gstep, limits), the proposed
+        geometrical steps and the step-limit record for perform()."""
+        import torch
+        n = state["ekin"].numel()
+        if gstep is None:
+            gstep = torch.empty(n, dtype=torch.float64, device=state["ekin"].device)
+        if limits is None:
+            limits = torch.empty(max(int(lib().hepem_step_limit_bytes(n)), 1), dtype=torch.uint8,
+                                 device=state["ekin"].device)
+        sin = make_state_struct(state)
+        check(lib().hepem_howfar(self.h, FORMS[form], n, C.byref(sin), _ptr(uniforms) if n_uniform else None,
+                                 n_uniform, seed, _ptr(gstep), _ptr(limits),
+                                 _ptr(counters) if counters is not None else None, _stream_ptr(stream)))
+        return gstep, limits
+
+    def perform(self, state_in: dict, state_out: dict, gstep, limits, uniforms, n_uniform: int, seed: int,
+                res: dict, counters=None, stream=None, form="plain"):
+        """hepem_perform on device tensors (state_in carries the direction and
+        boundary status after transport; gstep the steps made)."""
+        n = state_in["ekin"].numel()
+        sin, sout, sres = make_state_struct(state_in), make_state_struct(state_out), make_out_struct(res)
+        check(lib().hepem_perform(self.h, FORMS[form], n, C.byref(sin), C.byref(sout), _ptr(gstep), _ptr(limits),
+                                  _ptr(uniforms) if n_uniform else None, n_uniform, seed, C.byref(sres),
+                                  _ptr(counters) if counters is not None else None, _stream_ptr(stream)))
+
+    def howfar_host(self, state: dict, uniforms, n_uniform: int, seed: int, form="plain", stream=None):
+        """hepem_howfar_host on numpy arrays: returns (gstep, limits, counters)."""
+        n = len(state["ekin"])
+        gstep = np.empty(n)
+        limits = np.empty(max(int(lib().hepem_step_limit_bytes(n)), 1), dtype=np.uint8)
+        cnt = StepCounters()
+        sin = make_state_struct(state)
+        check(lib().hepem_howfar_host(self.h, FORMS[form], n, C.byref(sin), _ptr(uniforms) if n_uniform else None,
+                                      n_uniform, seed, _ptr(gstep), _ptr(limits), C.byref(cnt),
+                                      _stream_ptr(stream)))
+        return gstep, limits, cnt
+
+    def perform_host(self, state_in: dict, state_out: dict, gstep, limits, uniforms, n_uniform: int, seed: int,
+                     res: dict, form="plain", stream=None):
+        """hepem_perform_host on numpy arrays; returns the counters."""
+        n = len(state_in["ekin"])
+        cnt = StepCounters()
+        sin, sout, sres = make_state_struct(state_in), make_state_struct(state_out), make_out_struct(res)
+        check(lib().hepem_perform_host(self.h, FORMS[form], n, C.byref(sin), C.byref(sout), _ptr(gstep),
+                                       _ptr(limits), _ptr(uniforms) if n_uniform else None, n_uniform, seed,
+                                       C.byref(sres), C.byref(cnt), _stream_ptr(stream)))
+        return cnt
+
     # -- Woodcock gamma tracking ---------------------------------------------------
     def woodcock_gamma(self, state_in: dict, state_out: dict, pos: tuple, box: dict, uniforms, n_uniform: int,
                        seed: int, res: dict, reached=None, stream=None):

@@ -108,6 +108,44 @@ def mixed_batch(n: int, n_couples: int = 3, seed: int = 7, emin=1.0, emax=1.0e4,
     return fresh_state(types, imc, ekin, dirs, safety, ids=np.arange(id0, id0 + n, dtype=np.int32))
 
 
+def transport(state: dict, seed: int, f_short=0.45, f_tiny=0.08, f_zero=0.02, f_turn=0.3):
+    """What a caller's geometry does to a batch between HowFar and Perform.
+
+    Returns (gfrac, new_dir, post_boundary): per track the fraction of the
+    proposed geometrical step that transport makes (1: the proposed step; a
+    shortened step: uniform in (0.05, 1) with probability f_short, log-uniform
+    in [1e-7, 1e-2] with probability f_tiny, 0 with probability f_zero), the
+    direction after transport (e+-: a fraction f_turn turned by up to 0.2 rad,
+    as a magnetic field does; gammas keep theirs), and the post-step boundary
+    status (80% of the shortened steps end on a boundary, 5% of the others)."""
+    n = len(state["ekin"])
+    rng = np.random.Generator(np.random.Philox(seed))
+    u = rng.random(n)
+    gfrac = np.ones(n)
+    short = u < f_short
+    gfrac[short] = 0.05 + 0.95 * rng.random(int(short.sum()))
+    tiny = (u >= f_short) & (u < f_short + f_tiny)
+    gfrac[tiny] = np.exp(np.log(1e-7) + (np.log(1e-2) - np.log(1e-7)) * rng.random(int(tiny.sum())))
+    gfrac[(u >= f_short + f_tiny) & (u < f_short + f_tiny + f_zero)] = 0.0
+    shortened = gfrac < 1.0
+    post = np.where(shortened, rng.random(n) < 0.8, rng.random(n) < 0.05).astype(np.uint8)
+    d = np.stack([state["dir_x"], state["dir_y"], state["dir_z"]], axis=1).copy()
+    turn = (state["type"] != TYPE_GAMMA) & (rng.random(n) < f_turn)
+    k = int(turn.sum())
+    if k:
+        axis = isotropic(rng, k)
+        ang = 0.2 * rng.random(k)
+        v = d[turn]
+        # Rodrigues rotation of v about axis by ang, renormalised
+        c, s = np.cos(ang)[:, None], np.sin(ang)[:, None]
+        kv = np.cross(axis, v)
+        kd = np.sum(axis * v, axis=1)[:, None]
+        w = v * c + kv * s + axis * kd * (1.0 - c)
+        d[turn] = w / np.linalg.norm(w, axis=1)[:, None]
+    new_dir = tuple(np.ascontiguousarray(d[:, j]) for j in range(3))
+    return gfrac, new_dir, post
+
+
 def electron_lookup_batch(n: int, n_couples: int = 3, seed: int = 11, emin=1e-3, emax=1e8):
     """e- energies log-uniform in [1 keV, 100 TeV] and uniform couples."""
     rng = np.random.Generator(np.random.Philox(seed))

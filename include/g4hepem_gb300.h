@@ -235,6 +235,70 @@ int  hepem_step_host_mixed(const hepem_ctx* ctx, int64_t n, const hepem_track_st
                            int32_t n_uniform, uint64_t seed, hepem_step_out* res,
                            hepem_step_counters* counters, void* stream);
 
+/* ---- HowFar and Perform as two calls, with the caller's transport between -- */
+/* The reference client calls HowFar, lets Geant4's transport move the track
+ * -- the geometry may shorten the step, a field may turn the direction, the
+ * step may end on a volume boundary -- and then Perform
+ * (apps/examples/TestEm3/src/G4HepEmProcess.cc:119-197).  hepem_howfar and
+ * hepem_perform are those two calls over a batch:
+ *
+ *   hepem_howfar(ctx, form, n, tracks, ..., gstep, limits, ...)
+ *       e+-: G4HepEmElectronManager::HowFar (G4HepEmElectronManager.hh:71,
+ *       .icc:35-169); gamma: G4HepEmGammaManager::HowFar
+ *       (G4HepEmGammaManager.hh:32, .icc:27-48).  gstep[i] (device, n) =
+ *       the proposed geometrical step; `limits` (device, hepem_step_limit_bytes(n)
+ *       bytes) receives what Perform needs (the reference keeps it in the
+ *       thread-local primary track).  The track state is not modified: the
+ *       sampled numbers of interaction lengths, the MSC step-limit state and
+ *       the uniforms consumed are kept in `limits` until Perform.
+ *   -- the caller transports the tracks: it may lower gstep[i] to the step
+ *      made (0 <= gstep[i]), write the direction after transport to dir_*,
+ *      and set on_boundary[i] to the post-step status (1: the step ended on a
+ *      boundary) --
+ *   hepem_perform(ctx, form, n, in, out, gstep, limits, ..., res, ...)
+ *       e+-: G4HepEmElectronManager::Perform (.hh:222, .icc:171-483), whose
+ *       UpdatePStepLength converts a shortened geometrical step back to the
+ *       true length (.icc:171-203, :653-691); on a boundary no discrete
+ *       interaction happens (.icc:433).  gamma: on a boundary only
+ *       UpdateNumIALeft (G4HepEmGammaManager.icc:95-104, the client's
+ *       G4HepEmProcess.cc:167-171); otherwise SelectInteraction and Perform
+ *       (G4HepEmGammaManager.hh:39,51), as the client calls them back to back
+ *       (G4HepEmProcess.cc:187-188).
+ *
+ * With gstep, direction and on_boundary left as HowFar found them, the pair
+ * gives the results of hepem_step bit for bit.  Both calls take the same n,
+ * the same track order, the same form, the same uniforms/seed (Perform
+ * continues the stream where HowFar stopped), and `in` of hepem_perform is the
+ * state given to hepem_howfar with only dir_*, on_boundary (and, for an
+ * in-place call, nothing else) changed; `out` may alias `in`.
+ * form: HEPEM_FORM_PLAIN (one thread per track, FP64), HEPEM_FORM_BATCHED
+ * (the sorted, queued FP64 form of hepem_step_batched; stream-ordered
+ * workspace) or HEPEM_FORM_MIXED (the precision form of hepem_step_mixed:
+ * results within 1e-5 of the FP64 forms, discrete outcomes identical; e+-
+ * steps that transport shortened, and e+- tracks whose FP32 decisions are too
+ * close to call, are stepped again in FP64 from the pre-step state).
+ * counters (device, may be NULL): hepem_howfar adds the uniforms it consumed;
+ * hepem_perform adds the step, its uniforms, interactions and secondaries. */
+enum { HEPEM_FORM_PLAIN = 0, HEPEM_FORM_BATCHED = 1, HEPEM_FORM_MIXED = 2 };
+int64_t hepem_step_limit_bytes(int64_t n);
+int  hepem_howfar(const hepem_ctx* ctx, int form, int64_t n, const hepem_track_state* tracks,
+                  const double* uniforms, int32_t n_uniform, uint64_t seed, double* gstep, void* limits,
+                  hepem_step_counters* counters, void* stream);
+int  hepem_perform(const hepem_ctx* ctx, int form, int64_t n, const hepem_track_state* in,
+                   hepem_track_state* out, const double* gstep, const void* limits,
+                   const double* uniforms, int32_t n_uniform, uint64_t seed, hepem_step_out* res,
+                   hepem_step_counters* counters, void* stream);
+/* The same two calls with HOST buffers (tracks, uniforms, gstep, limits,
+ * results and counters on the host): each copies its inputs to the device,
+ * runs, copies its outputs back and synchronises.  Pinned memory is fastest. */
+int  hepem_howfar_host(const hepem_ctx* ctx, int form, int64_t n, const hepem_track_state* tracks,
+                       const double* uniforms, int32_t n_uniform, uint64_t seed, double* gstep,
+                       void* limits, hepem_step_counters* counters, void* stream);
+int  hepem_perform_host(const hepem_ctx* ctx, int form, int64_t n, const hepem_track_state* in,
+                        hepem_track_state* out, const double* gstep, const void* limits,
+                        const double* uniforms, int32_t n_uniform, uint64_t seed, hepem_step_out* res,
+                        hepem_step_counters* counters, void* stream);
+
 /* ---- stage timing (profiling aid; not thread-safe) ------------------------ */
 /* enable != 0: the following hepem_step_batched calls on this context record
  * CUDA events around each of their stage kernels (no reference counterpart:

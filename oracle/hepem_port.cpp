@@ -1513,8 +1513,19 @@ struct Step {
   }
 };
 
+// Transport between HowFar and Perform (the caller's geometry): the
+// geometrical step made is gfrac[i] times the proposed one, the track leaves
+// with direction nd*[i] and post-step boundary status post[i]; proposed[i]
+// receives HowFar's geometrical step.  Null: no geometry (the step is the
+// proposed one, direction and boundary status unchanged).
+struct Geo {
+  const double *gfrac, *ndx, *ndy, *ndz;
+  const uint8_t* post;
+  double* proposed;
+};
+
 int step_range(const State& S, int64_t b, int64_t e, const hepem_track_state* in, hepem_track_state* out,
-               const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res) {
+               const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res, const Geo* geo = nullptr) {
   for (int64_t i = b; i < e; ++i) {
     Rng rng{uniforms + i * (int64_t)nu, nu, in->rng_cursor[i], seed, in->id[i], false,
             in->gauss_valid[i] != 0, in->gauss_value[i]};
@@ -1531,6 +1542,14 @@ int step_range(const State& S, int64_t b, int64_t e, const hepem_track_state* in
     if (type == 2) {
       t.charge = 0.0;
       s.gammaHowFar();
+      if (geo) {
+        // G4HepEmProcess.cc:167-197: the step made, the direction after
+        // transport, and the post-step boundary status
+        geo->proposed[i] = t.gstep;
+        t.gstep = geo->gfrac[i] * t.gstep;
+        t.dir[0] = geo->ndx[i]; t.dir[1] = geo->ndy[i]; t.dir[2] = geo->ndz[i];
+        t.onBoundary = geo->post[i] != 0;
+      }
       if (t.onBoundary) {
         t.nia[0] -= t.gstep / t.mfp[0];
       } else {
@@ -1547,6 +1566,12 @@ int step_range(const State& S, int64_t b, int64_t e, const hepem_track_state* in
       t.msc.tlimitMin = in->msc_tlimit_min[i];
       t.msc.firstStep = in->msc_first_step[i] != 0;
       s.elHowFar();
+      if (geo) {
+        geo->proposed[i] = t.gstep;
+        t.gstep = geo->gfrac[i] * t.gstep;
+        t.dir[0] = geo->ndx[i]; t.dir[1] = geo->ndy[i]; t.dir[2] = geo->ndz[i];
+        t.onBoundary = geo->post[i] != 0;
+      }
       s.elPerform();
       pstep = t.pstep;
     }
@@ -1577,6 +1602,7 @@ int step_range(const State& S, int64_t b, int64_t e, const hepem_track_state* in
       out->safety[i] = in->safety[i];
       out->on_boundary[i] = in->on_boundary[i];
     }
+    if (geo) out->on_boundary[i] = geo->post[i];
     res->edep[i] = t.edep;
     res->gstep[i] = t.gstep;
     res->pstep[i] = pstep;
@@ -1875,6 +1901,17 @@ void port_conv_select_target(void* st, int64_t n, const double* ekin, const int3
 int port_step(void* st, int64_t n, const hepem_track_state* in, hepem_track_state* out, const double* u,
               int32_t nu, uint64_t seed, hepem_step_out* res) {
   return port::step_range(*static_cast<port::State*>(st), 0, n, in, out, u, nu, seed, res);
+}
+
+// HowFar, the caller's transport (step gfrac * proposed, direction nd*,
+// post-step boundary status post), then Perform, in the order of
+// G4HepEmProcess (apps/examples/TestEm3/src/G4HepEmProcess.cc:119-197);
+// proposed[i] receives HowFar's geometrical step.
+int port_step_geom(void* st, int64_t n, const hepem_track_state* in, hepem_track_state* out, const double* u,
+                   int32_t nu, uint64_t seed, const double* gfrac, const double* ndx, const double* ndy,
+                   const double* ndz, const uint8_t* post, double* proposed, hepem_step_out* res) {
+  const port::Geo geo{gfrac, ndx, ndy, ndz, post, proposed};
+  return port::step_range(*static_cast<port::State*>(st), 0, n, in, out, u, nu, seed, res, &geo);
 }
 
 // The same over `threads` host threads (static partition of the batch).

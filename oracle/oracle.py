@@ -117,6 +117,10 @@ class _Lib:
                                                          _ip]
         getattr(L, p + "gamma_xs").argtypes = [C.c_void_p, C.c_int64, _dp, _ip, _dp, _dp, _dp, _ip]
         getattr(L, p + "conv_select_target").argtypes = [C.c_void_p, C.c_int64, _dp, _ip, _dp, _ip]
+        getattr(L, p + "step_geom").argtypes = [C.c_void_p, C.c_int64, C.POINTER(TrackState),
+                                                C.POINTER(TrackState), _dp, C.c_int32, C.c_uint64, _dp, _dp,
+                                                _dp, _dp, _ubp, _dp, C.POINTER(StepOut)]
+        getattr(L, p + "step_geom").restype = C.c_int
         self.st = None
 
     def _f(self, name):
@@ -195,6 +199,27 @@ class _Lib:
         if rc != 0:
             raise RuntimeError(f"step failed rc={rc}")
         return out_state, res
+
+
+    def step_geom(self, state: dict, uniforms, n_uniform, seed, gfrac, new_dir, post_boundary):
+        """HowFar, then a caller's transport -- geometrical step gfrac times the
+        proposed one, direction new_dir = (x, y, z) arrays, post-step boundary
+        status -- then Perform.  Returns (out_state, res, proposed)."""
+        n = len(state["ekin"])
+        out_state = copy_state(state)
+        res = alloc_out(n)
+        gfrac = np.ascontiguousarray(gfrac, dtype=np.float64)
+        nd = [np.ascontiguousarray(a, dtype=np.float64) for a in new_dir]
+        post = np.ascontiguousarray(post_boundary, dtype=np.uint8)
+        proposed = np.empty(n)
+        sin, sout, sres = make_state_struct(state), make_state_struct(out_state), make_out_struct(res)
+        u = np.ascontiguousarray(uniforms, dtype=np.float64)
+        rc = self._f("step_geom")(self.st, n, C.byref(sin), C.byref(sout), _ptr(u, _dp), n_uniform, seed,
+                                  _ptr(gfrac, _dp), *[_ptr(a, _dp) for a in nd], _ptr(post, _ubp),
+                                  _ptr(proposed, _dp), C.byref(sres))
+        if rc != 0:
+            raise RuntimeError(f"step failed rc={rc}")
+        return out_state, res, proposed
 
 
 class RefLib(_Lib):

@@ -331,4 +331,158 @@ int ref_step(void* st, int64_t n, const hepem_track_state* in, hepem_track_state
   return 0;
 }
 
+// HowFar, then the transport of a caller, then Perform, per track, in the
+// order of G4HepEmProcess::PostStepGetPhysicalInteractionLength and
+// ::PostStepDoIt (apps/examples/TestEm3/src/G4HepEmProcess.cc:119-197).
+// `in` holds the pre-step state (on_boundary: the pre-step point's status).
+// proposed[i] receives the geometrical step HowFar proposes; transport then
+// makes the geometrical step gfrac[i] * proposed[i] (gfrac 1: the proposed
+// step itself), leaves the track with direction (ndx, ndy, ndz)[i] and
+// post-step boundary status post_bnd[i].  A gamma on a boundary only updates
+// its number of interaction lengths left (G4HepEmProcess.cc:167-171); every
+// other track gets the new direction, step and status before Perform
+// (:175-197), gammas after SelectInteraction.  The direction is set for a
+// boundary gamma too (the reference leaves it to Geant4, which moved it).
+int ref_step_geom(void* st, int64_t n, const hepem_track_state* in, hepem_track_state* out,
+                  const double* uniforms, int32_t n_uniform, uint64_t seed, const double* gfrac,
+                  const double* ndx, const double* ndy, const double* ndz, const uint8_t* post_bnd,
+                  double* proposed, hepem_step_out* res) {
+  G4HepEmState* s = static_cast<G4HepEmState*>(st);
+  G4HepEmData* d = s->fData;
+  G4HepEmParameters* p = s->fParameters;
+  G4HepEmTLData tl;
+  for (int64_t i = 0; i < n; ++i) {
+    Stream strm{uniforms + i * (int64_t)n_uniform, n_uniform, in->rng_cursor[i], seed, in->id[i], 0};
+    G4HepEmRandomEngine rng(&strm);
+    rng.fIsGauss = in->gauss_valid[i] != 0;
+    rng.fGauss = in->gauss_value[i];
+    tl.SetRandomEngine(&rng);
+    tl.ResetNumSecondaryElectronTrack();
+    tl.ResetNumSecondaryGammaTrack();
+    const int type = in->type[i];
+    const bool post = post_bnd[i] != 0;
+    G4HepEmTrack* t = nullptr;
+    double pstep = 0.0;
+    const double* disp = nullptr;
+    double zero3[3] = {0.0, 0.0, 0.0};
+    G4HepEmMSCTrackData* msc = nullptr;
+    if (type == 2) {
+      G4HepEmGammaTrack* gt = tl.GetPrimaryGammaTrack();
+      gt->ReSet();
+      t = gt->GetTrack();
+      t->SetCharge(0.0);
+      t->SetEKin(in->ekin[i]);
+      t->SetDirection(in->dir_x[i], in->dir_y[i], in->dir_z[i]);
+      t->SetMCIndex(in->imc[i]);
+      t->SetID(in->id[i]);
+      t->SetNumIALeft(in->nia0[i], 0);
+      t->SetOnBoundary(in->on_boundary[i] != 0);
+      G4HepEmGammaManager::HowFar(d, p, &tl);
+      proposed[i] = t->GetGStepLength();
+      const double g = gfrac[i] * proposed[i];
+      t->SetDirection(ndx[i], ndy[i], ndz[i]);
+      if (post) {
+        t->SetGStepLength(g);
+        G4HepEmGammaManager::UpdateNumIALeft(t);
+      } else {
+        t->SetGStepLength(g);
+        t->SetOnBoundary(false);
+        G4HepEmGammaManager::SelectInteraction(d, &tl);
+        G4HepEmGammaManager::Perform(d, p, &tl);
+      }
+      pstep = t->GetGStepLength();
+      disp = zero3;
+    } else {
+      G4HepEmElectronTrack* et = tl.GetPrimaryElectronTrack();
+      et->ReSet();
+      t = et->GetTrack();
+      t->SetCharge(type == 0 ? -1.0 : 1.0);
+      t->SetEKin(in->ekin[i]);
+      t->SetDirection(in->dir_x[i], in->dir_y[i], in->dir_z[i]);
+      t->SetMCIndex(in->imc[i]);
+      t->SetID(in->id[i]);
+      t->SetNumIALeft(in->nia0[i], 0);
+      t->SetNumIALeft(in->nia1[i], 1);
+      t->SetNumIALeft(in->nia2[i], 2);
+      t->SetNumIALeft(in->nia3[i], 3);
+      t->SetSafety(in->safety[i]);
+      t->SetOnBoundary(in->on_boundary[i] != 0);
+      msc = et->GetMSCTrackData();
+      msc->fInitialRange = in->msc_init_range[i];
+      msc->fDynamicRangeFactor = in->msc_dyn_factor[i];
+      msc->fTlimitMin = in->msc_tlimit_min[i];
+      msc->fIsFirstStep = in->msc_first_step[i] != 0;
+      G4HepEmElectronManager::HowFar(d, p, &tl);
+      proposed[i] = t->GetGStepLength();
+      const double g = gfrac[i] * proposed[i];
+      t->SetDirection(ndx[i], ndy[i], ndz[i]);
+      t->SetGStepLength(g);
+      t->SetOnBoundary(post);
+      G4HepEmElectronManager::Perform(d, p, &tl);
+      pstep = et->GetPStepLength();
+      disp = msc->GetDisplacement();
+    }
+    out->ekin[i] = t->GetEKin();
+    const double* nd = t->GetDirection();
+    out->dir_x[i] = nd[0]; out->dir_y[i] = nd[1]; out->dir_z[i] = nd[2];
+    out->nia0[i] = t->GetNumIALeft(0);
+    if (type != 2) {
+      out->nia1[i] = t->GetNumIALeft(1);
+      out->nia2[i] = t->GetNumIALeft(2);
+      out->nia3[i] = t->GetNumIALeft(3);
+      out->msc_init_range[i] = msc->fInitialRange;
+      out->msc_dyn_factor[i] = msc->fDynamicRangeFactor;
+      out->msc_tlimit_min[i] = msc->fTlimitMin;
+      out->msc_first_step[i] = msc->fIsFirstStep ? 1 : 0;
+    } else {
+      out->nia1[i] = in->nia1[i];
+      out->nia2[i] = in->nia2[i];
+      out->nia3[i] = in->nia3[i];
+      out->msc_init_range[i] = in->msc_init_range[i];
+      out->msc_dyn_factor[i] = in->msc_dyn_factor[i];
+      out->msc_tlimit_min[i] = in->msc_tlimit_min[i];
+      out->msc_first_step[i] = in->msc_first_step[i];
+    }
+    out->gauss_valid[i] = rng.fIsGauss ? 1 : 0;
+    out->gauss_value[i] = rng.fGauss;
+    out->rng_cursor[i] = strm.cursor;
+    out->type[i] = in->type[i];
+    out->imc[i] = in->imc[i];
+    out->id[i] = in->id[i];
+    out->safety[i] = in->safety[i];
+    out->on_boundary[i] = post_bnd[i];
+    res->edep[i] = t->GetEnergyDeposit();
+    res->gstep[i] = t->GetGStepLength();
+    res->pstep[i] = pstep;
+    res->winner[i] = (int8_t)t->GetWinnerProcessIndex();
+    res->disp_x[i] = disp[0]; res->disp_y[i] = disp[1]; res->disp_z[i] = disp[2];
+    res->flags[i] = strm.overflow ? 1 : 0;
+    int ns = 0;
+    const int nel = (int)tl.GetNumSecondaryElectronTrack();
+    const int ngm = (int)tl.GetNumSecondaryGammaTrack();
+    for (int k = 0; k < nel && ns < 2; ++k, ++ns) {
+      G4HepEmTrack* sec = tl.GetSecondaryElectronTrack(k)->GetTrack();
+      const bool isPos = (type == 2 && res->winner[i] == 0 && k == 1);
+      res->sec_type[2 * i + ns] = isPos ? 1 : 0;
+      res->sec_ekin[2 * i + ns] = sec->GetEKin();
+      const double* sd = sec->GetDirection();
+      res->sec_dir_x[2 * i + ns] = sd[0];
+      res->sec_dir_y[2 * i + ns] = sd[1];
+      res->sec_dir_z[2 * i + ns] = sd[2];
+    }
+    for (int k = 0; k < ngm && ns < 2; ++k, ++ns) {
+      G4HepEmTrack* sec = tl.GetSecondaryGammaTrack(k)->GetTrack();
+      res->sec_type[2 * i + ns] = 2;
+      res->sec_ekin[2 * i + ns] = sec->GetEKin();
+      const double* sd = sec->GetDirection();
+      res->sec_dir_x[2 * i + ns] = sd[0];
+      res->sec_dir_y[2 * i + ns] = sd[1];
+      res->sec_dir_z[2 * i + ns] = sd[2];
+    }
+    res->n_sec[i] = (int8_t)ns;
+    if (nel + ngm > 2) return -1;
+  }
+  return 0;
+}
+
 }  // extern "C"

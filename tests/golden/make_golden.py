@@ -11,7 +11,9 @@ sections, target-element selectors (brem SB/RB for e- and e+, conversion),
 gamma cross sections and interaction selection, on three and on sixteen
 couples, and full HowFar+Perform steps (fresh tracks, a second step that
 carries MSC/Gauss/RNG state, boundary and safety variants, and a 16-couple
-table with two regions).  Uniform streams are not stored: they are the Philox
+table with two regions), and steps whose geometry shortens the proposed
+step, turns charged tracks and ends steps on a boundary between HowFar and
+Perform (`--only-geometry` writes just those).  Uniform streams are not stored: they are the Philox
 streams of the C-ABI contract and are regenerated from (seed, id).
 """
 from __future__ import annotations
@@ -55,6 +57,41 @@ def step_fixture(ref, state, seed, nu=NU, prefix=""):
     return d, out
 
 
+def geom_fixture(ref, state, seed, tseed, nu=NU, prefix=""):
+    """HowFar, a caller's transport (workload.transport), Perform."""
+    u = W.philox_uniforms(seed, state["id"], nu)
+    gfrac, nd, post = W.transport(state, tseed)
+    out, res, proposed = ref.step_geom(state, u, nu, seed, gfrac, nd, post)
+    d = {f"{prefix}gfrac": gfrac, f"{prefix}ndir_x": nd[0], f"{prefix}ndir_y": nd[1], f"{prefix}ndir_z": nd[2],
+         f"{prefix}post_bnd": post, f"{prefix}proposed": proposed}
+    for k, v in state.items():
+        d[f"{prefix}in_{k}"] = v
+    for k, v in out.items():
+        d[f"{prefix}out_{k}"] = v
+    for k, v in res.items():
+        d[f"{prefix}res_{k}"] = v
+    return d, out
+
+
+def geometry_fixtures():
+    """Geometry-limited steps: HowFar, transport that shortens the step,
+    turns charged tracks and sets the post-step boundary status, Perform; a
+    first and a second step on three couples, one step on sixteen."""
+    ref = O.RefLib().load(T3)
+    st = wide_batch(8192, 3, 31)
+    d1, out1 = geom_fixture(ref, st, SEED + 10, 101, prefix="g1_")
+    st2 = O.copy_state(out1)
+    st2["rng_cursor"] = np.zeros_like(st2["rng_cursor"])
+    alive = st2["ekin"] > 0
+    st2 = {k: np.ascontiguousarray(v[alive]) for k, v in st2.items()}
+    d2, _ = geom_fixture(ref, st2, SEED + 11, 102, prefix="g2_")
+    save("geosteps_3couples.npz", seed=np.array([SEED + 10, SEED + 11]), nu=np.array([NU]), **d1, **d2)
+    ref16 = O.RefLib().load(T16)
+    st = wide_batch(8192, 16, 32)
+    d3, _ = geom_fixture(ref16, st, SEED + 12, 103, prefix="g1_")
+    save("geosteps_16couples.npz", seed=np.array([SEED + 12]), nu=np.array([NU]), **d3)
+
+
 def wide_batch(n, n_couples, seed):
     """Energies log-uniform 1 keV - 100 TeV, 10% on a boundary, 10% zero safety."""
     st = W.mixed_batch(n, n_couples=n_couples, seed=seed, emin=1e-3, emax=1e8, frac=(0.4, 0.4, 0.2))
@@ -65,6 +102,11 @@ def wide_batch(n, n_couples, seed):
 
 
 def main():
+    if "--only-geometry" in sys.argv:
+        if not O.build_ref():
+            raise SystemExit("could not build oracle/_ref (reference sources missing?)")
+        geometry_fixtures()
+        return
     if not os.path.exists(T16):
         regions = [dict(), dict(fIsMSCMinimalStepLimit=True, fIsELossFluctuation=False, fLinELossLimit=0.02,
                                 fFinalRange=0.1, fDRoverRange=0.8, fMSCRangeFactor=0.08)]
@@ -143,6 +185,8 @@ def main():
         for k, v in ref16.electron_xs_stepping(es, ic, bool(pos)).items():
             d[f"p{pos}_step_{k}"] = v
     save("selectors_16couples.npz", **d)
+
+    geometry_fixtures()
 
 
 if __name__ == "__main__":

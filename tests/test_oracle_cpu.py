@@ -156,3 +156,57 @@ def test_port_in_place_equals_out_of_place(port):
     o2, r2 = p.step(st2, u, 64, 5, in_place=True)
     for k in o1:
         assert np.array_equal(o1[k], o2[k])
+
+
+GEO_CASES = [("geosteps_3couples.npz", T3, "g1_", 0), ("geosteps_3couples.npz", T3, "g2_", 1),
+             ("geosteps_16couples.npz", T16, "g1_", 0)]
+
+
+def geo_inputs(g, prefix):
+    """Pre-step state, transport (step fraction, direction after transport,
+    post-step boundary status) of a geometry fixture."""
+    st = golden_state(g, prefix, "in")
+    nd = tuple(np.ascontiguousarray(g[f"{prefix}ndir_{c}"]) for c in "xyz")
+    return st, g[f"{prefix}gfrac"], nd, np.ascontiguousarray(g[f"{prefix}post_bnd"])
+
+
+@pytest.mark.parametrize("name,table,prefix,k", GEO_CASES)
+def test_port_geometry_steps_match_reference_golden(port, name, table, prefix, k):
+    """HowFar, a transport that shortens the step (some below the MSC
+    geometrical length and below 1e-6 mm, some to 0), turns charged tracks and
+    ends steps on a boundary, then Perform: the port equals the reference bit
+    for bit, including the geometrical -> true length conversion
+    (G4HepEmElectronManager.icc:171-203, :653-691) and the gamma boundary exit
+    (G4HepEmProcess.cc:167-171)."""
+    g = load_golden(name)
+    seed, nu = int(g["seed"][k]), int(g["nu"][0])
+    st, gfrac, nd, post = geo_inputs(g, prefix)
+    u = W.philox_uniforms(seed, st["id"], nu)
+    out, res, proposed = port(table).step_geom(st, u, nu, seed, gfrac, nd, post)
+    assert np.array_equal(proposed, g[f"{prefix}proposed"])
+    ref_out, ref_res = golden_state(g, prefix, "out"), golden_res(g, prefix)
+    for key in ref_out:
+        assert np.array_equal(out[key], ref_out[key]), key
+    for key in ref_res:
+        assert np.array_equal(res[key], ref_res[key]), key
+
+
+def test_geometry_fixtures_cover_the_branches():
+    """The fixtures exercise what a geometry-free step never reaches: e+-
+    steps whose true length was recomputed from a shorter geometrical one
+    (pstep > gstep, gstep < proposed), steps shortened below 1e-6 mm and to
+    0, e+- steps ending on a boundary (no discrete interaction), and gammas
+    taking the boundary exit (nia0 updated, no interaction)."""
+    g = load_golden("geosteps_3couples.npz")
+    for prefix in ("g1_", "g2_"):
+        st, gfrac, _, post = geo_inputs(g, prefix)
+        res = golden_res(g, prefix)
+        ch = st["type"] != 2
+        shortened = gfrac < 1.0
+        conv = ch & shortened & (res["pstep"] > res["gstep"])
+        assert conv.sum() > 500, prefix
+        assert np.sum(ch & shortened & (res["gstep"] > 0) & (res["gstep"] < 1e-6)) > 20, prefix
+        assert np.sum(gfrac == 0.0) > 20
+        assert np.sum(ch & (post == 1) & (res["winner"] >= 0)) > 100
+        gb = (st["type"] == 2) & (post == 1)
+        assert gb.sum() > 200 and np.all(res["n_sec"][gb] == 0)
