@@ -449,6 +449,48 @@ int hepem_step_host_mixed(const hepem_ctx* c, int64_t n, const hepem_track_state
   return step_host(c, n, in, out, uniforms, nu, seed, res, counters, stream, true);
 }
 
+// ---- single functions of the path (the reference's device-test quantities) -------------
+namespace {
+int probe(const hepem_ctx* c, hepem::ProbeArgs& a, int precision, void* stream) {
+  if (!c || a.n < 0 || !(precision == 0 || precision == 1)) return fail(HEPEM_BAD_ARG, "bad context, size or precision");
+  if (a.n == 0) return HEPEM_OK;
+  if (!a.ekin || !a.imc) return fail(HEPEM_BAD_ARG, "null array");
+  HEPEM_CUDA(hepem::launch_probe(c->tables, a, precision, (cudaStream_t)stream, c->sms));
+  return HEPEM_OK;
+}
+}  // namespace
+
+int hepem_electron_xs_stepping(const hepem_ctx* c, int64_t n, int is_positron, int precision, const double* ekin,
+                               const int32_t* imc, double* xi, double* xb, double* xa, double* xn, double* tr,
+                               void* stream) {
+  if (n > 0 && (!xi || !xb || !xa || !xn || !tr)) return fail(HEPEM_BAD_ARG, "null output");
+  hepem::ProbeArgs a{n, hepem::kProbeElXs, is_positron ? 1 : 0, 0, ekin, imc, nullptr, {xi, xb, xa, xn, tr}, nullptr};
+  return probe(c, a, precision, stream);
+}
+
+int hepem_brem_select_target(const hepem_ctx* c, int64_t n, int is_positron, int is_sb, int precision,
+                             const double* ekin, const int32_t* imc, const double* urnd, int32_t* elem,
+                             void* stream) {
+  if (n > 0 && (!urnd || !elem)) return fail(HEPEM_BAD_ARG, "null array");
+  hepem::ProbeArgs a{n, hepem::kProbeBremTarget, is_positron ? 1 : 0, is_sb ? 1 : 0, ekin, imc, urnd, {}, elem};
+  return probe(c, a, precision, stream);
+}
+
+int hepem_conv_select_target(const hepem_ctx* c, int64_t n, int precision, const double* ekin, const int32_t* imc,
+                             const double* urnd, int32_t* elem, void* stream) {
+  if (n > 0 && (!urnd || !elem)) return fail(HEPEM_BAD_ARG, "null array");
+  hepem::ProbeArgs a{n, hepem::kProbeConvTarget, 0, 0, ekin, imc, urnd, {}, elem};
+  return probe(c, a, precision, stream);
+}
+
+int hepem_gamma_xs(const hepem_ctx* c, int64_t n, int precision, const double* ekin, const int32_t* imc,
+                   const double* urnd, double* xs_tot, double* xs_pe, int32_t* winner, void* stream) {
+  if (n > 0 && (!urnd || !xs_tot || !xs_pe || !winner)) return fail(HEPEM_BAD_ARG, "null array");
+  hepem::ProbeArgs a{n, hepem::kProbeGammaXs, 0, 0, ekin, imc, urnd, {xs_tot, xs_pe, nullptr, nullptr, nullptr},
+                     winner};
+  return probe(c, a, precision, stream);
+}
+
 // ---- HowFar and Perform as two calls ----------------------------------------------------
 int64_t hepem_step_limit_bytes(int64_t n) { return n < 0 ? 0 : (int64_t)hepem::limits_bytes(n); }
 

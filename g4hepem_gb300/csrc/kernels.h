@@ -139,6 +139,20 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
 enum { kSampleSB = 0, kSampleRB = 1, kSampleMoller = 2, kSampleBhabha = 3, kSampleCompton = 4, kSampleConversion = 5 };
 cudaError_t launch_sample(const DevTables& T, int model, int mixed, int64_t n, double ekin, int imc, uint64_t seed,
                           double* out, unsigned long long* nFallback, cudaStream_t s, int sms);
+// the quantities of the reference's device tests, function by function
+// (hepem_electron_xs_stepping, hepem_brem_select_target,
+// hepem_conv_select_target, hepem_gamma_xs)
+enum { kProbeElXs = 0, kProbeBremTarget = 1, kProbeConvTarget = 2, kProbeGammaXs = 3 };
+struct ProbeArgs {
+  int64_t n;
+  int kind, positron, sb;
+  const double* ekin;
+  const int32_t* imc;
+  const double* urnd;
+  double* out[5];
+  int32_t* iout;
+};
+cudaError_t launch_probe(const DevTables& T, const ProbeArgs& a, int mixed, cudaStream_t s, int sms);
 // stage timing: events recorded before the first and after every stage kernel
 constexpr int kNumStageEvents = 13;
 const char* stage_name(int i);

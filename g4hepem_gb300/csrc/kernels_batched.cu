@@ -1229,6 +1229,129 @@ cudaError_t launch_sample(const DevTables& T, int model, int mixed, int64_t n, d
 }
 #endif  // HEPEM_FP64_UNIT
 
+// ---- 5. the quantities of the reference's device tests -----------------------------------
+// One function of the path per kernel, on given energies, couples and
+// uniforms: the step-limit cross sections of e+- (G4HepEmElectronManager.icc:
+// 534-599, testing/ElectronXSections/src/ResMacXSecs.cu:16-33), the target
+// element of brem (G4HepEmElectronInteractionBrem SelectTargetAtom,
+// testing/ElectronTargetElementSelector/src/ElemSelector.cu:14-30) and of
+// pair production (G4HepEmGammaInteractionConversion SelectTargetAtom,
+// testing/GammaTargetElementSelector/src/GammaElemSelector.cu:14-27), the
+// gamma total cross section and the interaction it selects
+// (G4HepEmGammaManager.icc:108-219, testing/GammaXSections/src/
+// GammaMacXSecs.cu:20-30).  MIXED: the FP32 code of the precision form, where
+// a selection too close to call is made again in FP64 as in the step.
+template <bool MIXED>
+__global__ void __launch_bounds__(256) probe_kernel(const __grid_constant__ DevTables T, const ProbeArgs a) {
+  const double nan = __longlong_as_double(0x7FF8000000000000LL);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double e = a.ekin[i];
+    const int c = a.imc[i];
+    if (track_input_bad(T, 0, c, e)) {
+      if (a.kind == kProbeElXs || a.kind == kProbeGammaXs)
+        for (int k = 0; k < 5; ++k)
+          if (a.out[k]) a.out[k][i] = nan;
+      if (a.iout) a.iout[i] = -1;
+      continue;
+    }
+    const int imat = ld(&T.couples[c].mat);
+    Track t;
+    Rng rng;
+    t.imc = c;
+    t.setE(e);
+    t.isEl = !a.positron;
+    t.flags = 0;
+    t.nsec = 0;
+    t.onBoundary = false;
+    t.nia[0] = 1.0;
+    t.peXS = 0.0;
+    rng.u = a.urnd ? a.urnd + i : nullptr;
+    rng.n = a.urnd ? 1 : 0;
+    rng.cursor = 0;
+    rng.id = (int32_t)i;
+    rng.overflow = 0u;
+    rng.seed = 0;
+    rng.gaussValid = false;
+    rng.gaussValue = 0.0;
+    if (a.kind == kProbeElXs) {
+      const DevElData& d = T.el[a.positron ? 1 : 0];
+      double v[5];
+      if (MIXED) {
+        const DevElData32& f = T.el32[a.positron ? 1 : 0];
+        const float ef = d2f(e), lef = logf(ef);
+        v[0] = (double)rest_macxs_stepping32(d, f, c, e, ef, lef, true);
+        v[1] = (double)rest_macxs_stepping32(d, f, c, e, ef, lef, false);
+        v[2] = a.positron ? (double)annih_macxs32(0.8f * ef, ld(&T.mats32[imat].elDensity)) : 0.0;
+        v[3] = (double)nuc_macxs32(d, f, imat, e, ef, lef);
+        v[4] = (double)transport_mfp32(f, d.nLoss, imat, ef, lef);
+      } else {
+        const double le = vdt_log(e);
+        v[0] = rest_macxs_stepping(d, c, e, le, true);
+        v[1] = rest_macxs_stepping(d, c, e, le, false);
+        v[2] = a.positron ? annih_macxs(0.8 * e, ld(&T.mats[imat].elDensity)) : 0.0;
+        v[3] = nuc_macxs(d, imat, e, le);
+        v[4] = transport_mfp(d, imat, e, le);
+      }
+      for (int k = 0; k < 5; ++k) a.out[k][i] = v[k];
+    } else if (a.kind == kProbeBremTarget || a.kind == kProbeConvTarget) {
+      int k = 0;
+      if (ld(&T.mats[imat].nElem) > 1) {
+        const double u = a.urnd[i];
+        bool redo = !MIXED;
+        if (MIXED) {
+          MixedB M{T, rng, t, false};
+          k = a.kind == kProbeBremTarget ? M.select_brem_target(e, f2d(logf(d2f(e))), u, a.sb ? 1 : 2)
+                                         : M.conv_target32(imat, e, u);
+          redo = M.trip;
+        }
+        if (redo) {
+          Physics P{T, rng, t};
+          k = a.kind == kProbeBremTarget ? P.select_brem_target(e, vdt_log(e), u, a.sb ? 1 : 2)
+                                         : P.conv_target(imat, e, vdt_log(e), u);
+        }
+      }
+      a.iout[i] = k;
+    } else {
+      double tot;
+      if (MIXED) {
+        MixedG G{T, rng, t, false};
+        GammaLimit32 q;
+        G.howfar(q);
+        tot = (double)q.tot;
+        G.perform(q, 0.f);
+      } else {
+        Physics P{T, rng, t};
+        tot = P.gamma_total_xs();
+        t.mfp[0] = tot > 0. ? 1. / tot : kLarge;
+        P.gamma_select();
+      }
+      a.out[0][i] = tot;
+      a.out[1][i] = t.winner == 2 ? t.peXS : 0.0;
+      a.iout[i] = t.winner;
+    }
+  }
+}
+
+static int probe_grid(int64_t n, int sms) {
+  const int64_t b = (n + 255) / 256;
+  return (int)(b < (int64_t)sms * 16 ? (b > 0 ? b : 1) : (int64_t)sms * 16);
+}
+
+#if HEPEM_FP64_UNIT
+cudaError_t launch_probe_mixed(const DevTables& T, const ProbeArgs& a, cudaStream_t s, int sms);
+cudaError_t launch_probe(const DevTables& T, const ProbeArgs& a, int mixed, cudaStream_t s, int sms) {
+  if (a.n <= 0) return cudaSuccess;
+  if (mixed) return launch_probe_mixed(T, a, s, sms);
+  probe_kernel<false><<<probe_grid(a.n, sms), 256, 0, s>>>(T, a);
+  return cudaGetLastError();
+}
+#else
+cudaError_t launch_probe_mixed(const DevTables& T, const ProbeArgs& a, cudaStream_t s, int sms) {
+  probe_kernel<true><<<probe_grid(a.n, sms), 256, 0, s>>>(T, a);
+  return cudaGetLastError();
+}
+#endif
+
 }  // namespace hepem
 
 // diagnostics exports: the trip counters of the precision form's kernels live

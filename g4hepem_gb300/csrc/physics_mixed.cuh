@@ -1137,7 +1137,7 @@ static __device__ __noinline__ int gamma_select64(const DevTables& T, Track& t, 
 
 // What the FP32 HowFar of MixedG leaves for its Perform.
 struct GammaLimit32 {
-  float mfp, pe, nia0, gstep;
+  float tot, mfp, pe, nia0, gstep;
 };
 
 struct MixedG {
@@ -1211,6 +1211,7 @@ struct MixedG {
       pe = fmx(0.f, macxs_pe32(imat, e, ef));
       tot = y1 + b * (ld(d + i2 + 3) - y1) + pe;
     }
+    q.tot = tot;
     q.mfp = tot > 0.f ? 1.f / tot : kLargeF;
     q.pe = pe;
     q.nia0 = d2f(t.nia[0]);

@@ -94,7 +94,8 @@ EXPORTED = ["hepem_create", "hepem_create_from_file", "hepem_image_from_json", "
             "hepem_server_wait", "hepem_server_cancel", "hepem_server_get_stats", "hepem_server_reset_stats",
             "hepem_server_destroy", "hepem_sample_model", "hepem_stack_secondaries", "hepem_woodcock_gamma", "hepem_get_launch_config", "hepem_set_launch_config", "hepem_autotune",
             "hepem_set_table_l2_window", "hepem_step_limit_bytes", "hepem_howfar", "hepem_perform",
-            "hepem_howfar_host", "hepem_perform_host"]
+            "hepem_howfar_host", "hepem_perform_host", "hepem_electron_xs_stepping", "hepem_brem_select_target",
+            "hepem_conv_select_target", "hepem_gamma_xs"]
 FORMS = {"plain": 0, "batched": 1, "mixed": 2}
 STATUS_CANCELLED, STATUS_TIMEOUT, STATUS_OOM_ADMISSION = 8, 5, 6
 
@@ -160,6 +161,10 @@ def lib():
         L.hepem_perform.argtypes = [_vp, C.c_int, C.c_int64, C.POINTER(TrackState), C.POINTER(TrackState), _vp,
                                     _vp, _vp, C.c_int32, C.c_uint64, C.POINTER(StepOut), _vp, _vp]
         L.hepem_perform_host.argtypes = L.hepem_perform.argtypes
+        L.hepem_electron_xs_stepping.argtypes = [_vp, C.c_int64, C.c_int, C.c_int] + [_vp] * 7 + [_vp]
+        L.hepem_brem_select_target.argtypes = [_vp, C.c_int64, C.c_int, C.c_int, C.c_int] + [_vp] * 4 + [_vp]
+        L.hepem_conv_select_target.argtypes = [_vp, C.c_int64, C.c_int] + [_vp] * 4 + [_vp]
+        L.hepem_gamma_xs.argtypes = [_vp, C.c_int64, C.c_int] + [_vp] * 6 + [_vp]
         L.hepem_server_create.argtypes = [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]
         L.hepem_server_capacity.argtypes = [_vp, C.POINTER(C.c_int64)]
         L.hepem_server_submit.argtypes = [_vp, C.c_int64, C.POINTER(TrackState), C.c_uint64, C.POINTER(C.c_int64)]
@@ -267,6 +272,40 @@ class Context:
               "noalloc": lib().hepem_step_batched_noalloc}[form]
         check(fn(self.h, n, C.byref(sin), C.byref(sout), _ptr(uniforms), n_uniform, seed, C.byref(sres),
                  _ptr(counters) if counters is not None else None, _stream_ptr(stream)))
+
+    # -- single functions of the path (the reference's device-test quantities) ----
+    def electron_xs_stepping(self, ekin, imc, positron=False, mixed=False, stream=None):
+        import torch
+        n = ekin.numel()
+        out = {k: torch.empty(n, dtype=torch.float64, device=ekin.device)
+               for k in ("xs_ioni", "xs_brem", "xs_annih", "xs_nuc", "tr_mfp")}
+        check(lib().hepem_electron_xs_stepping(self.h, n, int(positron), int(mixed), _ptr(ekin), _ptr(imc),
+                                               *[_ptr(v) for v in out.values()], _stream_ptr(stream)))
+        return out
+
+    def brem_select_target(self, ekin, imc, urnd, positron=False, sb=True, mixed=False, stream=None):
+        import torch
+        out = torch.empty(ekin.numel(), dtype=torch.int32, device=ekin.device)
+        check(lib().hepem_brem_select_target(self.h, ekin.numel(), int(positron), int(sb), int(mixed), _ptr(ekin),
+                                             _ptr(imc), _ptr(urnd), _ptr(out), _stream_ptr(stream)))
+        return out
+
+    def conv_select_target(self, ekin, imc, urnd, mixed=False, stream=None):
+        import torch
+        out = torch.empty(ekin.numel(), dtype=torch.int32, device=ekin.device)
+        check(lib().hepem_conv_select_target(self.h, ekin.numel(), int(mixed), _ptr(ekin), _ptr(imc), _ptr(urnd),
+                                             _ptr(out), _stream_ptr(stream)))
+        return out
+
+    def gamma_xs(self, ekin, imc, urnd, mixed=False, stream=None):
+        import torch
+        n = ekin.numel()
+        tot = torch.empty(n, dtype=torch.float64, device=ekin.device)
+        pe = torch.empty(n, dtype=torch.float64, device=ekin.device)
+        win = torch.empty(n, dtype=torch.int32, device=ekin.device)
+        check(lib().hepem_gamma_xs(self.h, n, int(mixed), _ptr(ekin), _ptr(imc), _ptr(urnd), _ptr(tot), _ptr(pe),
+                                   _ptr(win), _stream_ptr(stream)))
+        return dict(xs_tot=tot, xs_pe=pe, winner=win)
 
     # -- HowFar and Perform as two calls (the caller's transport between them) -----
     def howfar(self, state: dict, uniforms, n_uniform: int, seed: int, gstep=None, limits=None, counters=None,

@@ -299,6 +299,43 @@ int  hepem_perform_host(const hepem_ctx* ctx, int form, int64_t n, const hepem_t
                         const double* uniforms, int32_t n_uniform, uint64_t seed, hepem_step_out* res,
                         hepem_step_counters* counters, void* stream);
 
+/* ---- single functions of the path, as the reference's device tests call them */
+/* Each takes n energies (device), couple indices and, where a selection is
+ * made, uniforms; precision 0 runs the FP64 code of hepem_step, 1 the FP32
+ * code of hepem_step_mixed (a selection whose FP32 operands are too close to
+ * call is made again in FP64, as in the step).  Inputs outside the tables
+ * give NaN (cross sections) or -1 (indices).
+ *
+ * hepem_electron_xs_stepping: the step-limit macroscopic cross sections of e-
+ * (is_positron 0) or e+ -- restricted ionisation and brem at the stepping
+ * energy (GetRestMacXSecForStepping), e+ annihilation (0 for e-), e-nuclear,
+ * and the transport mean free path (G4HepEmElectronManager.icc:534-599); the
+ * reference's device test testing/ElectronXSections/src/ResMacXSecs.cu:16-33
+ * and its TestXSectionData. */
+int  hepem_electron_xs_stepping(const hepem_ctx* ctx, int64_t n, int is_positron, int precision,
+                                const double* ekin, const int32_t* imc, double* xs_ioni, double* xs_brem,
+                                double* xs_annih, double* xs_nuc, double* tr_mfp, void* stream);
+/* Target element (index in the material's element list, 0 for a one-element
+ * material) of Seltzer-Berger (is_sb 1) or relativistic (0) brem for the
+ * uniform urnd[i]: G4HepEmElectronInteractionBrem::SelectTargetAtom
+ * (G4HepEmElectronInteractionBrem.icc), as in
+ * testing/ElectronTargetElementSelector/src/ElemSelector.cu:14-30. */
+int  hepem_brem_select_target(const hepem_ctx* ctx, int64_t n, int is_positron, int is_sb, int precision,
+                              const double* ekin, const int32_t* imc, const double* urnd, int32_t* elem,
+                              void* stream);
+/* Target element of pair production for urnd[i] in the couple's material:
+ * G4HepEmGammaInteractionConversion::SelectTargetAtom, as in
+ * testing/GammaTargetElementSelector/src/GammaElemSelector.cu:14-27. */
+int  hepem_conv_select_target(const hepem_ctx* ctx, int64_t n, int precision, const double* ekin,
+                              const int32_t* imc, const double* urnd, int32_t* elem, void* stream);
+/* Gamma total macroscopic cross section (GetTotalMacXSec), the interaction
+ * SampleInteraction selects for urnd[i] (0 conversion, 1 Compton, 2
+ * photoelectric, 3 gamma-nuclear) and, when it is the photoelectric effect,
+ * its macroscopic cross section (else 0) (G4HepEmGammaManager.icc:108-219);
+ * as in testing/GammaXSections/src/GammaMacXSecs.cu:20-30. */
+int  hepem_gamma_xs(const hepem_ctx* ctx, int64_t n, int precision, const double* ekin, const int32_t* imc,
+                    const double* urnd, double* xs_tot, double* xs_pe, int32_t* winner, void* stream);
+
 /* ---- stage timing (profiling aid; not thread-safe) ------------------------ */
 /* enable != 0: the following hepem_step_batched calls on this context record
  * CUDA events around each of their stage kernels (no reference counterpart:
