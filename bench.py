@@ -443,6 +443,129 @@ def c4_serving(torch, N, args):
             "form": "precision (hepem_server_config.precision = 1)" if args.form == "mixed" else "FP64 batched"}
 
 
+# ---- distribution checks of the sampled interaction models ----------------------------
+MEC2 = 0.51099890999999997
+
+
+def kn_cdf(eps, k):
+    """CDF of eps = E'/E of Klein-Nishina Compton scattering at k = E / m_e c^2:
+    the integral of 1/eps + eps - sin^2(theta), 1 - cos(theta) = (1 - eps) / (k eps),
+    over [1 / (1 + 2k), eps], in closed form."""
+    import numpy as np
+
+    def F(e):
+        le = np.log(e)
+        return le + 0.5 * e * e - (2.0 / k) * (le - e) + (1.0 / (k * k)) * (-1.0 / e - 2.0 * le + e)
+
+    e0 = 1.0 / (1.0 + 2.0 * k)
+    return (F(np.asarray(eps, dtype=np.float64)) - F(e0)) / (F(1.0) - F(e0))
+
+
+def kn_equal_count_edges(e_mev, nb):
+    """Bin edges in eps with equal Klein-Nishina probability (bisection on kn_cdf)."""
+    import numpy as np
+    k = e_mev / MEC2
+    lo = np.full(nb - 1, 1.0 / (1.0 + 2.0 * k))
+    hi = np.ones(nb - 1)
+    target = np.arange(1, nb) / nb
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        below = kn_cdf(mid, k) < target
+        lo = np.where(below, mid, lo)
+        hi = np.where(below, hi, mid)
+    return np.concatenate([[1.0 / (1.0 + 2.0 * k)], 0.5 * (lo + hi), [1.0]])
+
+
+def chi2_pvalue(c2, ndf):
+    try:
+        from scipy.stats import chi2 as _c2
+        return float(_c2.sf(c2, ndf))
+    except Exception:
+        return None
+
+
+def chi2_expected(counts, probs):
+    """Pearson chi2 of counts against bin probabilities; ndf = bins - 1."""
+    import numpy as np
+    counts = np.asarray(counts, dtype=np.float64)
+    exp = counts.sum() * np.asarray(probs, dtype=np.float64)
+    c2 = float(np.sum((counts - exp) ** 2 / exp))
+    ndf = len(counts) - 1
+    return {"chi2": c2, "ndf": ndf, "p_value": chi2_pvalue(c2, ndf)}
+
+
+def chi2_two_sample(a, b):
+    """Two-sample chi2 of histograms a, b (any totals) over the bins where
+    either has counts; ndf = those bins - 1."""
+    import numpy as np
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    m = (a + b) > 0
+    a, b = a[m], b[m]
+    ra, rb = np.sqrt(b.sum() / a.sum()), np.sqrt(a.sum() / b.sum())
+    c2 = float(np.sum((ra * a - rb * b) ** 2 / (a + b)))
+    ndf = int(m.sum()) - 1
+    return {"chi2": c2, "ndf": ndf, "p_value": chi2_pvalue(c2, ndf)}
+
+
+def sample_histograms(torch, ctx, draws, chunk, seed0):
+    """Histograms of independent draws of the FP64 and the FP32 model, each
+    from its own seeds (seed0 + c for FP64 chunk c, seed0 + 1000 + c for FP32):
+    Seltzer-Berger brem at 999 MeV in G4_Pb in 100 bins of ln(k/E) over
+    [ln 1e-4, 0], and Klein-Nishina Compton at 1 MeV in G4_lAr in 100 bins of
+    eps = E'/E of equal Klein-Nishina probability.  Returns
+    {model: {"fp64": counts, "fp32": counts, "probs": expected or None,
+    "fallback": FP32 draws redone in FP64, "draws_per_s": {...}}}."""
+    import math
+    import numpy as np
+    out = {}
+    for name, model, e_mev, imc in (("sb_999MeV_G4_Pb", "sb", 999.0, 2), ("compton_1MeV_G4_lAr", "compton", 1.0, 1)):
+        if model == "compton":
+            edges = torch.from_numpy(kn_equal_count_edges(e_mev, 100)).cuda()
+        else:
+            edges = torch.linspace(math.log(1e-4), 0.0, 101, dtype=torch.float64, device="cuda")
+        rec = {"fallback": 0, "draws_per_s": {}}
+        for mixed in (False, True):
+            h = torch.zeros(100, dtype=torch.float64, device="cuda")
+            t_ms = 0.0
+            for c in range(draws // chunk):
+                t0 = torch.cuda.Event(enable_timing=True)
+                t1 = torch.cuda.Event(enable_timing=True)
+                t0.record()
+                x, fb = ctx.sample_model(model, chunk, e_mev, imc, seed0 + (1000 if mixed else 0) + c, mixed=mixed)
+                t1.record()
+                torch.cuda.synchronize()
+                t_ms += t0.elapsed_time(t1)
+                if mixed:
+                    rec["fallback"] += int(fb.item())
+                y = x / e_mev
+                if model == "sb":
+                    y = torch.log(y.clamp_min(1e-300))
+                idx = torch.bucketize(y, edges[1:-1], right=True)
+                inside = (y >= edges[0]) & (y <= edges[-1])
+                h += torch.bincount(idx[inside], minlength=100).double()
+            rec["fp32" if mixed else "fp64"] = h.cpu().numpy()
+            rec["draws_per_s"]["fp32" if mixed else "fp64"] = draws / (t_ms / 1e3)
+        rec["probs"] = np.full(100, 0.01) if model == "compton" else None
+        out[name] = rec
+    return out
+
+
+def chi2_report(hists, draws):
+    """chi2 of independent FP32 and FP64 samples against each other, and of
+    Klein-Nishina samples against the analytic spectrum."""
+    rep = {}
+    for name, r in hists.items():
+        d = {"draws_per_arm": draws, "bins": 100, "streams": "independent seeds per arm",
+             "fp32_vs_fp64": chi2_two_sample(r["fp32"], r["fp64"]), "fp64_fallback_draws": r["fallback"],
+             "draws_per_s": r["draws_per_s"]}
+        if r["probs"] is not None:
+            d["fp32_vs_analytic"] = chi2_expected(r["fp32"], r["probs"])
+            d["fp64_vs_analytic"] = chi2_expected(r["fp64"], r["probs"])
+        rep[name] = d
+    return rep
+
+
 def c5_precision(torch, N, args, n_tracks=1 << 24):
     """Precision: the precision form (hepem_step_mixed) on a
     16,777,216-track batch with the mix of the 4M-track step, against the FP64
@@ -451,7 +574,8 @@ def c5_precision(torch, N, args, n_tracks=1 << 24):
     relative errors; the 2^20-track electron lookups from the FP32 tables against
     the FP64 ones; and chi2 of 1e8 Seltzer-Berger brem draws at 999 MeV in G4_Pb
     (just below the 1 GeV switch to the relativistic model) and 1e8
-    Klein-Nishina draws at 1 MeV in G4_lAr, FP32 models against FP64 models."""
+    Klein-Nishina draws at 1 MeV in G4_lAr, FP32 models against FP64 models
+    on independent streams, Klein-Nishina also against the analytic spectrum."""
     from g4hepem_gb300 import workload as W
     ctx = N.Context(TABLE)
     n = n_tracks
@@ -510,46 +634,9 @@ def c5_precision(torch, N, args, n_tracks=1 << 24):
     l32 = ctx.electron_lookup(ekin, imc, mixed=True)
     torch.cuda.synchronize()
     lookups = {k: rel(l32[k], l64[k]) for k in l64}
-    # chi2 of the sampled energies, 1e8 draws per model and precision
-    import math
-    chi = {}
-    for name, model, e_mev, imc_c, lo, hi, logb in (("sb_999MeV_G4_Pb", "sb", 999.0, 2, None, None, True),
-                                                   ("compton_1MeV_G4_lAr", "compton", 1.0, 1, 0.0, 1.0, False)):
-        draws, chunk, nb = 10 ** 8, 10 ** 7, 100
-        h = {False: torch.zeros(nb, dtype=torch.float64, device="cuda"),
-             True: torch.zeros(nb, dtype=torch.float64, device="cuda")}
-        fb_total, tms = 0, {}
-        for mixed in (False, True):
-            t0 = torch.cuda.Event(enable_timing=True)
-            t1 = torch.cuda.Event(enable_timing=True)
-            t_ms = 0.0
-            for c in range(draws // chunk):
-                t0.record()
-                x, fb = ctx.sample_model(model, chunk, e_mev, imc_c, SEED + 100 + c, mixed=mixed)
-                t1.record()
-                torch.cuda.synchronize()
-                t_ms += t0.elapsed_time(t1)
-                if mixed:
-                    fb_total += int(fb.item())
-                y = x / e_mev
-                if logb:
-                    y = torch.log(y.clamp_min(1e-300))
-                    edges = (math.log(1e-4), 0.0)
-                else:
-                    edges = (lo, hi)
-                h[mixed] += torch.histc(y, bins=nb, min=edges[0], max=edges[1]).double()
-            tms["fp32" if mixed else "fp64"] = draws / (t_ms / 1e3)
-        a, b = h[False], h[True]
-        m = (a + b) > 0
-        c2 = float(((a[m] - b[m]) ** 2 / (a[m] + b[m])).sum())
-        ndf = int(m.sum())
-        try:
-            from scipy.stats import chi2 as _c2
-            pval = float(_c2.sf(c2, ndf))
-        except Exception:
-            pval = None
-        chi[name] = {"draws": draws, "bins": nb, "chi2": c2, "ndf": ndf, "p_value": pval,
-                     "fp64_fallback_draws": fb_total, "draws_per_s": tms}
+    # chi2 of the sampled energies: 1e8 draws per model and precision, each
+    # arm from its own seeds; Klein-Nishina also against its analytic spectrum
+    chi = chi2_report(sample_histograms(torch, ctx, 10 ** 8, 10 ** 7, SEED + 100), 10 ** 8)
     ctx.close()
     c = cnts["mixed"].cpu().numpy()
     return {"workload": f"{n} mixed tracks (mix of the 4M-track step), 64 Philox uniforms/track, identical streams",
@@ -784,9 +871,9 @@ def main():
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if hbm_src == "measured" else "fallback",
             "algorithmic_bytes_per_launch": alg, "ms_per_launch": ms_dom,
             "note": ("HBM is not the limit of this kernel: the precision form's stage A is bound by the latency "
-                     "of dependent table and state gathers (profiles/stage_a_charged_mixed_2M_tracks.md); traffic is "
-                     "the ncu DRAM bytes per e+- track x the e+- tracks of the step" if args.form == "mixed" else
-                     "HBM is not the limit of this kernel: the FP64 pipe is (roofline_fp64, profiles/)")}
+                     "of dependent table and state gathers; traffic is the ncu DRAM bytes per e+- track x the e+- "
+                     "tracks of the step" if args.form == "mixed" else
+                     "HBM is not the limit of this kernel: the FP64 pipe is (roofline_fp64)")}
     fp64 = {"bound": "fp64", "kernel": dom, "unit": "TFLOP/s", "peak": None,
             "peak_source": "measured here: cuBLAS DGEMM 4096^3 (MEASURED_PEAKS.json has no FP64 figure)"}
     fp32 = {"bound": "fp32", "kernel": dom, "unit": "TFLOP/s", "peak": None,

@@ -758,7 +758,8 @@ __device__ __forceinline__ void interaction_fp64(Physics& P) {
 // HowFar from the pre-step state with the pre-step boundary status (the state
 // is the pre-step one: HowFar left it unchanged), then the caller's transport
 // (its geometrical step, unless it is the proposed one, the direction and the
-// post-step boundary status in the state), then Perform.
+// post-step boundary status in the state), then Perform.  An unshortened step
+// is the FP64 proposed one, as in the fused step (results equal to it).
 template <int PHASE>
 __device__ void charged_full_step(const DevTables& T, const hepem_track_state& in, const hepem_track_state& out,
                                   const double* uniforms, int nu, uint64_t seed, const hepem_step_out& res,
@@ -790,7 +791,6 @@ __device__ void charged_full_step(const DevTables& T, const hepem_track_state& i
     P.el_howfar();
   }
   const int key = P.el_perform_until_discrete();
-  if (PHASE == kPhasePerform) t.gstep = w.gstep[i];
   const int32_t cA = rng.cursor;
   const uint32_t ovA = rng.overflow;
   switch (key) {

@@ -15,7 +15,10 @@
 // name of a __device__ array as a device address (in host code it names a
 // host-side stand-in), so the address is looked up with cudaGetSymbolAddress,
 // once per device, with that device current, by the first call on that device.
-// That first call should therefore come before any stream capture.  All calls
+// That first call should therefore come before any stream capture.  The
+// address stays valid for the life of the device's primary context: a
+// cudaDeviceReset (or anything else that tears the context down) may move the
+// array, so no call may follow such a reset in the same process.  All calls
 // share the one array and it keeps the contents of the last call: the counters
 // and histograms that must start at zero are cleared on the stream at the start
 // of every call (launch_step_batched), and calls whose work overlaps on the GPU

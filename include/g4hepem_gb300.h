@@ -192,7 +192,8 @@ int  hepem_step_batched(const hepem_ctx* ctx, int64_t n, const hepem_track_state
  * limited to HEPEM_NOALLOC_MAX_TRACKS tracks (larger ones: HEPEM_BAD_ARG).
  * The first call on a device looks up the array's device address on the
  * current device (make it before any stream capture); the current device must
- * be the context's.  All calls share the array: calls that overlap on the GPU
+ * be the context's.  The address is kept for the life of the device's primary
+ * context: make no call after a cudaDeviceReset in the same process.  All calls share the array: calls that overlap on the GPU
  * (other streams, other threads) race.  No counterpart in the reference (its
  * host functions need no device workspace). */
 #define HEPEM_NOALLOC_MAX_TRACKS 524288

@@ -87,9 +87,19 @@ def copy_state(state: dict) -> dict:
     return {k: v.copy() for k, v in state.items()}
 
 
+def reference_dir() -> str:
+    """Where the reference sources lie: $HEPEM_REFERENCE_DIR, else the
+    default of oracle/Makefile (`make print-ref`)."""
+    env = os.environ.get("HEPEM_REFERENCE_DIR")
+    if env:
+        return env
+    r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+    return r.stdout.strip()
+
+
 def build_ref(quiet=True) -> bool:
     """Compile oracle/_ref (needs the reference sources)."""
-    r = subprocess.run(["make", "-C", HERE, "ref"], capture_output=quiet)
+    r = subprocess.run(["make", "-C", HERE, "ref", f"REF={reference_dir()}"], capture_output=quiet)
     return r.returncode == 0 and os.path.exists(REF_SO)
 
 

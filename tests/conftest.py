@@ -42,7 +42,7 @@ def port():
 def ref():
     """The reference itself, where its sources are present (this container)."""
     from oracle import oracle as O
-    if not os.path.isdir("/root/reference") or not O.build_ref():
+    if not os.path.isdir(O.reference_dir()) or not O.build_ref():
         pytest.skip("reference sources not available on this host")
     libs = {}
 

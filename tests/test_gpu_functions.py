@@ -51,8 +51,14 @@ def test_selectors_and_gamma_xs_golden(native, gpu_ctx, name, table, mixed):
     gx = ctx.gamma_xs(_t(g["g_ekin"]), _t(g_imc.astype(np.int32)), _t(gu), mixed=mixed)
     win = _np(gx["winner"])
     assert np.array_equal(win, g["g_winner"]), np.sum(win != g["g_winner"])
-    # the photoelectric cross section the photoelectric model uses is FP64 in both forms
-    assert np.array_equal(_np(gx["xs_pe"]), g["g_xs_pe"])
+    # the photoelectric cross section the photoelectric model uses is FP64 in
+    # both forms; the precision form's translation unit contracts FP64
+    # multiply-adds, so there it agrees to a few ulp
+    pe = _np(gx["xs_pe"])
+    if mixed:
+        assert np.array_equal(pe == 0, g["g_xs_pe"] == 0) and rel(pe, g["g_xs_pe"]).max() <= 1e-15
+    else:
+        assert np.array_equal(pe, g["g_xs_pe"])
     tot = _np(gx["xs_tot"])
     if mixed:
         assert rel(tot, g["g_xs_tot"]).max() <= TOL32

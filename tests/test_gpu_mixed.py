@@ -155,3 +155,26 @@ def test_sampled_model_fp32_equals_fp64_per_draw(native, gpu_ctx, model, e, imc)
     assert np.max(rel_err(b, a)) <= TOL
     assert int(fb.item()) < 0.02 * n
     assert np.all(a >= 0) and np.all(a <= e)
+
+
+def test_sampled_distributions_chi2(native, gpu_ctx):
+    """The FP32 models draw from the right distributions, not only the same
+    values as FP64 on the same uniforms: 10^7 Seltzer-Berger draws at 999 MeV
+    in G4_Pb and 10^7 Klein-Nishina draws at 1 MeV in G4_lAr per arm, each arm
+    from its own seeds; chi2 of FP32 against FP64 (two-sample, 100 bins) and
+    of both Klein-Nishina arms against the analytic spectrum (100 bins of
+    equal probability), each with p > 1e-3."""
+    pytest.importorskip("scipy")
+    import torch
+    import bench
+    ctx = gpu_ctx(T3)
+    draws = 10 ** 7
+    rep = bench.chi2_report(bench.sample_histograms(torch, ctx, draws, draws // 4, 4242), draws)
+    print()
+    for name, d in rep.items():
+        for key in ("fp32_vs_fp64", "fp32_vs_analytic", "fp64_vs_analytic"):
+            if key in d:
+                r = d[key]
+                print(f"{name} {key}: chi2 {r['chi2']:.1f} / ndf {r['ndf']}, p = {r['p_value']:.3g}")
+                assert r["ndf"] >= 80 and r["p_value"] > 1e-3, (name, key, r)
+        assert d["fp64_fallback_draws"] < 0.02 * draws
