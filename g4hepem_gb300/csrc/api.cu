@@ -305,6 +305,18 @@ int hepem_step_mixed(const hepem_ctx* c, int64_t n, const hepem_track_state* in,
   return step_batched(c, n, in, out, uniforms, nu, seed, res, counters, stream, true);
 }
 
+// The device-mapped address of a page-locked host array (cudaHostAlloc,
+// cudaHostRegister), or null when the GPU cannot address it directly.
+static void* mapped_address(const void* h) {
+  if (!h) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 // chunks of a host-buffer step: more overlap of the copies against smaller,
 // less efficient device steps
 #ifndef HEPEM_HOST_CHUNKS
@@ -362,6 +374,18 @@ int step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem
   void* const* hres = reinterpret_cast<void* const*>(res);
   static_assert(sizeof(hepem_track_state) == 20 * sizeof(void*), "state struct layout");
   static_assert(sizeof(hepem_step_out) == 14 * sizeof(void*), "out struct layout");
+  // Pinned (page-locked) host arrays have device-mapped addresses: then each
+  // chunk moves in one gather launch and one scatter launch over all its
+  // arrays instead of one copy per array and direction.
+  void* min[20];
+  void* mout[20];
+  void* mres[14];
+  void* mu = nullptr;
+  bool zc = nu == 0 || (mu = mapped_address(uniforms)) != nullptr;
+  for (int k = 0; k < 20 && zc; ++k) zc = (min[k] = mapped_address(hin[k])) != nullptr;
+  for (int k = 3; k < 20 && zc; ++k)
+    if (k != 11 && k != 12) zc = (mout[k] = mapped_address(hout[k])) != nullptr;
+  for (int k = 0; k < 14 && zc; ++k) zc = (mres[k] = mapped_address(hres[k])) != nullptr;
   hepem_step_counters* dcnt[hepem_ctx::kSlots] = {};
   for (int ch = 0; ch < nChunks; ++ch) {
     const int64_t off = (int64_t)ch * m;
@@ -388,11 +412,29 @@ int step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem
     hepem_step_out dr;
     memcpy(&ds, dstate, sizeof(ds));
     memcpy(&dr, dout, sizeof(dr));
-    for (int k = 0; k < 20; ++k)
-      HEPEM_CUDA(cudaMemcpyAsync(dstate[k], (const uint8_t*)hin[k] + kStateSizes[k] * off, kStateSizes[k] * mc,
-                                 cudaMemcpyHostToDevice, ss));
-    if (nu > 0)
-      HEPEM_CUDA(cudaMemcpyAsync(du, uniforms + off * nu, sizeof(double) * (size_t)mc * nu, cudaMemcpyHostToDevice, ss));
+    if (zc) {
+      hepem::SegList g;
+      g.n = 0;
+      for (int k = 0; k < 20; ++k) {
+        g.src[g.n] = (const uint8_t*)min[k] + kStateSizes[k] * off;
+        g.dst[g.n] = (uint8_t*)dstate[k];
+        g.bytes[g.n++] = kStateSizes[k] * mc;
+      }
+      if (nu > 0) {
+        g.src[g.n] = (const uint8_t*)mu + sizeof(double) * (size_t)off * nu;
+        g.dst[g.n] = (uint8_t*)du;
+        g.bytes[g.n++] = sizeof(double) * (size_t)mc * nu;
+      }
+      hepem::seglist_finish(g);
+      HEPEM_CUDA(hepem::launch_copy_segments(g, ss, c->sms));
+    } else {
+      for (int k = 0; k < 20; ++k)
+        HEPEM_CUDA(cudaMemcpyAsync(dstate[k], (const uint8_t*)hin[k] + kStateSizes[k] * off, kStateSizes[k] * mc,
+                                   cudaMemcpyHostToDevice, ss));
+      if (nu > 0)
+        HEPEM_CUDA(cudaMemcpyAsync(du, uniforms + off * nu, sizeof(double) * (size_t)mc * nu,
+                                   cudaMemcpyHostToDevice, ss));
+    }
     hepem::BatchOpts o;
     o.cfg = &c->launch;
     o.mixed = mixed;
@@ -405,14 +447,32 @@ int step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem
     HEPEM_CUDA(hepem::launch_step_batched(c->tables, mc, ds, ds, du, nu, seed, dr, counters ? cnt : nullptr, dwork,
                                           ss, c->sms, o));
     // persistent per-track fields come back (type/imc/id/safety/boundary are inputs only)
-    for (int k = 3; k < 20; ++k) {
-      if (k == 11 || k == 12) continue;
-      HEPEM_CUDA(cudaMemcpyAsync((uint8_t*)hout[k] + kStateSizes[k] * off, dstate[k], kStateSizes[k] * mc,
-                                 cudaMemcpyDeviceToHost, ss));
+    if (zc) {
+      hepem::SegList g;
+      g.n = 0;
+      for (int k = 3; k < 20; ++k) {
+        if (k == 11 || k == 12) continue;
+        g.src[g.n] = (const uint8_t*)dstate[k];
+        g.dst[g.n] = (uint8_t*)mout[k] + kStateSizes[k] * off;
+        g.bytes[g.n++] = kStateSizes[k] * mc;
+      }
+      for (int k = 0; k < 14; ++k) {
+        g.src[g.n] = (const uint8_t*)dout[k];
+        g.dst[g.n] = (uint8_t*)mres[k] + kOutSizes[k] * off;
+        g.bytes[g.n++] = kOutSizes[k] * mc;
+      }
+      hepem::seglist_finish(g);
+      HEPEM_CUDA(hepem::launch_copy_segments(g, ss, c->sms));
+    } else {
+      for (int k = 3; k < 20; ++k) {
+        if (k == 11 || k == 12) continue;
+        HEPEM_CUDA(cudaMemcpyAsync((uint8_t*)hout[k] + kStateSizes[k] * off, dstate[k], kStateSizes[k] * mc,
+                                   cudaMemcpyDeviceToHost, ss));
+      }
+      for (int k = 0; k < 14; ++k)
+        HEPEM_CUDA(cudaMemcpyAsync((uint8_t*)hres[k] + kOutSizes[k] * off, dout[k], kOutSizes[k] * mc,
+                                   cudaMemcpyDeviceToHost, ss));
     }
-    for (int k = 0; k < 14; ++k)
-      HEPEM_CUDA(cudaMemcpyAsync((uint8_t*)hres[k] + kOutSizes[k] * off, dout[k], kOutSizes[k] * mc,
-                                 cudaMemcpyDeviceToHost, ss));
   }
   if (hout[0] != hin[0]) {
     for (int k : {0, 1, 2, 11, 12}) memcpy(hout[k], hin[k], kStateSizes[k] * n);

@@ -162,6 +162,23 @@ cudaError_t launch_woodcock(const DevTables& T, int64_t n, const hepem_track_sta
                             const hepem_layered_box& box, const double* uniforms, int nu, uint64_t seed,
                             const hepem_step_out& res, uint8_t* reached, cudaStream_t s, int sms);
 
+// Copies of up to kMaxSegs byte ranges in one launch (the host-buffer steps:
+// the caller's pinned arrays, reached through their device-mapped addresses,
+// to and from the device batch).  Ranges are moved in 16-byte units where both
+// ends are 16-byte aligned, by bytes otherwise.
+constexpr int kMaxSegs = 48;
+struct SegList {
+  const uint8_t* src[kMaxSegs];
+  uint8_t* dst[kMaxSegs];
+  uint64_t bytes[kMaxSegs];
+  uint64_t unitStart[kMaxSegs + 1];  // prefix sums of each range's units (16 B, or 1 B unaligned)
+  uint32_t vec;                      // bit k: range k moves in 16-byte units
+  int n;
+};
+// fills unitStart / vec from src, dst, bytes, n
+void seglist_finish(SegList& L);
+cudaError_t launch_copy_segments(const SegList& L, cudaStream_t s, int sms);
+
 cudaError_t launch_fill_uniforms(int64_t n, const int32_t* id, int nu, uint64_t seed, double* u, cudaStream_t s,
                                  int sms);
 

@@ -80,6 +80,9 @@ struct Work {
   double* gstep;
   Limits limits;
   int phase;
+  // the batch: n tracks, active[0..n) of larger arrays or all
+  int64_t n;
+  const int32_t* active;
 };
 
 __device__ __forceinline__ uint64_t key_of(const Work& w, int64_t i, uint64_t seed) {
@@ -141,6 +144,8 @@ static Work carve(void* ws, int64_t n) {
   w.gstep = nullptr;
   w.limits = Limits{};
   w.phase = kPhaseStep;
+  w.n = n;
+  w.active = nullptr;
   w.counts = reinterpret_cast<uint32_t*>(p);
   p += rnd(64 * sizeof(uint32_t));
   w.hist = reinterpret_cast<uint32_t*>(p);
@@ -456,13 +461,162 @@ __device__ __forceinline__ void fb_push(bool trip, int32_t idx, uint8_t kind, co
 // PHASE kPhaseStep: HowFar and Perform up to the interaction (the fused step);
 // kPhaseHowFar: HowFar only, into the step-limit record (nothing queued);
 // kPhasePerform: Perform from the record with the caller's geometrical step.
+// Stage A of one e+- track idx: HowFar + Perform up to the pending discrete
+// interaction.  Returns the queue of that interaction (-1: none); tripped =
+// the precision form handed the track to its FP64 fallback (nothing stored).
+template <int MODE, int PHASE>
+__device__ __forceinline__ int charged_item(const DevTables& T, const hepem_track_state& in,
+                                            const hepem_track_state& out, const double* uniforms, int nu,
+                                            uint64_t seed, const hepem_step_out& res, const Work& w, int32_t idx,
+                                            int type, bool& tripped, StepCount& cnt) {
+  int key = -1;
+  Track t;
+  Rng rng;
+  load_track(in, idx, t, rng, uniforms, nu, key_of(w, idx, seed), type);
+  int32_t c0 = rng.cursor;
+  if (MODE == kStageMixed) {
+    MixedEl M{T, rng, t, false};
+    if (PHASE == kPhaseStep) {
+      key = M.stage_a();
+    } else if (PHASE == kPhaseHowFar) {
+      ElLimit32 h;
+      M.howfar(h);
+      if (!M.trip) store_limits32(w.limits, idx, h, t, rng, w.gstep);
+    } else {
+      ElLimit32 h;
+      load_limits32(w.limits, idx, h, t, rng);
+      c0 = rng.cursor;
+      // an FP64 record (its HowFar tripped), or a step that transport
+      // shortened (the geometrical -> true conversion): the FP64 code
+      if (!(w.limits.bits[idx] & kLimFp32) || w.gstep[idx] != f2d(h.gstep))
+        M.set_trip();
+      else
+        key = M.perform(h);
+    }
+    tripped = M.trip;
+    if (tripped) HEPEM_COUNT_TRIP(M.tripLine);
+  } else {
+    Physics P{T, rng, t};
+    if (PHASE == kPhaseStep) {
+      P.el_howfar();
+      key = P.el_perform_until_discrete();
+    } else if (PHASE == kPhaseHowFar) {
+      P.el_howfar();
+      store_limits64(w.limits, idx, t, rng, type, w.gstep);
+    } else {
+      load_limits64(w.limits, idx, t, rng, type, w.gstep);
+      c0 = rng.cursor;
+      key = P.el_perform_until_discrete();
+    }
+  }
+  if (PHASE == kPhaseHowFar) {
+    key = -1;
+    if (!tripped) {
+      cnt.uniforms += (uint32_t)(rng.cursor - c0);
+      cnt.overflow += rng.overflow;
+    }
+  } else if (tripped) {
+    key = -1;
+  } else {
+    if (MODE == kStageMixed && w.preCopy && key >= 0 && key != kQAnnihRest) save_pre(in, w.pre, idx);
+    store_track(in, out, res, idx, t, rng, type, false);
+    res.n_sec[idx] = 0;
+    cnt.steps += 1;
+    cnt.uniforms += (uint32_t)(rng.cursor - c0);
+    cnt.overflow += rng.overflow;
+    if (t.winner >= 0 && t.winner < 4) count_inter(cnt, t.winner);
+  }
+  return key;
+}
+
+// Stage A of one gamma idx: HowFar, the interaction choice and Perform up to
+// the interaction; pe = the photoelectric cross section for its model.
+// MODE kStageMixed: from the FP32 table (MixedG); a tripped gamma is not
+// stored but goes to the fallback list.
+template <int MODE, int PHASE>
+__device__ __forceinline__ int gamma_item(const DevTables& T, const hepem_track_state& in,
+                                          const hepem_track_state& out, const double* uniforms, int nu,
+                                          uint64_t seed, const hepem_step_out& res, const Work& w, int32_t idx,
+                                          double& pe, bool& tripped, StepCount& cnt) {
+  int key = -1;
+  Track t;
+  Rng rng;
+  load_track(in, idx, t, rng, uniforms, nu, key_of(w, idx, seed), 2);
+  int32_t c0 = rng.cursor;
+  t.isEl = false;
+  if (MODE == kStageMixed) {
+    MixedG G{T, rng, t, false};
+    if (PHASE == kPhaseStep) {
+      key = G.stage_a();
+    } else if (PHASE == kPhaseHowFar) {
+      GammaLimit32 q;
+      G.howfar(q);
+      store_glimits32(w.limits, idx, q, t, rng, w.gstep);
+    } else {
+      GammaLimit32 q;
+      load_glimits32(w.limits, idx, q, t, rng);
+      c0 = rng.cursor;
+      const double g = w.gstep[idx];
+      key = G.perform(q, d2f(g));
+      t.gstep = g;
+      t.pstep = g;
+    }
+    tripped = G.trip;
+    if (tripped) {
+      HEPEM_COUNT_TRIP(G.tripLine);
+      key = -1;
+    }
+  } else {
+    Physics P{T, rng, t};
+    if (PHASE == kPhaseHowFar) {
+      P.gamma_howfar();
+      store_limits64(w.limits, idx, t, rng, 2, w.gstep);
+    } else {
+      if (PHASE == kPhaseStep) {
+        P.gamma_howfar();
+      } else {
+        load_limits64(w.limits, idx, t, rng, 2, w.gstep);
+        c0 = rng.cursor;
+      }
+      if (t.onBoundary) {
+        t.nia[0] -= t.gstep / t.mfp[0];
+      } else {
+        P.gamma_select();
+        key = P.gamma_perform_until_interaction();
+      }
+      t.pstep = t.gstep;
+    }
+  }
+  if (PHASE == kPhaseHowFar) {
+    key = -1;
+    cnt.uniforms += (uint32_t)(rng.cursor - c0);
+    cnt.overflow += rng.overflow;
+  } else if (!tripped) {
+    if (key == -2) {
+      Physics P{T, rng, t};
+      P.gamma_tracking_cut();
+      key = -1;
+    }
+    pe = t.peXS;
+    store_track(in, out, res, idx, t, rng, 2, false);
+    res.n_sec[idx] = 0;
+    cnt.steps += 1;
+    cnt.uniforms += (uint32_t)(rng.cursor - c0);
+    cnt.overflow += rng.overflow;
+    if (t.winner >= 0 && t.winner < 4) count_inter(cnt, 4 + t.winner);
+  }
+  return key;
+}
+
+// PHASE kPhaseStep: HowFar and Perform up to the interaction (the fused step);
+// kPhaseHowFar: HowFar only, into the step-limit record (nothing queued);
+// kPhasePerform: Perform from the record with the caller's geometrical step.
+// The e+- tracks in sort order (perm[0, nEm + nEp)).
 template <int BS, int MODE, int PHASE = kPhaseStep>
 __global__ void __launch_bounds__(BS, MODE == kStageMixed ? HEPEM_MIXED_A_WARPS * 32 / BS : 1)
-    stage_a_charged_kernel(const __grid_constant__ DevTables T,
-                                                              const hepem_track_state in, const hepem_track_state out,
-                                                              const double* __restrict__ uniforms, int nu,
-                                                              uint64_t seed, const hepem_step_out res, const Work w,
-                                                              hepem_step_counters* counters) {
+    stage_a_charged_kernel(const __grid_constant__ DevTables T, const hepem_track_state in,
+                           const hepem_track_state out, const double* __restrict__ uniforms, int nu, uint64_t seed,
+                           const hepem_step_out res, const Work w, hepem_step_counters* counters) {
   const uint32_t nEm = w.counts[0], nEp = w.counts[1];
   const int64_t total = (int64_t)nEm + nEp;
   StepCount cnt = {};
@@ -474,62 +628,7 @@ __global__ void __launch_bounds__(BS, MODE == kStageMixed ? HEPEM_MIXED_A_WARPS 
     if (j < total) {
       idx = w.perm[j];
       const int type = w.oneChargedKey ? (int)in.type[idx] : (j < nEm ? 0 : 1);
-      Track t;
-      Rng rng;
-      load_track(in, idx, t, rng, uniforms, nu, key_of(w, idx, seed), type);
-      int32_t c0 = rng.cursor;
-      if (MODE == kStageMixed) {
-        MixedEl M{T, rng, t, false};
-        if (PHASE == kPhaseStep) {
-          key = M.stage_a();
-        } else if (PHASE == kPhaseHowFar) {
-          ElLimit32 h;
-          M.howfar(h);
-          if (!M.trip) store_limits32(w.limits, idx, h, t, rng, w.gstep);
-        } else {
-          ElLimit32 h;
-          load_limits32(w.limits, idx, h, t, rng);
-          c0 = rng.cursor;
-          // an FP64 record (its HowFar tripped), or a step that transport
-          // shortened (the geometrical -> true conversion): the FP64 code
-          if (!(w.limits.bits[idx] & kLimFp32) || w.gstep[idx] != f2d(h.gstep))
-            M.set_trip();
-          else
-            key = M.perform(h);
-        }
-        tripped = M.trip;
-        if (tripped) HEPEM_COUNT_TRIP(M.tripLine);
-      } else {
-        Physics P{T, rng, t};
-        if (PHASE == kPhaseStep) {
-          P.el_howfar();
-          key = P.el_perform_until_discrete();
-        } else if (PHASE == kPhaseHowFar) {
-          P.el_howfar();
-          store_limits64(w.limits, idx, t, rng, type, w.gstep);
-        } else {
-          load_limits64(w.limits, idx, t, rng, type, w.gstep);
-          c0 = rng.cursor;
-          key = P.el_perform_until_discrete();
-        }
-      }
-      if (PHASE == kPhaseHowFar) {
-        key = -1;
-        if (!tripped) {
-          cnt.uniforms += (uint32_t)(rng.cursor - c0);
-          cnt.overflow += rng.overflow;
-        }
-      } else if (tripped) {
-        key = -1;
-      } else {
-        if (MODE == kStageMixed && w.preCopy && key >= 0 && key != kQAnnihRest) save_pre(in, w.pre, idx);
-        store_track(in, out, res, idx, t, rng, type, false);
-        res.n_sec[idx] = 0;
-        cnt.steps += 1;
-        cnt.uniforms += (uint32_t)(rng.cursor - c0);
-        cnt.overflow += rng.overflow;
-        if (t.winner >= 0 && t.winner < 4) count_inter(cnt, t.winner);
-      }
+      key = charged_item<MODE, PHASE>(T, in, out, uniforms, nu, seed, res, w, idx, type, tripped, cnt);
     }
     warp_push(key, idx, w.queue, w.counts + 3);
     if (MODE == kStageMixed) fb_push(tripped, idx, 0, w);
@@ -537,8 +636,7 @@ __global__ void __launch_bounds__(BS, MODE == kStageMixed ? HEPEM_MIXED_A_WARPS 
   add_counters(cnt, counters);
 }
 
-// MODE kStageMixed: HowFar and the interaction choice from the FP32 table
-// (MixedG); a tripped gamma is not stored but goes to the fallback list.
+// The gammas in sort order (perm[nEm + nEp, ...)).
 template <int BS, int MODE, int PHASE = kPhaseStep>
 __global__ void __launch_bounds__(BS) stage_a_gamma_kernel(const __grid_constant__ DevTables T,
                                                             const hepem_track_state in, const hepem_track_state out,
@@ -555,72 +653,7 @@ __global__ void __launch_bounds__(BS) stage_a_gamma_kernel(const __grid_constant
     bool tripped = false;
     if (j < total) {
       idx = w.perm[w.counts[0] + w.counts[1] + j];
-      Track t;
-      Rng rng;
-      load_track(in, idx, t, rng, uniforms, nu, key_of(w, idx, seed), 2);
-      int32_t c0 = rng.cursor;
-      t.isEl = false;
-      if (MODE == kStageMixed) {
-        MixedG G{T, rng, t, false};
-        if (PHASE == kPhaseStep) {
-          key = G.stage_a();
-        } else if (PHASE == kPhaseHowFar) {
-          GammaLimit32 q;
-          G.howfar(q);
-          store_glimits32(w.limits, idx, q, t, rng, w.gstep);
-        } else {
-          GammaLimit32 q;
-          load_glimits32(w.limits, idx, q, t, rng);
-          c0 = rng.cursor;
-          const double g = w.gstep[idx];
-          key = G.perform(q, d2f(g));
-          t.gstep = g;
-          t.pstep = g;
-        }
-        tripped = G.trip;
-        if (tripped) {
-          HEPEM_COUNT_TRIP(G.tripLine);
-          key = -1;
-        }
-      } else {
-        Physics P{T, rng, t};
-        if (PHASE == kPhaseHowFar) {
-          P.gamma_howfar();
-          store_limits64(w.limits, idx, t, rng, 2, w.gstep);
-        } else {
-          if (PHASE == kPhaseStep) {
-            P.gamma_howfar();
-          } else {
-            load_limits64(w.limits, idx, t, rng, 2, w.gstep);
-            c0 = rng.cursor;
-          }
-          if (t.onBoundary) {
-            t.nia[0] -= t.gstep / t.mfp[0];
-          } else {
-            P.gamma_select();
-            key = P.gamma_perform_until_interaction();
-          }
-          t.pstep = t.gstep;
-        }
-      }
-      if (PHASE == kPhaseHowFar) {
-        key = -1;
-        cnt.uniforms += (uint32_t)(rng.cursor - c0);
-        cnt.overflow += rng.overflow;
-      } else if (!tripped) {
-        if (key == -2) {
-          Physics P{T, rng, t};
-          P.gamma_tracking_cut();
-          key = -1;
-        }
-        pe = t.peXS;
-        store_track(in, out, res, idx, t, rng, 2, false);
-        res.n_sec[idx] = 0;
-        cnt.steps += 1;
-        cnt.uniforms += (uint32_t)(rng.cursor - c0);
-        cnt.overflow += rng.overflow;
-        if (t.winner >= 0 && t.winner < 4) count_inter(cnt, 4 + t.winner);
-      }
+      key = gamma_item<MODE, PHASE>(T, in, out, uniforms, nu, seed, res, w, idx, pe, tripped, cnt);
     }
     warp_push(key, idx, w.queue, w.counts + 3, pe, w.peXS, kQPhotoelectric);
     if (MODE == kStageMixed) fb_push(tripped, idx, kFbGammaA, w);
@@ -1063,11 +1096,12 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
   };
   const int64_t blocks = (n + 255) / 256;
   const int gC = (int)(blocks < (int64_t)sms * 8 ? blocks : (int64_t)sms * 8);
+  w.active = o.active;
   mark();
   sort_hist_kernel<<<gC, 256, nkeys * sizeof(uint32_t), s>>>(T, n, o.active, in, out, res, w, ncb, neb, counters);
   sort_scan_kernel<<<1, 1024, 0, s>>>(w, ncb, neb);
-  const int64_t tiles = (n + 256 * kScatterItems - 1) / (256 * kScatterItems);
-  const int gS = (int)(tiles < (int64_t)sms * 8 ? tiles : (int64_t)sms * 8);
+  const int64_t nt = (n + 256 * kScatterItems - 1) / (256 * kScatterItems);
+  const int gS = (int)(nt < (int64_t)sms * 8 ? nt : (int64_t)sms * 8);
   sort_scatter_kernel<<<gS, 256, nkeys * sizeof(uint32_t), s>>>(T, n, o.active, in, w, ncb, neb);
   mark();
   // the stage kernels: with a table window, launched with it as a launch

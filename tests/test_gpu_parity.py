@@ -178,6 +178,44 @@ def test_host_entry_point_equals_device_entry_point(native, gpu_ctx):
 
 
 @pytest.mark.parametrize("mixed", [False, True])
+@pytest.mark.parametrize("in_place", [False, True])
+def test_host_entry_point_pinned_buffers(native, gpu_ctx, mixed, in_place):
+    """Pinned host buffers take the mapped path (one gather and one scatter
+    launch per chunk over all arrays): the same results as pageable buffers
+    (one copy per array), in and out of place,
+    with and without a uniform buffer, over several chunks."""
+    import torch
+    n = 300001
+    st = W.mixed_batch(n, seed=29)
+    ctx = gpu_ctx(T3)
+    for nu in (0, 64):
+        # pageable
+        out_a = {k: np.empty_like(v) for k, v in st.items()}
+        res_a = native.alloc_out_numpy(n)
+        u = W.philox_uniforms(31, st["id"], nu).reshape(-1) if nu else None
+        ctx.step_host(st, out_a, u, nu, 31, res_a, mixed=mixed)
+        # pinned: torch tensors keep the pinned storage alive
+        keep = []
+
+        def pin(a):
+            t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+            keep.append(t)
+            return t.numpy()
+        st_p = {k: pin(v) for k, v in st.items()}
+        out_p = st_p if in_place else {k: pin(np.empty_like(v)) for k, v in st.items()}
+        res_p = {k: pin(v) for k, v in native.alloc_out_numpy(n).items()}
+        u_p = pin(u) if nu else None
+        ctx.step_host(st_p, out_p, u_p, nu, 31, res_p, mixed=mixed)
+        for k in native.STATE_OUT_FIELDS:
+            assert np.array_equal(out_a[k], out_p[k], equal_nan=True), (nu, k)
+        ns = res_a["n_sec"].astype(int)
+        valid = (np.arange(2)[None, :] < ns[:, None]).reshape(-1)
+        for k in res_a:
+            a, b = (res_a[k][valid], res_p[k][valid]) if k.startswith("sec_") else (res_a[k], res_p[k])
+            assert np.array_equal(a, b, equal_nan=True), (nu, k)
+
+
+@pytest.mark.parametrize("mixed", [False, True])
 def test_host_entry_point_without_buffer_draws_the_same_stream(native, gpu_ctx, mixed):
     # n_uniform = 0: every uniform comes from the on-device counter-based
     # stream, whose values the buffer holds in the device entry point: the
