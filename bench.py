@@ -260,18 +260,19 @@ def c1_lookups(torch, N, ctx, stream, args, hbm):
 
 
 def c3_batching(torch, N, args):
-    """Uneven batching: 64 sub-batches of log-normal sizes (median 30k
-    before scaling, sigma 1.5, clipped to [1k, 1M], scaled to 16,777,216 tracks
-    in total), the particle and energy mix of the 4M-track step, 16 random couples
-    (1-4 elements, Z in 1..82, 1-12 g/cm3, cuts 0.1/0.7/1.0 mm).  Each
-    sub-batch is one call; timed: the plain form, the batched form with the
-    default launch configuration, the batched form with the configuration
-    chosen by the autotuner, and the latter captured once in a CUDA graph and
-    replayed; then the precision form, called and replayed from a graph."""
+    """Uneven batching: 64 sub-batches of log-normal sizes (median 30k,
+    clipped to [1k, 1M], the width fitted so that the sizes sum to 16,777,216
+    tracks), the particle and energy mix of the 4M-track step, 16 random couples
+    (1-4 elements, Z in 1..82, 1-12 g/cm3, cuts 0.1/0.7/1.0 mm).  Timed: one
+    call per sub-batch with the plain form, the batched form with the default
+    launch configuration and with the configuration chosen by the autotuner
+    (also captured once in a CUDA graph and replayed), the precision form
+    (called and replayed from a graph); and all sub-batches in one
+    hepem_step_subbatches call, in the batched and the precision form."""
     from g4hepem_gb300 import workload as W
     table = os.path.join(REPO, "g4hepem_gb300", "data", "random16.json")
     ctx = N.Context(table)
-    sizes = W.subbatch_sizes()
+    sizes, sigma = W.subbatch_sizes()
     total = int(sizes.sum())
     off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
     st = W.mixed_batch(total, n_couples=16, seed=17)
@@ -324,11 +325,20 @@ def c3_batching(torch, N, args):
     with torch.cuda.graph(graph_m):
         one_pass("mixed")
     ms_mixed_graph = timed(graph_m.replay, reps)
+    # all 64 sub-batches in one sorted, queued pass (hepem_step_subbatches)
+    batches = [(int(off[b]), int(sizes[b]), SEED) for b in range(len(sizes))]
+    ms_sub = timed(lambda: ctx.step_subbatches(batches, sin, sout, u, NU, res, form="batched"), reps)
+    ms_sub_mixed = timed(lambda: ctx.step_subbatches(batches, sin, sout, u, NU, res, form="mixed"), reps)
     ctx.close()
-    return {"workload": "64 sub-batches (log-normal, median 30k, sigma 1.5, clipped [1k, 1M], scaled to "
-                        "16,777,216 tracks), 16 random couples, the particle/energy mix of the 4M-track step",
-            "subbatch_min": int(sizes.min()), "subbatch_median": int(np.median(sizes)),
-            "subbatch_max": int(sizes.max()),
+    return {"workload": f"64 sub-batches (log-normal, median 30k, sigma {sigma:.2f} fitted so that the sizes "
+                        "clipped to [1k, 1M] sum to 16,777,216 tracks), 16 random couples, the particle/energy "
+                        "mix of the 4M-track step",
+            "subbatch_min": int(sizes.min()), "subbatch_median": float(np.median(sizes)),
+            "subbatch_max": int(sizes.max()), "subbatch_sigma": sigma,
+            "batched_subbatches": {"value": total / (ms_sub / 1e3), "unit": UNIT, "ms_per_pass": ms_sub,
+                                   "entry_point": "hepem_step_subbatches (HEPEM_FORM_BATCHED), one call"},
+            "mixed_subbatches": {"value": total / (ms_sub_mixed / 1e3), "unit": UNIT, "ms_per_pass": ms_sub_mixed,
+                                 "entry_point": "hepem_step_subbatches (HEPEM_FORM_MIXED), one call"},
             "plain": {"value": total / (ms_plain / 1e3), "unit": UNIT, "ms_per_pass": ms_plain},
             "batched_default_launch": {"value": total / (ms_default / 1e3), "unit": UNIT, "ms_per_pass": ms_default},
             "batched": {"value": total / (ms_batched / 1e3), "unit": UNIT, "ms_per_pass": ms_batched,

@@ -305,16 +305,73 @@ int hepem_step_mixed(const hepem_ctx* c, int64_t n, const hepem_track_state* in,
   return step_batched(c, n, in, out, uniforms, nu, seed, res, counters, stream, true);
 }
 
-// The device-mapped address of a page-locked host array (cudaHostAlloc,
-// cudaHostRegister), or null when the GPU cannot address it directly.
-static void* mapped_address(const void* h) {
-  if (!h) return nullptr;
-  cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
-    cudaGetLastError();
-    return nullptr;
+int hepem_step_subbatches(const hepem_ctx* c, int form, int32_t nb, const hepem_subbatch* batches,
+                          const hepem_track_state* in, hepem_track_state* out, const double* uniforms, int32_t nu,
+                          hepem_step_out* res, hepem_step_counters* counters, void* stream) {
+  if (!c || nb < 0 || nu < 0) return fail(HEPEM_BAD_ARG, "bad context, sub-batch count or size");
+  if (form != HEPEM_FORM_BATCHED && form != HEPEM_FORM_MIXED)
+    return fail(HEPEM_BAD_ARG, "form must be HEPEM_FORM_BATCHED or HEPEM_FORM_MIXED");
+  if (nb == 0) return HEPEM_OK;
+  if (!batches) return fail(HEPEM_BAD_ARG, "null sub-batch array");
+  std::vector<hepem_subbatch> b(batches, batches + nb);
+  std::stable_sort(b.begin(), b.end(), [](const hepem_subbatch& x, const hepem_subbatch& y) {
+    return x.offset < y.offset;
+  });
+  std::vector<int64_t> prefix(nb + 1, 0);
+  int64_t end = 0, maxIdx = 0;
+  for (int k = 0; k < nb; ++k) {
+    if (b[k].offset < 0 || b[k].n < 0) return fail(HEPEM_BAD_ARG, "negative sub-batch offset or size");
+    if (b[k].n > 0 && b[k].offset < end) return fail(HEPEM_BAD_ARG, "sub-batches overlap");
+    if (b[k].n > 0) end = b[k].offset + b[k].n;
+    prefix[k + 1] = prefix[k] + b[k].n;
+    if (end > maxIdx) maxIdx = end;
   }
-  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+  const int64_t total = prefix[nb];
+  if (total == 0) return HEPEM_OK;
+  if (maxIdx > (int64_t)INT32_MAX) return fail(HEPEM_BAD_ARG, "batch too large");
+  if (!state_ok(in) || !state_ok(out) || !out_ok(res) || (nu > 0 && !uniforms))
+    return fail(HEPEM_BAD_ARG, "null array in track batch");
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool mixed = form == HEPEM_FORM_MIXED;
+  const bool preCopy = mixed && in->ekin == out->ekin;
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t wsBytes = al(hepem::batched_workspace_bytes(total));
+  const size_t need = wsBytes + al(4 * (size_t)total) + al(8 * (size_t)maxIdx) + al(sizeof(hepem_subbatch) * nb) +
+                      al(8 * (size_t)(nb + 1)) + (preCopy ? hepem::mixed_pre_state_bytes(maxIdx) : 0);
+  void* ws = nullptr;
+  HEPEM_CUDA(cudaMallocAsync(&ws, need, s));
+  uint8_t* p = static_cast<uint8_t*>(ws) + wsBytes;
+  int32_t* active = reinterpret_cast<int32_t*>(p);
+  p += al(4 * (size_t)total);
+  uint64_t* keys = reinterpret_cast<uint64_t*>(p);
+  p += al(8 * (size_t)maxIdx);
+  hepem_subbatch* dB = reinterpret_cast<hepem_subbatch*>(p);
+  p += al(sizeof(hepem_subbatch) * nb);
+  int64_t* dPrefix = reinterpret_cast<int64_t*>(p);
+  p += al(8 * (size_t)(nb + 1));
+  // pageable host -> device copies return once the host arrays have been read
+  cudaError_t e = cudaMemcpyAsync(dB, b.data(), sizeof(hepem_subbatch) * nb, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dPrefix, prefix.data(), 8 * (size_t)(nb + 1), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = hepem::launch_subbatch_index(dB, dPrefix, nb, total, active, keys, s, c->sms);
+  if (e == cudaSuccess) {
+    hepem::BatchOpts o;
+    o.ev = c->profile ? const_cast<cudaEvent_t*>(c->stageEv) : nullptr;
+    o.cfg = &c->launch;
+    o.mixed = mixed;
+    o.active = active;
+    o.seeds = keys;
+    hepem::apply_table_window(c, o);
+    hepem_track_state pre;
+    if (preCopy) {
+      pre = hepem::carve_pre_state(p, maxIdx, *in);
+      o.preState = &pre;
+    }
+    e = hepem::launch_step_batched(c->tables, total, *in, *out, uniforms, nu, 0, *res, counters, ws, s, c->sms, o);
+  }
+  const cudaError_t f = cudaFreeAsync(ws, s);
+  if (e != cudaSuccess) return cuda_fail(e, "sub-batch step launch");
+  if (f != cudaSuccess) return cuda_fail(f, "cudaFreeAsync");
+  return HEPEM_OK;
 }
 
 // chunks of a host-buffer step: more overlap of the copies against smaller,
@@ -374,18 +431,6 @@ int step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem
   void* const* hres = reinterpret_cast<void* const*>(res);
   static_assert(sizeof(hepem_track_state) == 20 * sizeof(void*), "state struct layout");
   static_assert(sizeof(hepem_step_out) == 14 * sizeof(void*), "out struct layout");
-  // Pinned (page-locked) host arrays have device-mapped addresses: then each
-  // chunk moves in one gather launch and one scatter launch over all its
-  // arrays instead of one copy per array and direction.
-  void* min[20];
-  void* mout[20];
-  void* mres[14];
-  void* mu = nullptr;
-  bool zc = nu == 0 || (mu = mapped_address(uniforms)) != nullptr;
-  for (int k = 0; k < 20 && zc; ++k) zc = (min[k] = mapped_address(hin[k])) != nullptr;
-  for (int k = 3; k < 20 && zc; ++k)
-    if (k != 11 && k != 12) zc = (mout[k] = mapped_address(hout[k])) != nullptr;
-  for (int k = 0; k < 14 && zc; ++k) zc = (mres[k] = mapped_address(hres[k])) != nullptr;
   hepem_step_counters* dcnt[hepem_ctx::kSlots] = {};
   for (int ch = 0; ch < nChunks; ++ch) {
     const int64_t off = (int64_t)ch * m;
@@ -412,29 +457,11 @@ int step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem
     hepem_step_out dr;
     memcpy(&ds, dstate, sizeof(ds));
     memcpy(&dr, dout, sizeof(dr));
-    if (zc) {
-      hepem::SegList g;
-      g.n = 0;
-      for (int k = 0; k < 20; ++k) {
-        g.src[g.n] = (const uint8_t*)min[k] + kStateSizes[k] * off;
-        g.dst[g.n] = (uint8_t*)dstate[k];
-        g.bytes[g.n++] = kStateSizes[k] * mc;
-      }
-      if (nu > 0) {
-        g.src[g.n] = (const uint8_t*)mu + sizeof(double) * (size_t)off * nu;
-        g.dst[g.n] = (uint8_t*)du;
-        g.bytes[g.n++] = sizeof(double) * (size_t)mc * nu;
-      }
-      hepem::seglist_finish(g);
-      HEPEM_CUDA(hepem::launch_copy_segments(g, ss, c->sms));
-    } else {
-      for (int k = 0; k < 20; ++k)
-        HEPEM_CUDA(cudaMemcpyAsync(dstate[k], (const uint8_t*)hin[k] + kStateSizes[k] * off, kStateSizes[k] * mc,
-                                   cudaMemcpyHostToDevice, ss));
-      if (nu > 0)
-        HEPEM_CUDA(cudaMemcpyAsync(du, uniforms + off * nu, sizeof(double) * (size_t)mc * nu,
-                                   cudaMemcpyHostToDevice, ss));
-    }
+    for (int k = 0; k < 20; ++k)
+      HEPEM_CUDA(cudaMemcpyAsync(dstate[k], (const uint8_t*)hin[k] + kStateSizes[k] * off, kStateSizes[k] * mc,
+                                 cudaMemcpyHostToDevice, ss));
+    if (nu > 0)
+      HEPEM_CUDA(cudaMemcpyAsync(du, uniforms + off * nu, sizeof(double) * (size_t)mc * nu, cudaMemcpyHostToDevice, ss));
     hepem::BatchOpts o;
     o.cfg = &c->launch;
     o.mixed = mixed;
@@ -447,32 +474,14 @@ int step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem
     HEPEM_CUDA(hepem::launch_step_batched(c->tables, mc, ds, ds, du, nu, seed, dr, counters ? cnt : nullptr, dwork,
                                           ss, c->sms, o));
     // persistent per-track fields come back (type/imc/id/safety/boundary are inputs only)
-    if (zc) {
-      hepem::SegList g;
-      g.n = 0;
-      for (int k = 3; k < 20; ++k) {
-        if (k == 11 || k == 12) continue;
-        g.src[g.n] = (const uint8_t*)dstate[k];
-        g.dst[g.n] = (uint8_t*)mout[k] + kStateSizes[k] * off;
-        g.bytes[g.n++] = kStateSizes[k] * mc;
-      }
-      for (int k = 0; k < 14; ++k) {
-        g.src[g.n] = (const uint8_t*)dout[k];
-        g.dst[g.n] = (uint8_t*)mres[k] + kOutSizes[k] * off;
-        g.bytes[g.n++] = kOutSizes[k] * mc;
-      }
-      hepem::seglist_finish(g);
-      HEPEM_CUDA(hepem::launch_copy_segments(g, ss, c->sms));
-    } else {
-      for (int k = 3; k < 20; ++k) {
-        if (k == 11 || k == 12) continue;
-        HEPEM_CUDA(cudaMemcpyAsync((uint8_t*)hout[k] + kStateSizes[k] * off, dstate[k], kStateSizes[k] * mc,
-                                   cudaMemcpyDeviceToHost, ss));
-      }
-      for (int k = 0; k < 14; ++k)
-        HEPEM_CUDA(cudaMemcpyAsync((uint8_t*)hres[k] + kOutSizes[k] * off, dout[k], kOutSizes[k] * mc,
-                                   cudaMemcpyDeviceToHost, ss));
+    for (int k = 3; k < 20; ++k) {
+      if (k == 11 || k == 12) continue;
+      HEPEM_CUDA(cudaMemcpyAsync((uint8_t*)hout[k] + kStateSizes[k] * off, dstate[k], kStateSizes[k] * mc,
+                                 cudaMemcpyDeviceToHost, ss));
     }
+    for (int k = 0; k < 14; ++k)
+      HEPEM_CUDA(cudaMemcpyAsync((uint8_t*)hres[k] + kOutSizes[k] * off, dout[k], kOutSizes[k] * mc,
+                                 cudaMemcpyDeviceToHost, ss));
   }
   if (hout[0] != hin[0]) {
     for (int k : {0, 1, 2, 11, 12}) memcpy(hout[k], hin[k], kStateSizes[k] * n);

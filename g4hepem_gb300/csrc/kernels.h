@@ -127,6 +127,12 @@ struct BatchOpts {
   double* gstep = nullptr;
   Limits limits = {};
 };
+// the index list and per-track RNG keys of a sub-batch step: active[p] =
+// offset_b + (p - prefix[b]) and keys[that index] = seed_b for the
+// sub-batch b holding position p (prefix: exclusive sums of the sizes,
+// nb + 1 entries; batches and prefix in device memory)
+cudaError_t launch_subbatch_index(const hepem_subbatch* batches, const int64_t* prefix, int nb, int64_t total,
+                                  int32_t* active, uint64_t* keys, cudaStream_t s, int sms);
 // bytes of the pre-step copy of an in-place precision-form step (n tracks)
 size_t mixed_pre_state_bytes(int64_t n);
 // carve the copy from `mem` (mixed_pre_state_bytes(n) bytes) around the batch `in`
@@ -161,23 +167,6 @@ cudaError_t launch_woodcock(const DevTables& T, int64_t n, const hepem_track_sta
                             const hepem_track_state& out, double* px, double* py, double* pz,
                             const hepem_layered_box& box, const double* uniforms, int nu, uint64_t seed,
                             const hepem_step_out& res, uint8_t* reached, cudaStream_t s, int sms);
-
-// Copies of up to kMaxSegs byte ranges in one launch (the host-buffer steps:
-// the caller's pinned arrays, reached through their device-mapped addresses,
-// to and from the device batch).  Ranges are moved in 16-byte units where both
-// ends are 16-byte aligned, by bytes otherwise.
-constexpr int kMaxSegs = 48;
-struct SegList {
-  const uint8_t* src[kMaxSegs];
-  uint8_t* dst[kMaxSegs];
-  uint64_t bytes[kMaxSegs];
-  uint64_t unitStart[kMaxSegs + 1];  // prefix sums of each range's units (16 B, or 1 B unaligned)
-  uint32_t vec;                      // bit k: range k moves in 16-byte units
-  int n;
-};
-// fills unitStart / vec from src, dst, bytes, n
-void seglist_finish(SegList& L);
-cudaError_t launch_copy_segments(const SegList& L, cudaStream_t s, int sms);
 
 cudaError_t launch_fill_uniforms(int64_t n, const int32_t* id, int nu, uint64_t seed, double* u, cudaStream_t s,
                                  int sms);

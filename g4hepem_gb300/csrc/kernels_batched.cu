@@ -1175,6 +1175,32 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
   return le != cudaSuccess ? le : e2;
 }
 
+// ---- sub-batches: index list and per-track RNG keys --------------------------------------
+__global__ void __launch_bounds__(256) subbatch_index_kernel(const hepem_subbatch* __restrict__ batches,
+                                                             const int64_t* __restrict__ prefix, int nb,
+                                                             int64_t total, int32_t* __restrict__ active,
+                                                             uint64_t* __restrict__ keys) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < total; p += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nb - 1;  // prefix[lo] <= p < prefix[lo + 1]
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (prefix[mid] <= p) lo = mid; else hi = mid - 1;
+    }
+    const int64_t i = batches[lo].offset + (p - prefix[lo]);
+    active[p] = (int32_t)i;
+    keys[i] = batches[lo].seed;
+  }
+}
+
+cudaError_t launch_subbatch_index(const hepem_subbatch* batches, const int64_t* prefix, int nb, int64_t total,
+                                  int32_t* active, uint64_t* keys, cudaStream_t s, int sms) {
+  if (total <= 0 || nb <= 0) return cudaSuccess;
+  const int64_t blocks = (total + 255) / 256;
+  const int g = (int)(blocks < (int64_t)sms * 16 ? blocks : (int64_t)sms * 16);
+  subbatch_index_kernel<<<g, 256, 0, s>>>(batches, prefix, nb, total, active, keys);
+  return cudaGetLastError();
+}
+
 // ---- 4. per-model sampling (interaction unit tests and distribution checks) -------------
 // n independent draws of one interaction model at a fixed energy and couple:
 // draw i is a track with id i, direction +z and the pure Philox stream of

@@ -483,51 +483,6 @@ cudaError_t launch_step(const DevTables& T, int64_t n, const hepem_track_state& 
   return cudaGetLastError();
 }
 
-// ---- byte-range copies (host-buffer steps over mapped pinned memory) ----------------------
-__global__ void __launch_bounds__(256) copy_segments_kernel(const __grid_constant__ SegList L) {
-  const uint64_t total = L.unitStart[L.n];
-  for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < total;
-       u += (uint64_t)gridDim.x * blockDim.x) {
-    int lo = 0, hi = L.n - 1;  // the range holding unit u: unitStart[k] <= u < unitStart[k + 1]
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (L.unitStart[mid] <= u) lo = mid; else hi = mid - 1;
-    }
-    const uint64_t k = u - L.unitStart[lo];
-    if (L.vec & (1u << lo)) {
-      const uint64_t nfull = L.bytes[lo] >> 4;
-      if (k < nfull) {
-        reinterpret_cast<uint4*>(L.dst[lo])[k] = reinterpret_cast<const uint4*>(L.src[lo])[k];
-      } else {
-        // the tail of a range that is not a multiple of 16 bytes
-        for (uint64_t b = nfull << 4; b < L.bytes[lo]; ++b) L.dst[lo][b] = L.src[lo][b];
-      }
-    } else {
-      L.dst[lo][k] = L.src[lo][k];
-    }
-  }
-}
-
-void seglist_finish(SegList& L) {
-  L.vec = 0;
-  L.unitStart[0] = 0;
-  for (int k = 0; k < L.n; ++k) {
-    const bool al = ((reinterpret_cast<uintptr_t>(L.src[k]) | reinterpret_cast<uintptr_t>(L.dst[k])) & 15u) == 0;
-    uint64_t units = L.bytes[k];
-    if (al) {
-      L.vec |= 1u << k;
-      units = (L.bytes[k] >> 4) + ((L.bytes[k] & 15u) ? 1 : 0);
-    }
-    L.unitStart[k + 1] = L.unitStart[k] + units;
-  }
-}
-
-cudaError_t launch_copy_segments(const SegList& L, cudaStream_t s, int sms) {
-  if (L.n <= 0 || L.unitStart[L.n] == 0) return cudaSuccess;
-  copy_segments_kernel<<<grid_for((int64_t)L.unitStart[L.n], 256, sms), 256, 0, s>>>(L);
-  return cudaGetLastError();
-}
-
 cudaError_t launch_howfar(const DevTables& T, int64_t n, const hepem_track_state& in, const double* uniforms, int nu,
                           uint64_t seed, double* gstep, const Limits& L, hepem_step_counters* counters,
                           cudaStream_t s, int sms) {

@@ -48,6 +48,10 @@ class StepCounters(C.Structure):
                 ("secondaries", C.c_uint64), ("interactions", C.c_uint64 * 8), ("fp64_fallback", C.c_uint64)]
 
 
+class SubBatch(C.Structure):
+    _fields_ = [("offset", C.c_int64), ("n", C.c_int64), ("seed", C.c_uint64)]
+
+
 class LaunchConfig(C.Structure):
     _fields_ = [("block", C.c_int32 * 11), ("ctas_per_sm", C.c_int32 * 11), ("sort_energy_bins", C.c_int32),
                 ("ms", C.c_float * 11)]
@@ -95,7 +99,7 @@ EXPORTED = ["hepem_create", "hepem_create_from_file", "hepem_image_from_json", "
             "hepem_server_destroy", "hepem_sample_model", "hepem_stack_secondaries", "hepem_woodcock_gamma", "hepem_get_launch_config", "hepem_set_launch_config", "hepem_autotune",
             "hepem_set_table_l2_window", "hepem_step_limit_bytes", "hepem_howfar", "hepem_perform",
             "hepem_howfar_host", "hepem_perform_host", "hepem_electron_xs_stepping", "hepem_brem_select_target",
-            "hepem_conv_select_target", "hepem_gamma_xs"]
+            "hepem_conv_select_target", "hepem_gamma_xs", "hepem_step_subbatches"]
 FORMS = {"plain": 0, "batched": 1, "mixed": 2}
 STATUS_CANCELLED, STATUS_TIMEOUT, STATUS_OOM_ADMISSION = 8, 5, 6
 
@@ -161,6 +165,8 @@ def lib():
         L.hepem_perform.argtypes = [_vp, C.c_int, C.c_int64, C.POINTER(TrackState), C.POINTER(TrackState), _vp,
                                     _vp, _vp, C.c_int32, C.c_uint64, C.POINTER(StepOut), _vp, _vp]
         L.hepem_perform_host.argtypes = L.hepem_perform.argtypes
+        L.hepem_step_subbatches.argtypes = [_vp, C.c_int, C.c_int32, C.POINTER(SubBatch), C.POINTER(TrackState),
+                                            C.POINTER(TrackState), _vp, C.c_int32, C.POINTER(StepOut), _vp, _vp]
         L.hepem_electron_xs_stepping.argtypes = [_vp, C.c_int64, C.c_int, C.c_int] + [_vp] * 7 + [_vp]
         L.hepem_brem_select_target.argtypes = [_vp, C.c_int64, C.c_int, C.c_int, C.c_int] + [_vp] * 4 + [_vp]
         L.hepem_conv_select_target.argtypes = [_vp, C.c_int64, C.c_int] + [_vp] * 4 + [_vp]
@@ -272,6 +278,15 @@ class Context:
               "noalloc": lib().hepem_step_batched_noalloc}[form]
         check(fn(self.h, n, C.byref(sin), C.byref(sout), _ptr(uniforms), n_uniform, seed, C.byref(sres),
                  _ptr(counters) if counters is not None else None, _stream_ptr(stream)))
+
+    def step_subbatches(self, batches, state_in: dict, state_out: dict, uniforms, n_uniform: int, res: dict,
+                        counters=None, stream=None, form="batched"):
+        """hepem_step_subbatches: batches = [(offset, n, seed), ...] over the same arrays."""
+        arr = (SubBatch * max(len(batches), 1))(*[SubBatch(int(o), int(n), int(sd)) for o, n, sd in batches])
+        sin, sout, sres = make_state_struct(state_in), make_state_struct(state_out), make_out_struct(res)
+        check(lib().hepem_step_subbatches(self.h, FORMS[form], len(batches), arr, C.byref(sin), C.byref(sout),
+                                          _ptr(uniforms) if n_uniform else None, n_uniform, C.byref(sres),
+                                          _ptr(counters) if counters is not None else None, _stream_ptr(stream)))
 
     # -- single functions of the path (the reference's device-test quantities) ----
     def electron_xs_stepping(self, ekin, imc, positron=False, mixed=False, stream=None):

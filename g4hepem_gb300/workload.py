@@ -154,31 +154,40 @@ def electron_lookup_batch(n: int, n_couples: int = 3, seed: int = 11, emin=1e-3,
     return ekin, imc
 
 
-def subbatch_sizes(total: int = 1 << 24, n_sub: int = 64, median: float = 30000.0, sigma: float = 1.5,
-                   lo: int = 1000, hi: int = 1 << 20, seed: int = 3) -> np.ndarray:
+def subbatch_sizes(total: int = 1 << 24, n_sub: int = 64, median: float = 30000.0, lo: int = 1000,
+                   hi: int = 1 << 20, seed: int = 3):
     """Uneven sub-batch sizes of the batching workload: log-normal with the
-    given median and sigma, scaled so that the clipped sizes sum to `total`
-    (the scale factor is found by bisection; the last size absorbs rounding)."""
+    given median, clipped to [lo, hi], with the width sigma chosen so that the
+    clipped sizes of the n_sub draws sum to `total` (the draws z_k of a
+    standard normal are fixed by the seed, sigma is found by bisection on the
+    clipped sum of median * exp(sigma z_k), with the z_k shifted so that their
+    median is 0; rounding is absorbed by the sizes inside the clip range).
+    Returns (sizes, sigma)."""
     rng = np.random.Generator(np.random.Philox(seed))
-    base = median * np.exp(sigma * rng.standard_normal(n_sub))
-    f_lo, f_hi = 1e-6, 1e6
+    z = rng.standard_normal(n_sub)
+    z -= np.median(z)  # the median draw is the stated median
+
+    def clipped_sum(sig):
+        return np.clip(median * np.exp(sig * z), lo, hi).sum()
+
+    s_lo, s_hi = 0.0, 20.0
     for _ in range(200):
-        f = np.sqrt(f_lo * f_hi)
-        s = np.clip(base * f, lo, hi).sum()
-        if s < total:
-            f_lo = f
+        sig = 0.5 * (s_lo + s_hi)
+        if clipped_sum(sig) < total:
+            s_lo = sig
         else:
-            f_hi = f
-    sizes = np.clip(np.round(base * np.sqrt(f_lo * f_hi)), lo, hi).astype(np.int64)
+            s_hi = sig
+    sigma = 0.5 * (s_lo + s_hi)
+    sizes = np.clip(np.round(median * np.exp(sigma * z)), lo, hi).astype(np.int64)
     diff = total - int(sizes.sum())
-    order = np.argsort(-sizes) if diff < 0 else np.argsort(sizes)
+    free = [k for k in np.argsort(-sizes) if lo < sizes[k] < hi]
     k = 0
-    while diff != 0:
-        j = order[k % n_sub]
+    while diff != 0 and free:
+        j = free[k % len(free)]
         step = int(np.clip(sizes[j] + diff, lo, hi)) - int(sizes[j])
         sizes[j] += step
         diff -= step
         k += 1
         if k > 10 * n_sub:
             break
-    return sizes
+    return sizes, sigma

@@ -54,6 +54,11 @@ enum {
 
 typedef struct hepem_ctx hepem_ctx;
 
+/* Forms of the step, for the entry points that take one: the plain FP64 form
+ * (hepem_step), the batched FP64 form (hepem_step_batched) and the precision
+ * form (hepem_step_mixed). */
+enum { HEPEM_FORM_PLAIN = 0, HEPEM_FORM_BATCHED = 1, HEPEM_FORM_MIXED = 2 };
+
 /* ---- track batches ----------------------------------------------------- */
 /* Persistent per-track state, SoA, arrays of length n.  Mirrors the fields of
  * G4HepEmTrack (G4HepEm/G4HepEmRun/include/G4HepEmTrack.hh:246-264),
@@ -202,6 +207,28 @@ int  hepem_step_batched_noalloc(const hepem_ctx* ctx, int64_t n, const hepem_tra
                                 int32_t n_uniform, uint64_t seed, hepem_step_out* res,
                                 hepem_step_counters* counters, void* stream);
 
+/* Many sub-batches (e.g. the track batches of several events) stepped in ONE
+ * sorted and queued pass: one sort and one sequence of stage kernels over
+ * all of them, instead of one call per sub-batch.  The sub-batches lie in
+ * the same SoA arrays: sub-batch b is tracks [offset, offset + n) with
+ * uniforms keyed by its own seed (uniforms[i*n_uniform + k] for track i, and
+ * hepem_philox_uniform(seed_b, id[i], k) past them).  Ranges must not overlap;
+ * tracks outside every range are left as they are (also in `out`).  form:
+ * HEPEM_FORM_BATCHED or HEPEM_FORM_MIXED; the results equal one
+ * hepem_step_batched / hepem_step_mixed call per sub-batch, bit for bit.
+ * `batches` is a host array; counters (device, may be NULL) are the sums
+ * over all sub-batches.  Uses a stream-ordered workspace.  No reference
+ * counterpart (the reference steps one track at a time). */
+typedef struct hepem_subbatch {
+  int64_t  offset;   /* first track of the sub-batch in the arrays            */
+  int64_t  n;        /* number of its tracks                                  */
+  uint64_t seed;     /* key of its tracks' uniform streams                    */
+} hepem_subbatch;
+int  hepem_step_subbatches(const hepem_ctx* ctx, int form, int32_t n_batches, const hepem_subbatch* batches,
+                           const hepem_track_state* in, hepem_track_state* out, const double* uniforms,
+                           int32_t n_uniform, hepem_step_out* res, hepem_step_counters* counters,
+                           void* stream);
+
 /* Precision form of hepem_step_batched: the e+- HowFar and continuous step
  * (step limits, MSC, energy loss and its fluctuations, the delta-interaction
  * test), the gamma HowFar and interaction choice, and the interaction models
@@ -280,7 +307,6 @@ int  hepem_step_host_mixed(const hepem_ctx* ctx, int64_t n, const hepem_track_st
  * close to call, are stepped again in FP64 from the pre-step state).
  * counters (device, may be NULL): hepem_howfar adds the uniforms it consumed;
  * hepem_perform adds the step, its uniforms, interactions and secondaries. */
-enum { HEPEM_FORM_PLAIN = 0, HEPEM_FORM_BATCHED = 1, HEPEM_FORM_MIXED = 2 };
 int64_t hepem_step_limit_bytes(int64_t n);
 int  hepem_howfar(const hepem_ctx* ctx, int form, int64_t n, const hepem_track_state* tracks,
                   const double* uniforms, int32_t n_uniform, uint64_t seed, double* gstep, void* limits,

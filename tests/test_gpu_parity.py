@@ -180,10 +180,9 @@ def test_host_entry_point_equals_device_entry_point(native, gpu_ctx):
 @pytest.mark.parametrize("mixed", [False, True])
 @pytest.mark.parametrize("in_place", [False, True])
 def test_host_entry_point_pinned_buffers(native, gpu_ctx, mixed, in_place):
-    """Pinned host buffers take the mapped path (one gather and one scatter
-    launch per chunk over all arrays): the same results as pageable buffers
-    (one copy per array), in and out of place,
-    with and without a uniform buffer, over several chunks."""
+    """Pinned host buffers give the same results as pageable ones, in and out
+    of place, with and without a uniform buffer, over several chunks (a
+    ragged last one)."""
     import torch
     n = 300001
     st = W.mixed_batch(n, seed=29)

@@ -53,11 +53,14 @@ def test_electron_lookup_batch_ranges():
     assert set(np.unique(imc)) == {0, 1, 2}
 
 
-def test_subbatch_sizes_sum_and_clip():
-    s = W.subbatch_sizes()
+def test_subbatch_sizes_sum_clip_and_median():
+    s, sigma = W.subbatch_sizes()
     assert len(s) == 64 and int(s.sum()) == 1 << 24
     assert s.min() >= 1000 and s.max() <= 1 << 20
-    assert len(np.unique(s)) > 32  # uneven
+    assert len(np.unique(s)) > 16  # uneven
+    # the median of the draws is the stated 30k (no rescaling of the sizes)
+    assert 0.5 * 30000 < np.median(s) < 2.0 * 30000
+    assert 2.0 < sigma < 8.0
 
 
 def test_uniform_streams_depend_on_seed_and_id_only():
