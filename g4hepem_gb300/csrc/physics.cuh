@@ -88,8 +88,19 @@ __device__ __forceinline__ double spline(double x1, double x2, double y1, double
   const double c1 = (1.0 + b) * s2;
   return y1 + b * (y2 - y1) + (b * (b - 1.0)) * (c0 + c1) * (dl * dl * os);
 }
+// (int)max(0, min(v, hi)) for an integer hi >= 0, as the FP64 min/max and the
+// truncation give it (NaN: hi), in integer operations on the bits of v
+__device__ __forceinline__ int clamp_trunc(double v, int hi) {
+  const long long b = __double_as_longlong(v);
+  if (b <= 0) return 0;  // +0, -0 and negative values
+  const int e = (int)(b >> 52) - 1023;
+  if (e < 0) return 0;
+  if (e >= 31) return hi;  // also inf and NaN
+  const int t = (int)(((b & 0xFFFFFFFFFFFFFLL) | (1LL << 52)) >> (52 - e));
+  return t < hi ? t : hi;
+}
 __device__ __forceinline__ int bin_of(double lx, double lxm, double ild, int nd) {
-  return (int)dmax_(0., dmin_((lx - lxm) * ild, nd - 2.));
+  return clamp_trunc((lx - lxm) * ild, nd - 2);
 }
 __device__ __forceinline__ double spline_log_xy(int nd, const double* xd, const double* yd, double x, double lx,
                                                 double lxm, double ild) {
@@ -114,7 +125,7 @@ __device__ __forceinline__ double spline_log_9(int nd, const double* d, double x
 __device__ __forceinline__ int lower_bin(const double* xd, int num, double x, int step) {
   int ml = -1, mu = num - 1;
   while (abs(mu - ml) > 1) {
-    const int mav = 0.5 * (ml + mu);
+    const int mav = (ml + mu) / 2;  // (int)(0.5 * (ml + mu)): both truncate toward 0
     if (x < ld(xd + step * mav)) mu = mav; else ml = mav;
   }
   return mu - 1;
@@ -157,8 +168,8 @@ __device__ __forceinline__ double inv_range(const DevElData& d, int imc, double 
 }
 __device__ __forceinline__ double rest_macxs(const DevElData& d, int imc, double e, double le, bool ioni) {
   const int i0 = ld(d.xsStart + imc);
-  const int st = ioni ? i0 : i0 + 3 * (int)ld(d.xs + i0) + 5;
-  const int nd = (int)ld(d.xs + st);
+  const int st = ioni ? i0 : i0 + 3 * double_to_int_rz_exact(ld(d.xs + i0)) + 5;
+  const int nd = double_to_int_rz_exact(ld(d.xs + st));
   if (e < ld(d.xs + st + 5)) return 0.0;
   return dmax_(0.0, spline_log_3(nd, d.xs + st + 5, e, le, ld(d.xs + st + 3), ld(d.xs + st + 4)));
 }
@@ -170,8 +181,8 @@ __device__ __forceinline__ double nuc_macxs(const DevElData& d, int imat, double
 __device__ __forceinline__ double rest_macxs_stepping(const DevElData& d, int imc, double e, double le, bool ioni) {
   const double log08 = -0.22314355131420971;
   const int i0 = ld(d.xsStart + imc);
-  const int st = ioni ? i0 : i0 + 3 * (int)ld(d.xs + i0) + 5;
-  const int nd = (int)ld(d.xs + st);
+  const int st = ioni ? i0 : i0 + 3 * double_to_int_rz_exact(ld(d.xs + i0)) + 5;
+  const int nd = double_to_int_rz_exact(ld(d.xs + st));
   const double minE = ld(d.xs + st + 5), maxE = ld(d.xs + st + 1), maxV = ld(d.xs + st + 2);
   if (e > maxE) {
     const double er = 0.8 * e;
@@ -911,11 +922,11 @@ struct Physics {
     const DevElData& d = eld();
     const int st = ld(d.selStart[which] + t.imc);
     const double* D = d.sel[which] + st;
-    const int nd = (int)ld(D);
-    const int ne = (int)ld(D + 1);
+    const int nd = double_to_int_rz_exact(ld(D));
+    const int ne = double_to_int_rz_exact(ld(D + 1));
     const double* x = D + 4;
     const double xv = dmax_(ld(x), dmin_(ld(x + ne * (nd - 1)), E));
-    const int ie = (int)dmax_(0.0, dmin_((le - ld(D + 2)) * ld(D + 3), nd - 2.0));
+    const int ie = clamp_trunc((le - ld(D + 2)) * ld(D + 3), nd - 2);
     int i0 = ie * ne, i1 = i0 + ne;
     const double x1 = ld(x + i0++), x2 = ld(x + i1++);
     const double b = dmax_(0., dmin_(1., (xv - x1) / (x2 - x1)));
@@ -948,16 +959,16 @@ struct Physics {
     const int nElem = ld(&md.nElem);
     const int ei = nElem > 1 ? select_brem_target(E, le, rng.flat(), 1) : 0;
     const int Z = ld(T.matElemZ + ld(&md.elemOff) + ei);
-    const double dZ = (double)Z;
+    const double dZ = int_to_double_exact(Z);
     const DevSB& sb = T.sb;
     const int st = ld(sb.startPerZ + Z);
     const int gci = ld(sb.gcIdx + ld(sb.gcStart + t.imc) + ei);
     bool corner = false, simple = false;
-    int ie = (int)ld(sb.data + st + 2);
+    int ie = double_to_int_rz_exact(ld(sb.data + st + 2));
     if (E < ld(sb.elE + ie)) {
       const double val = (le - sb.logMinE) * sb.ildE;
-      ie = (int)val;
-      double pH = val - ie;
+      ie = double_to_int_rz_exact(val);
+      double pH = val - int_to_double_exact(ie);
       if (ie < 0 || ie > kNumElEnergySB - 2) { t.flags |= kFlagBadIndex; return E; }
       if (ld(sb.elE + ie) <= gcut) {
         pH = (le - lgcut) / (ld(sb.lelE + ie + 1) - lgcut);
@@ -966,10 +977,10 @@ struct Physics {
       if (rng.flat() < pH) ++ie;
       else if (corner) simple = true;
     }
-    const int minIE = (int)ld(sb.data + st + 1);
-    const int maxIE = (int)ld(sb.data + st + 2);
+    const int minIE = double_to_int_rz_exact(ld(sb.data + st + 1));
+    const int maxIE = double_to_int_rz_exact(ld(sb.data + st + 2));
     if (ie < minIE || ie > maxIE) { t.flags |= kFlagBadIndex; return E; }
-    const int ncut = (int)ld(sb.data + st + 3);
+    const int ncut = double_to_int_rz_exact(ld(sb.data + st + 3));
     const int size1 = ncut + 3 * kNumKappaSB;
     const int tst = st + 4 + (ie - minIE) * size1;
     const double minV = ld(sb.data + tst + gci);
@@ -1116,8 +1127,8 @@ struct Physics {
     }
     if (sh < 2.0) {
       double val = sh * 20.0;
-      int il = (int)val;
-      val -= il;
+      int il = double_to_int_rz_exact(val);
+      val -= int_to_double_exact(il);
       il *= 2;
       il = il < 0 ? 0 : (il > 78 ? 78 : il);
       gS = (kFuncLPM[il + 2] - kFuncLPM[il]) * val + kFuncLPM[il];
@@ -1293,10 +1304,10 @@ struct Physics {
     const DevGamma& g = T.gm;
     const double* D = g.conv + ld(g.convStart + imat);
     const int nd = g.convN;
-    const int ne = (int)ld(D);
+    const int ne = double_to_int_rz_exact(ld(D));
     const double* x = g.convGrid;
     const double xv = dmax_(ld(x), dmin_(ld(x + nd - 1), e));
-    const int ie = (int)dmax_(0.0, dmin_((le - g.convLogMin) * g.convILD, nd - 2.0));
+    const int ie = clamp_trunc((le - g.convLogMin) * g.convILD, nd - 2);
     const double x1 = ld(x + ie), x2 = ld(x + ie + 1);
     const double b = dmax_(0., dmin_(1., (xv - x1) / (x2 - x1)));
     const int i0 = ie * (ne - 1) + 1;
