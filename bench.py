@@ -45,9 +45,8 @@ NU = 64
 SEED = 20261203
 WORKLOAD_SEED = 7
 LAUNCHES_PER_STEP = 14  # 3 sort kernels, 2 stage-A kernels, 9 interaction kernels (plus two memsets)
-# precision form: + the FP64 redo of the tracks whose FP32 decisions were too
-# close to call (its stage A and nine interaction kernels) at the end of the step
-LAUNCHES_PER_STEP_MIXED = 24
+# precision form: + one FP64 fallback kernel at the end of the step
+LAUNCHES_PER_STEP_MIXED = 15
 METRIC = "mixed e±/γ physics steps/s (1 GB300) vs plain FP64 path; p50/p99 batch latency"
 UNIT = "steps/s"
 CONFIG = {"workload": "full physics step (HowFar + Perform), 4,194,304 mixed tracks (45% gamma, 45% e-, 10% e+), "

@@ -768,33 +768,35 @@ __global__ void __launch_bounds__(BS, MODE == kStageMixed ? HEPEM_MIXED_B_WARPS 
   add_counters(cnt, counters);
 }
 
-#if HEPEM_FP64_UNIT
-// Precision form, the end of a step: the FP64 redo of every track on the
-// fallback list.  A tripped e+- stage A, or a tripped e+- interaction, is
+// Precision form, last kernel of the step: the FP64 redo of every track on
+// the fallback list.  A tripped e+- stage A, or a tripped e+- interaction, is
 // stepped again entirely in FP64 from its pre-step state (the interaction's
 // input energy carries the FP32 continuous loss, so the FP64 interaction
 // alone would not give the FP64 path's outcome at the near-tie that tripped
-// the guard); in the Perform phase of the split step that is HowFar from the
-// pre-step state with the pre-step boundary status (HowFar left the state
-// unchanged), then the caller's transport (its geometrical step, unless it is
-// the proposed one, the direction and the post-step boundary status in the
-// state), then Perform -- an unshortened step is the FP64 proposed one, as in
-// the fused step.  A tripped gamma interaction has exact inputs: only the
-// FP64 interaction is redone.
-// The FP64 redo in two stages, so that the FP64 interaction models run one
-// model per kernel as in the FP64 form: fallback_stage_a_kernel steps every
-// e+- on the fallback list through its FP64 stage A (from the pre-step state,
-// as charged_full_step) and every gamma whose FP32 stage A tripped through the
-// FP64 gamma stage A, stores them, and queues their interactions -- and the
-// tripped gamma interactions as they are -- on fallback queues (the queue
-// arrays, free again after stage B, with counts at counts[kFbQueueShift + 3 +
-// Q]); the FP64 interaction kernels then run over those queues.
-constexpr int kFbQueueShift = 13;
+// the guard).  A tripped gamma interaction has exact inputs: only the FP64
+// interaction is redone.  One launch for all of them keeps the latency of
+// these few long FP64 threads to one kernel's tail.
+template <int Q>
+__device__ __forceinline__ void interaction_fp64(Physics& P) {
+  if (Q == kQIoniEm || Q == kQIoniEp) P.ioni();
+  if (Q == kQBremSB) P.brem(true);
+  if (Q == kQBremRB) P.brem(false);
+  if (Q == kQAnnihFlight) P.annihilate_in_flight();
+  if (Q == kQAnnihRest) P.annihilate_at_rest();
+}
 
+#if HEPEM_FP64_UNIT
+// PHASE kPhaseHowFar: the FP64 HowFar of a track whose FP32 HowFar tripped,
+// into the step-limit record.  kPhasePerform: the whole step again in FP64:
+// HowFar from the pre-step state with the pre-step boundary status (the state
+// is the pre-step one: HowFar left it unchanged), then the caller's transport
+// (its geometrical step, unless it is the proposed one, the direction and the
+// post-step boundary status in the state), then Perform.  An unshortened step
+// is the FP64 proposed one, as in the fused step (results equal to it).
 template <int PHASE>
-__device__ int charged_stage_a_fp64(const DevTables& T, const hepem_track_state& in, const hepem_track_state& out,
-                                    const double* uniforms, int nu, uint64_t seed, const hepem_step_out& res,
-                                    const Work& w, int32_t i, bool fromStageA, StepCount& cnt) {
+__device__ void charged_full_step(const DevTables& T, const hepem_track_state& in, const hepem_track_state& out,
+                                  const double* uniforms, int nu, uint64_t seed, const hepem_step_out& res,
+                                  const Work& w, int32_t i, bool fromStageA, StepCount& cnt) {
   const hepem_track_state& src = fromStageA ? in : w.pre;
   const int type = in.type[i];
   Track t;
@@ -802,6 +804,14 @@ __device__ int charged_stage_a_fp64(const DevTables& T, const hepem_track_state&
   load_track(src, i, t, rng, uniforms, nu, key_of(w, i, seed), type);
   Physics P{T, rng, t};
   int32_t c0 = rng.cursor;
+  if (PHASE == kPhaseHowFar) {
+    P.el_howfar();
+    store_limits64(w.limits, i, t, rng, type, w.gstep);
+    cnt.uniforms += (uint32_t)(rng.cursor - c0);
+    cnt.overflow += rng.overflow;
+    cnt.fallback += 1;
+    return;
+  }
   if (PHASE == kPhasePerform) {
     const bool post = t.onBoundary;
     t.onBoundary = (w.limits.bits[i] & kLimPreBoundary) != 0;
@@ -814,74 +824,97 @@ __device__ int charged_stage_a_fp64(const DevTables& T, const hepem_track_state&
     P.el_howfar();
   }
   const int key = P.el_perform_until_discrete();
+  const int32_t cA = rng.cursor;
+  const uint32_t ovA = rng.overflow;
+  switch (key) {
+    case kQIoniEm: interaction_fp64<kQIoniEm>(P); break;
+    case kQIoniEp: interaction_fp64<kQIoniEp>(P); break;
+    case kQBremSB: interaction_fp64<kQBremSB>(P); break;
+    case kQBremRB: interaction_fp64<kQBremRB>(P); break;
+    case kQAnnihFlight: interaction_fp64<kQAnnihFlight>(P); break;
+    case kQAnnihRest: interaction_fp64<kQAnnihRest>(P); break;
+    default: break;
+  }
   store_track(in, out, res, i, t, rng, type, false);
-  res.n_sec[i] = 0;
+  store_secondaries(res, i, t, 0);
   if (fromStageA) {
-    // the FP32 stage A counted nothing for this track; a tripped interaction's
-    // stage A was counted there (same discrete outcomes, same uniforms)
+    // stage A counted nothing for this track
     cnt.steps += 1;
     cnt.uniforms += (uint32_t)(rng.cursor - c0);
     cnt.overflow += rng.overflow;
     if (t.winner >= 0 && t.winner < 4) count_inter(cnt, t.winner);
+  } else {
+    cnt.uniforms += (uint32_t)(rng.cursor - cA);
+    cnt.overflow += (rng.overflow && !ovA) ? 1u : 0u;
   }
-  return key;
+  cnt.secondaries += (uint32_t)(t.nsec > 2 ? 2 : t.nsec);
+  cnt.fallback += 1;
 }
 
-template <int BS, int PHASE>
-__global__ void __launch_bounds__(BS) fallback_stage_a_kernel(const __grid_constant__ DevTables T,
-                                                               const hepem_track_state in,
-                                                               const hepem_track_state out,
-                                                               const double* __restrict__ uniforms, int nu,
-                                                               uint64_t seed, const hepem_step_out res, const Work w,
-                                                               hepem_step_counters* counters) {
+// the FP64 step of a gamma whose FP32 stage A tripped: stage A as
+// stage_a_gamma_kernel (MODE kStageFp64) and its interaction as stage_b_one,
+// in one thread from the unchanged input state
+__device__ void gamma_full_step(const DevTables& T, const hepem_track_state& in, const hepem_track_state& out,
+                                const double* uniforms, int nu, uint64_t seed, const hepem_step_out& res,
+                                const Work& w, int32_t i, StepCount& cnt) {
+  Track t;
+  Rng rng;
+  load_track(in, i, t, rng, uniforms, nu, key_of(w, i, seed), 2);
+  const int32_t c0 = rng.cursor;
+  t.isEl = false;
+  Physics P{T, rng, t};
+  P.gamma_howfar();
+  int key = -1;
+  if (t.onBoundary) {
+    t.nia[0] -= t.gstep / t.mfp[0];
+  } else {
+    P.gamma_select();
+    key = P.gamma_perform_until_interaction();
+  }
+  t.pstep = t.gstep;
+  if (key == kQConversion) P.conversion();
+  if (key == kQCompton) P.compton();
+  if (key == kQPhotoelectric) P.photoelectric();
+  if (key != -1) P.gamma_tracking_cut();
+  store_track(in, out, res, i, t, rng, 2, false);
+  store_secondaries(res, i, t, 0);
+  cnt.steps += 1;
+  cnt.uniforms += (uint32_t)(rng.cursor - c0);
+  cnt.overflow += rng.overflow;
+  if (t.winner >= 0 && t.winner < 4) count_inter(cnt, 4 + t.winner);
+  cnt.secondaries += (uint32_t)(t.nsec > 2 ? 2 : t.nsec);
+  cnt.fallback += 1;
+}
+
+template <int BS, int PHASE = kPhaseStep>
+__global__ void __launch_bounds__(BS) final_fallback_kernel(const __grid_constant__ DevTables T,
+                                                             const hepem_track_state in, const hepem_track_state out,
+                                                             const double* __restrict__ uniforms, int nu,
+                                                             uint64_t seed, const hepem_step_out res, const Work w,
+                                                             hepem_step_counters* counters) {
   const int64_t total = w.counts[kFbCount];
   StepCount cnt = {};
-  for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < total; base += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t j = base + threadIdx.x;
-    int key = -1;
-    int32_t i = 0;
-    double pe = 0.0;
-    if (j < total) {
-      i = w.queue[kNumQueues][j];
-      const int kind = w.fbKind[j];
-      if (kind == kFbGammaA) {
-        bool unused = false;
-        key = gamma_item<kStageFp64, kPhaseStep>(T, in, out, uniforms, nu, seed, res, w, i, pe, unused, cnt);
-      } else if (kind == 0 || charged_model(kind - 1)) {
-        key = charged_stage_a_fp64<PHASE>(T, in, out, uniforms, nu, seed, res, w, i, kind == 0, cnt);
-      } else {
-        key = kind - 1;  // a gamma interaction: its inputs are exact
-      }
+  // every block takes an equal contiguous share of the list: the few (~1% of
+  // the tracks), long FP64 steps spread over every SM's FP64 pipe instead of
+  // filling the first blocks, and a share holds mostly one kind (the list is
+  // appended kernel by kernel)
+  const int64_t per = (total + gridDim.x - 1) / gridDim.x;
+  const int64_t j0 = (int64_t)blockIdx.x * per;
+  const int64_t j1 = j0 + per < total ? j0 + per : total;
+  for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
+    const int32_t i = w.queue[kNumQueues][j];
+    const int kind = w.fbKind[j];
+    if (kind == kFbGammaA) {
+      gamma_full_step(T, in, out, uniforms, nu, seed, res, w, i, cnt);
+    } else if (kind == 0 || charged_model(kind - 1)) {
+      charged_full_step<PHASE>(T, in, out, uniforms, nu, seed, res, w, i, kind == 0, cnt);
+    } else {
+      if (kind - 1 == kQConversion)
+        stage_b_one<kQConversion, false>(T, in, out, uniforms, nu, seed, res, w, i, -1, cnt);
+      else if (kind - 1 == kQCompton)
+        stage_b_one<kQCompton, false>(T, in, out, uniforms, nu, seed, res, w, i, -1, cnt);
       cnt.fallback += 1;
     }
-    warp_push(key, i, w.queue, w.counts + kFbQueueShift + 3, pe, w.peXS, kQPhotoelectric);
-  }
-  add_counters(cnt, counters);
-}
-
-// The HowFar phase of the split step: the FP64 HowFar of every e+- whose FP32
-// HowFar tripped, into the step-limit record (an FP64 record).
-template <int BS>
-__global__ void __launch_bounds__(BS) howfar_fallback_kernel(const __grid_constant__ DevTables T,
-                                                              const hepem_track_state in, const hepem_track_state out,
-                                                              const double* __restrict__ uniforms, int nu,
-                                                              uint64_t seed, const hepem_step_out res, const Work w,
-                                                              hepem_step_counters* counters) {
-  const int64_t total = w.counts[kFbCount];
-  StepCount cnt = {};
-  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < total; j += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t i = w.queue[kNumQueues][j];
-    const int type = in.type[i];
-    Track t;
-    Rng rng;
-    load_track(in, i, t, rng, uniforms, nu, key_of(w, i, seed), type);
-    Physics P{T, rng, t};
-    const int32_t c0 = rng.cursor;
-    P.el_howfar();
-    store_limits64(w.limits, i, t, rng, type, w.gstep);
-    cnt.uniforms += (uint32_t)(rng.cursor - c0);
-    cnt.overflow += rng.overflow;
-    cnt.fallback += 1;
   }
   add_counters(cnt, counters);
 }
@@ -954,13 +987,12 @@ struct StageKernels {
   int occ[3][kNumStageKernels];  // resident CTAs per SM
   StageFn mixed[3][kNumStageKernels];  // precision form (null: FP64 only)
   int occMixed[3][kNumStageKernels];
-  // precision form: stage A of the FP64 fallback, fused step / Perform phase
-  StageFn fbA[2];
-  int occFbA[2];
+  StageFn final_[3];                   // precision form: the FP64 fallback kernel
+  int occFinal[3];
   // the split step (256 threads per block): stage A of HowFar / Perform,
   // [phase - 1][0 e+-, 1 gamma], FP64 and FP32; the fallback of each phase
-  StageFn split[2][2], splitMixed[2][2], howfarFb;
-  int occSplit[2][2], occSplitMixed[2][2], occHowfarFb;
+  StageFn split[2][2], splitMixed[2][2], finalSplit[2];
+  int occSplit[2][2], occSplitMixed[2][2], occFinalSplit[2];
 };
 
 static int occupancy_of(StageFn f, int bs) {
@@ -979,24 +1011,26 @@ static const StageKernels& stage_kernels() {
     mixed_stage_table(0, r.mixed[0]);
     mixed_stage_table(1, r.mixed[1]);
     mixed_stage_table(2, r.mixed[2]);
+    r.final_[0] = final_fallback_kernel<128>;
+    r.final_[1] = final_fallback_kernel<256>;
+    r.final_[2] = final_fallback_kernel<512>;
     for (int b = 0; b < 3; ++b) {
       for (int k = 0; k < kNumStageKernels; ++k) {
         r.occ[b][k] = occupancy_of(r.fn[b][k], kBlockSizes[b]);
         r.occMixed[b][k] = r.mixed[b][k] ? occupancy_of(r.mixed[b][k], kBlockSizes[b]) : 0;
       }
+      r.occFinal[b] = occupancy_of(r.final_[b], kBlockSizes[b]);
     }
     split_table<kStageFp64>(r.split);
     mixed_split_table(r.splitMixed);
-    r.fbA[0] = fallback_stage_a_kernel<256, kPhaseStep>;
-    r.fbA[1] = fallback_stage_a_kernel<256, kPhasePerform>;
-    for (int ph = 0; ph < 2; ++ph) r.occFbA[ph] = occupancy_of(r.fbA[ph], 256);
-    r.howfarFb = howfar_fallback_kernel<256>;
-    r.occHowfarFb = occupancy_of(r.howfarFb, 256);
+    r.finalSplit[0] = final_fallback_kernel<256, kPhaseHowFar>;
+    r.finalSplit[1] = final_fallback_kernel<256, kPhasePerform>;
     for (int ph = 0; ph < 2; ++ph) {
       for (int q = 0; q < 2; ++q) {
         r.occSplit[ph][q] = occupancy_of(r.split[ph][q], 256);
         r.occSplitMixed[ph][q] = occupancy_of(r.splitMixed[ph][q], 256);
       }
+      r.occFinalSplit[ph] = occupancy_of(r.finalSplit[ph], 256);
     }
     return r;
   }();
@@ -1073,9 +1107,9 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
   // the stage kernels: with a table window, launched with it as a launch
   // attribute (the caller's stream is left as it is)
   cudaError_t le = cudaSuccess;
-  auto stage_w = [&](StageFn f, int grid, int block, const Work& ww) {
+  auto stage = [&](StageFn f, int grid, int block) {
     if (o.tableBytes == 0) {
-      f<<<grid, block, 0, s>>>(T, in, out, uniforms, nu, seed, res, ww, counters);
+      f<<<grid, block, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
       return;
     }
     cudaLaunchAttribute attr[1];
@@ -1092,18 +1126,8 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
     lc.stream = s;
     lc.attrs = attr;
     lc.numAttrs = 1;
-    const cudaError_t x = cudaLaunchKernelEx(&lc, f, T, in, out, uniforms, nu, seed, res, ww, counters);
+    const cudaError_t x = cudaLaunchKernelEx(&lc, f, T, in, out, uniforms, nu, seed, res, w, counters);
     if (le == cudaSuccess) le = x;
-  };
-  auto stage = [&](StageFn f, int grid, int block) { stage_w(f, grid, block, w); };
-  // the precision form's FP64 redo: stage A over the fallback list, then the
-  // FP64 interaction kernels over the fallback queues
-  auto fallback = [&]() {
-    const int ph = o.phase == kPhasePerform ? 1 : 0;
-    stage(K.fbA[ph], sms * K.occFbA[ph], 256);
-    Work wq = w;
-    wq.counts = w.counts + kFbQueueShift;
-    for (int q2 = 0; q2 < kNumQueues; ++q2) stage_w(K.fn[1][2 + q2], sms * K.occ[1][2 + q2], 256, wq);
   };
   if (o.phase != kPhaseStep) {
     // the split step: its stage A kernels (256 threads, occupancy grids)
@@ -1116,19 +1140,21 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
       mark();
     }
     if (o.phase == kPhaseHowFar) {
-      if (o.mixed) stage(K.howfarFb, sms * K.occHowfarFb, 256);
+      if (o.mixed) stage(K.finalSplit[0], sms * K.occFinalSplit[0], 256);
       const cudaError_t e3 = cudaGetLastError();
       return le != cudaSuccess ? le : e3;
     }
   }
   for (int q = o.phase == kPhaseStep ? 0 : 2; q < kNumStageKernels; ++q) {
     const int b = bs_index(cfg.block[q]);
+    StageFn const finalFn = o.phase == kPhasePerform ? K.finalSplit[1] : K.final_[1];
+    const int finalOcc = o.phase == kPhasePerform ? K.occFinalSplit[1] : K.occFinal[1];
     if (o.mixed && K.mixed[b][q]) {
       // precision form: the FP32 kernel (its FP64 fallbacks run after the last stage)
       const int om = K.occMixed[b][q];
       const int pm = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < om ? cfg.ctasPerSM[q] : om;
       stage(K.mixed[b][q], sms * pm, kBlockSizes[b]);
-      if (q == kNumStageKernels - 1) fallback();
+      if (q == kNumStageKernels - 1) stage(finalFn, sms * finalOcc, 256);
       mark();
       continue;
     }
@@ -1136,7 +1162,7 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
       const int occ = K.occ[b][q];
       const int per = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < occ ? cfg.ctasPerSM[q] : occ;
       stage(K.fn[b][q], sms * per, kBlockSizes[b]);
-      fallback();
+      stage(finalFn, sms * finalOcc, 256);
       mark();
       continue;
     }
