@@ -841,6 +841,18 @@ def main():
                + " (pinned host buffers)",
                "uniforms": "n_uniform = 0: drawn on the device from the same (seed, id, k) stream as the "
                            "buffer of the device-resident runs (identical results), not copied"}
+        if args.form == "mixed":
+            # the bit-exact FP64 form end to end as well (reference precision)
+            host_fn = N.lib().hepem_step_host
+            host_step()
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(ctx_steps):
+                host_step()
+            t_64 = max_over_ranks(torch, time.perf_counter() - t0, ws)
+            e2e["fp64_batched"] = {"value": whole_job_rate(ws, n, ctx_steps, t_64), "unit": UNIT,
+                                   "ms_per_step": 1e3 * t_64 / ctx_steps,
+                                   "entry_point": "hepem_step_host (pinned host buffers)"}
 
     if rank != 0:
         return
