@@ -14,6 +14,7 @@
 #include "kernels.h"
 #include "rng.cuh"
 #include "state_image.h"
+#include "trace.h"
 
 namespace {
 
@@ -105,6 +106,7 @@ const char* hepem_status_string(int s) {
 const char* hepem_last_error(void) { return g_last_error.c_str(); }
 
 int hepem_create(const char* json, size_t len, hepem_ctx** out) {
+  hepem::TraceRange trace("hepem_create", (int64_t)len);
   if (!json || !out) return fail(HEPEM_BAD_ARG, "null argument");
   *out = nullptr;
   try {
@@ -116,6 +118,7 @@ int hepem_create(const char* json, size_t len, hepem_ctx** out) {
 }
 
 int hepem_create_from_file(const char* path, hepem_ctx** out) {
+  hepem::TraceRange trace("hepem_create_from_file", 0);
   if (!path || !out) return fail(HEPEM_BAD_ARG, "null argument");
   *out = nullptr;
   try {
@@ -127,6 +130,7 @@ int hepem_create_from_file(const char* path, hepem_ctx** out) {
 }
 
 int hepem_image_from_json(const char* json, size_t len, void* out, size_t capacity, size_t* size) {
+  hepem::TraceRange trace("hepem_image_from_json", (int64_t)len);
   if (!json || !size) return fail(HEPEM_BAD_ARG, "null argument");
   try {
     const std::vector<uint8_t> img = hepem::serialize_image(hepem::build_state_image(json, len));
@@ -141,6 +145,7 @@ int hepem_image_from_json(const char* json, size_t len, void* out, size_t capaci
 }
 
 int hepem_image_check(const void* image, size_t size, int64_t* arena_bytes) {
+  hepem::TraceRange trace("hepem_image_check", (int64_t)size);
   try {
     hepem::StateImage img = hepem::deserialize_image(image, size);
     if (arena_bytes) *arena_bytes = (int64_t)img.bytes.size();
@@ -151,6 +156,7 @@ int hepem_image_check(const void* image, size_t size, int64_t* arena_bytes) {
 }
 
 int hepem_create_from_image(const void* image, size_t size, hepem_ctx** out) {
+  hepem::TraceRange trace("hepem_create_from_image", (int64_t)size);
   if (!image || !out) return fail(HEPEM_BAD_ARG, "null argument");
   *out = nullptr;
   try {
@@ -240,6 +246,7 @@ int hepem_woodcock_gamma(const hepem_ctx* c, int64_t n, const hepem_track_state*
   for (int32_t k = 0; k < box->n_layers; ++k)
     if (!(zb[k] < zb[k + 1]) || li[k] < 0 || li[k] >= c->tables.nCouples)
       return fail(HEPEM_BAD_ARG, "layer bounds must increase and layer couples must exist");
+  hepem::TraceRange trace("hepem_woodcock_gamma", n);
   HEPEM_CUDA(hepem::launch_woodcock(c->tables, n, *in, *out, px, py, pz, *box, uniforms, nu, seed, *res, reached,
                                     (cudaStream_t)stream, c->sms));
   return HEPEM_OK;
@@ -253,6 +260,7 @@ int hepem_step(const hepem_ctx* c, int64_t n, const hepem_track_state* in, hepem
   if (!state_ok(in) || !state_ok(out) || !out_ok(res) || (nu > 0 && !uniforms))
     return fail(HEPEM_BAD_ARG, "null array in track batch");
   if (n > (int64_t)INT32_MAX * 2 / 3) return fail(HEPEM_BAD_ARG, "batch too large");
+  hepem::TraceRange trace("hepem_step", n);
   HEPEM_CUDA(hepem::launch_step(c->tables, n, *in, *out, uniforms, nu, seed, *res, counters, (cudaStream_t)stream,
                                 c->sms));
   return HEPEM_OK;
@@ -267,6 +275,7 @@ int step_batched(const hepem_ctx* c, int64_t n, const hepem_track_state* in, hep
   if (!state_ok(in) || !state_ok(out) || !out_ok(res) || (nu > 0 && !uniforms))
     return fail(HEPEM_BAD_ARG, "null array in track batch");
   if (n > (int64_t)INT32_MAX) return fail(HEPEM_BAD_ARG, "batch too large");
+  hepem::TraceRange trace(mixed ? "hepem_step_mixed" : "hepem_step_batched", n);
   cudaStream_t s = (cudaStream_t)stream;
   // an in-place precision-form step keeps a copy of the pre-step state of the
   // e+- tracks that reach an FP32 interaction (their FP64 fallback restarts there)
@@ -328,6 +337,7 @@ int hepem_step_subbatches(const hepem_ctx* c, int form, int32_t nb, const hepem_
   }
   const int64_t total = prefix[nb];
   if (total == 0) return HEPEM_OK;
+  hepem::TraceRange trace("hepem_step_subbatches", total);
   if (maxIdx > (int64_t)INT32_MAX) return fail(HEPEM_BAD_ARG, "batch too large");
   if (!state_ok(in) || !state_ok(out) || !out_ok(res) || (nu > 0 && !uniforms))
     return fail(HEPEM_BAD_ARG, "null array in track batch");
@@ -390,6 +400,7 @@ int step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem
   if (!state_ok(in) || !state_ok(out) || !out_ok(res) || (nu > 0 && !uniforms))
     return fail(HEPEM_BAD_ARG, "null array in track batch");
   if (n > (int64_t)INT32_MAX) return fail(HEPEM_BAD_ARG, "batch too large");
+  hepem::TraceRange trace(mixed ? "hepem_step_host_mixed" : "hepem_step_host", n);
   std::lock_guard<std::mutex> lock(c->mu);
   cudaStream_t s = (cudaStream_t)stream;
   // The batch is cut into chunks that cycle over kSlots streams, each with its
@@ -693,6 +704,7 @@ int hepem_howfar(const hepem_ctx* c, int form, int64_t n, const hepem_track_stat
                  void* stream) {
   const int rc = split_check(c, form, n, nu, tracks, nullptr, gstep, limits, uniforms, nullptr, false);
   if (rc != HEPEM_OK || n == 0) return rc;
+  hepem::TraceRange trace("hepem_howfar", n);
   return split_device(c, form, hepem::kPhaseHowFar, n, tracks, nullptr, gstep, limits, uniforms, nu, seed, nullptr,
                       counters, (cudaStream_t)stream);
 }
@@ -702,6 +714,7 @@ int hepem_perform(const hepem_ctx* c, int form, int64_t n, const hepem_track_sta
                   hepem_step_out* res, hepem_step_counters* counters, void* stream) {
   const int rc = split_check(c, form, n, nu, in, out, gstep, limits, uniforms, res, true);
   if (rc != HEPEM_OK || n == 0) return rc;
+  hepem::TraceRange trace("hepem_perform", n);
   return split_device(c, form, hepem::kPhasePerform, n, in, out, const_cast<double*>(gstep),
                       const_cast<void*>(limits), uniforms, nu, seed, res, counters, (cudaStream_t)stream);
 }
@@ -711,6 +724,7 @@ int hepem_howfar_host(const hepem_ctx* c, int form, int64_t n, const hepem_track
                       hepem_step_counters* counters, void* stream) {
   const int rc = split_check(c, form, n, nu, tracks, nullptr, gstep, limits, uniforms, nullptr, false);
   if (rc != HEPEM_OK || n == 0) return rc;
+  hepem::TraceRange trace("hepem_howfar_host", n);
   return split_host(c, form, hepem::kPhaseHowFar, n, tracks, nullptr, gstep, limits, uniforms, nu, seed, nullptr,
                     counters, (cudaStream_t)stream);
 }
@@ -721,6 +735,7 @@ int hepem_perform_host(const hepem_ctx* c, int form, int64_t n, const hepem_trac
                        void* stream) {
   const int rc = split_check(c, form, n, nu, in, out, gstep, limits, uniforms, res, true);
   if (rc != HEPEM_OK || n == 0) return rc;
+  hepem::TraceRange trace("hepem_perform_host", n);
   return split_host(c, form, hepem::kPhasePerform, n, in, out, const_cast<double*>(gstep),
                     const_cast<void*>(limits), uniforms, nu, seed, res, counters, (cudaStream_t)stream);
 }

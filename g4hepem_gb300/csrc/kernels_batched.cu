@@ -27,6 +27,7 @@
 #include "kernels.h"
 #include "physics_mixed.cuh"
 #include "step_io.cuh"
+#include "trace.h"
 
 // This file is compiled twice.  As itself (the FP64 unit, -fmad=false: the
 // FP64 path is bit-exact only without contraction) it holds the sort, the
@@ -1097,6 +1098,8 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
   const int64_t blocks = (n + 255) / 256;
   const int gC = (int)(blocks < (int64_t)sms * 8 ? blocks : (int64_t)sms * 8);
   w.active = o.active;
+  TraceStages trace(n);
+  trace.next("sort");
   mark();
   sort_hist_kernel<<<gC, 256, nkeys * sizeof(uint32_t), s>>>(T, n, o.active, in, out, res, w, ncb, neb, counters);
   sort_scan_kernel<<<1, 1024, 0, s>>>(w, ncb, neb);
@@ -1133,6 +1136,7 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
     // the split step: its stage A kernels (256 threads, occupancy grids)
     const int ph = o.phase - 1;
     for (int q = 0; q < 2; ++q) {
+      trace.next(stage_name(q + 1));
       if (o.mixed)
         stage(K.splitMixed[ph][q], sms * K.occSplitMixed[ph][q], 256);
       else
@@ -1140,13 +1144,17 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
       mark();
     }
     if (o.phase == kPhaseHowFar) {
-      if (o.mixed) stage(K.finalSplit[0], sms * K.occFinalSplit[0], 256);
+      if (o.mixed) {
+        trace.next("fp64_fallback");
+        stage(K.finalSplit[0], sms * K.occFinalSplit[0], 256);
+      }
       const cudaError_t e3 = cudaGetLastError();
       return le != cudaSuccess ? le : e3;
     }
   }
   for (int q = o.phase == kPhaseStep ? 0 : 2; q < kNumStageKernels; ++q) {
     const int b = bs_index(cfg.block[q]);
+    trace.next(stage_name(q + 1));
     StageFn const finalFn = o.phase == kPhasePerform ? K.finalSplit[1] : K.final_[1];
     const int finalOcc = o.phase == kPhasePerform ? K.occFinalSplit[1] : K.occFinal[1];
     if (o.mixed && K.mixed[b][q]) {
@@ -1154,7 +1162,10 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
       const int om = K.occMixed[b][q];
       const int pm = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < om ? cfg.ctasPerSM[q] : om;
       stage(K.mixed[b][q], sms * pm, kBlockSizes[b]);
-      if (q == kNumStageKernels - 1) stage(finalFn, sms * finalOcc, 256);
+      if (q == kNumStageKernels - 1) {
+        trace.next("fp64_fallback");
+        stage(finalFn, sms * finalOcc, 256);
+      }
       mark();
       continue;
     }
@@ -1162,6 +1173,7 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
       const int occ = K.occ[b][q];
       const int per = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < occ ? cfg.ctasPerSM[q] : occ;
       stage(K.fn[b][q], sms * per, kBlockSizes[b]);
+      trace.next("fp64_fallback");
       stage(finalFn, sms * finalOcc, 256);
       mark();
       continue;

@@ -32,6 +32,7 @@
 #include "ctx.h"
 #include "g4hepem_gb300.h"
 #include "kernels.h"
+#include "trace.h"
 
 namespace {
 
@@ -83,6 +84,7 @@ extern "C" int hepem_step_batched_noalloc(const hepem_ctx* c, int64_t n, const h
   void* ws = nullptr;
   const int rc = scratch_address(&ws);
   if (rc != HEPEM_OK) return rc;
+  hepem::TraceRange trace("hepem_step_batched_noalloc", n);
   hepem::BatchOpts o;
   o.cfg = &c->launch;
   hepem::apply_table_window(c, o);

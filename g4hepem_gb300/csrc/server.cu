@@ -36,6 +36,7 @@
 #include "ctx.h"
 #include "g4hepem_gb300.h"
 #include "kernels.h"
+#include "trace.h"
 
 namespace {
 
@@ -241,6 +242,10 @@ struct hepem_server {
   } while (0)
 
 cudaError_t hepem_server::iterate() {
+  // ranges: admission, the collection of the live tracks, the step, retirement
+  // (payload: the iteration's index)
+  hepem::TraceStages trace(iterations);
+  trace.next("server_admit");
   std::vector<Request*> admitted;
   {
     std::lock_guard<std::mutex> lock(mu);
@@ -282,6 +287,7 @@ cudaError_t hepem_server::iterate() {
     total += act[k]->n;
   }
   hOff[nr] = total;
+  trace.next("server_collect");
   SRV_CUDA(cudaMemcpyAsync(dSlot0, hSlot0, sizeof(int64_t) * nr, cudaMemcpyHostToDevice, stream));
   SRV_CUDA(cudaMemcpyAsync(dCnt, hCnt, sizeof(int64_t) * nr, cudaMemcpyHostToDevice, stream));
   SRV_CUDA(cudaMemcpyAsync(dOff, hOff, sizeof(int64_t) * (nr + 1), cudaMemcpyHostToDevice, stream));
@@ -294,6 +300,7 @@ cudaError_t hepem_server::iterate() {
   SRV_CUDA(cudaMemcpyAsync(hNActive, dNActive, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
   SRV_CUDA(cudaStreamSynchronize(stream));
   const int64_t nAct = *hNActive;
+  trace.next("server_step");
   if (nAct > 0) {
     hepem::BatchOpts o;
     o.active = active;
@@ -313,6 +320,7 @@ cudaError_t hepem_server::iterate() {
   }
   SRV_CUDA(cudaMemcpyAsync(hAlive, dAlive, sizeof(uint32_t) * nr, cudaMemcpyDeviceToHost, stream));
   SRV_CUDA(cudaStreamSynchronize(stream));
+  trace.next("server_retire");
   // retire: nothing alive before this step, or the step budget is used up
   std::vector<int64_t> fin;
   for (int64_t k = 0; k < nr; ++k) {

@@ -17,6 +17,7 @@
 #include "ctx.h"
 #include "g4hepem_gb300.h"
 #include "tables.h"
+#include "trace.h"
 
 namespace {
 
@@ -192,6 +193,7 @@ extern "C" int hepem_stack_secondaries(const hepem_ctx* c, int64_t n, const hepe
     const cudaError_t e = cudaMemsetAsync(n_out, 0, sizeof(int64_t), s);
     return e == cudaSuccess ? HEPEM_OK : hepem::set_error(HEPEM_CUDA_ERROR, cudaGetErrorString(e));
   }
+  hepem::TraceRange trace("hepem_stack_secondaries", n);
   StackArgs a;
   a.n = n;
   a.par = *parents;

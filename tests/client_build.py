@@ -37,3 +37,37 @@ def build_client() -> str:
     if r.returncode != 0:
         raise RuntimeError(f"client build failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     return OUT
+
+
+TRACE_SRC = os.path.join(REPO, "tests", "trace", "trace_recorder.c")
+TRACE_OUT = os.path.join(REPO, "tests", "trace", "_build", "trace_recorder.so")
+
+
+def build_trace_recorder() -> str:
+    """Compile tests/trace/trace_recorder.c, the NVTX injection library that
+    records the library's ranges (gcc and the NVTX headers of the toolkit)."""
+    if os.path.exists(TRACE_OUT) and os.path.getmtime(TRACE_SRC) <= os.path.getmtime(TRACE_OUT):
+        return TRACE_OUT
+    os.makedirs(os.path.dirname(TRACE_OUT), exist_ok=True)
+    cmd = ["gcc", "-std=c99", "-O2", "-Wall", "-Wextra", "-fPIC", "-shared", "-I",
+           os.path.join(cuda_home(), "include"), TRACE_SRC, "-o", TRACE_OUT]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"trace recorder build failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return TRACE_OUT
+
+
+def run_traced(code: str, log_path: str, timeout: float = 600) -> list:
+    """Run `code` in a fresh python process with the trace recorder injected;
+    returns the recorded lines split into fields."""
+    import sys
+    env = dict(os.environ)
+    env["NVTX_INJECTION64_PATH"] = build_trace_recorder()
+    env["HEPEM_TRACE_LOG"] = log_path
+    env["PYTHONPATH"] = os.pathsep.join([REPO, os.path.join(REPO, "tests"), env.get("PYTHONPATH", "")])
+    r = subprocess.run([sys.executable, "-c", code], env=env, cwd=REPO, capture_output=True, text=True,
+                       timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError(f"traced run failed:\n{r.stdout}\n{r.stderr}")
+    with open(log_path) as f:
+        return [line.split() for line in f if line.strip()]
