@@ -17,6 +17,14 @@
 // counted by its index in the request, and every per-request sum is reduced in
 // a fixed order, so a request's result is the same alone and in any mix.
 // Waits are bounded: hepem_server_wait gives up with HEPEM_TIMEOUT.
+//
+// Snapshot and resume: between two iterations (the loop holds iterMu for a
+// whole iteration) the unfinished requests -- their track state as of the
+// last completed step, their per-track sums and step counts -- are written to
+// a host buffer; another server (same tables) resumes them, and each then ends
+// with the result it would have had without the interruption, bit for bit:
+// the state carries each track's id, RNG cursor and Gauss cache, the sums are
+// per track, and the reductions have a fixed order.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -36,6 +44,7 @@
 #include "ctx.h"
 #include "g4hepem_gb300.h"
 #include "kernels.h"
+#include "state_image.h"
 #include "trace.h"
 
 namespace {
@@ -68,6 +77,7 @@ struct Request {
   std::atomic<bool> cancelled{false};
   double tSubmit = 0, tAdmit = 0, tDone = 0;
   std::vector<uint8_t> host;       // 20 state arrays back to back (input, then final state)
+  std::vector<uint8_t> sums;       // resumed request: per-track sums so far (edep, e_sec, n_sec, steps)
   hepem_request_result result{};
 };
 
@@ -157,6 +167,63 @@ __global__ void fill_seed_kernel(uint64_t* __restrict__ seeds, int64_t a, int64_
   }
 }
 
+// snapshot format (hepem_server_snapshot)
+const char kSnapMagic[8] = {'H', 'E', 'P', 'E', 'M', 'S', 'N', 'P'};
+constexpr uint32_t kSnapVersion = 1;
+constexpr size_t kSnapHeader = 32;    // magic, version, 0, requests, tracks
+constexpr size_t kSnapRecord = 32;    // id, n, seed, steps, admitted, cancelled, 0
+constexpr size_t kSnapSumBytes = 24;  // per track: edep, e_sec (f64), n_sec, steps (i32)
+
+struct SnapRec {
+  int64_t id, n;
+  uint64_t seed;
+  int32_t steps;
+  bool admitted, cancelled;
+  const uint8_t* state;  // 20 state arrays, then the sums
+};
+
+// Checks a snapshot (magic, version, sizes, checksum) and lists its requests.
+int parse_snapshot(const void* buf, size_t size, std::vector<SnapRec>& out) {
+  out.clear();
+  if (!buf) return hepem::set_error(HEPEM_BAD_ARG, "null snapshot");
+  const uint8_t* p = static_cast<const uint8_t*>(buf);
+  if (size < kSnapHeader + 8 || memcmp(p, kSnapMagic, 8) != 0)
+    return hepem::set_error(HEPEM_PARSE_ERROR, "not a server snapshot");
+  uint32_t ver[2];
+  uint64_t counts[2], stored;
+  memcpy(ver, p + 8, 8);
+  memcpy(counts, p + 16, 16);
+  if (ver[0] != kSnapVersion) return hepem::set_error(HEPEM_PARSE_ERROR, "snapshot: unknown version");
+  memcpy(&stored, p + size - 8, 8);
+  if (hepem::fnv1a(p, size - 8) != stored) return hepem::set_error(HEPEM_PARSE_ERROR, "snapshot: checksum mismatch");
+  size_t per = kSnapSumBytes;
+  for (size_t b : kStateSizes) per += b;
+  size_t off = kSnapHeader;
+  uint64_t tracks = 0;
+  for (uint64_t k = 0; k < counts[0]; ++k) {
+    if (off + kSnapRecord > size - 8) return hepem::set_error(HEPEM_PARSE_ERROR, "snapshot: truncated");
+    SnapRec r;
+    uint8_t flags[4];
+    memcpy(&r.id, p + off, 8);
+    memcpy(&r.n, p + off + 8, 8);
+    memcpy(&r.seed, p + off + 16, 8);
+    memcpy(&r.steps, p + off + 24, 4);
+    memcpy(flags, p + off + 28, 4);
+    r.admitted = flags[0] != 0;
+    r.cancelled = flags[1] != 0;
+    off += kSnapRecord;
+    if (r.n <= 0 || r.steps < 0 || flags[0] > 1 || flags[1] > 1 || (uint64_t)r.n > (size - 8 - off) / per)
+      return hepem::set_error(HEPEM_PARSE_ERROR, "snapshot: bad request record");
+    r.state = p + off;
+    off += per * (size_t)r.n;
+    tracks += (uint64_t)r.n;
+    out.push_back(r);
+  }
+  if (off != size - 8 || tracks != counts[1])
+    return hepem::set_error(HEPEM_PARSE_ERROR, "snapshot: sizes do not add up");
+  return HEPEM_OK;
+}
+
 }  // namespace
 
 struct hepem_server {
@@ -190,6 +257,9 @@ struct hepem_server {
   // requests
   std::mutex mu;
   std::condition_variable cv, cvDone;
+  std::mutex iterMu;                   // held by the loop for a whole iteration (snapshots wait for it)
+  int snapWaiters = 0;                 // snapshots waiting for iterMu (under mu): the loop lets them in first
+  std::condition_variable cvSnap;
   std::deque<int64_t> waiting;
   std::vector<int64_t> activeReq;
   std::unordered_map<int64_t, std::unique_ptr<Request>> reqs;
@@ -270,6 +340,15 @@ cudaError_t hepem_server::iterate() {
     fill_seed_kernel<<<std::max<int64_t>(1, std::min<int64_t>((r->n + 255) / 256, 1024)), 256, 0, stream>>>(
         seeds, r->slot0, r->n, r->seed, edepSum, eSecSum, nSecSum, stepSum);
     SRV_CUDA(cudaGetLastError());
+    if (!r->sums.empty()) {
+      // a resumed request: its per-track sums so far (pageable source: staged before the call returns)
+      const uint8_t* q = r->sums.data();
+      SRV_CUDA(cudaMemcpyAsync(edepSum + r->slot0, q, 8 * r->n, cudaMemcpyHostToDevice, stream));
+      SRV_CUDA(cudaMemcpyAsync(eSecSum + r->slot0, q + 8 * r->n, 8 * r->n, cudaMemcpyHostToDevice, stream));
+      SRV_CUDA(cudaMemcpyAsync(nSecSum + r->slot0, q + 16 * r->n, 4 * r->n, cudaMemcpyHostToDevice, stream));
+      SRV_CUDA(cudaMemcpyAsync(stepSum + r->slot0, q + 20 * r->n, 4 * r->n, cudaMemcpyHostToDevice, stream));
+      std::vector<uint8_t>().swap(r->sums);
+    }
   }
   std::vector<Request*> act;
   {
@@ -392,7 +471,16 @@ void hepem_server::run() {
       idle = waiting.empty() && activeReq.empty();
     }
     if (idle) continue;
-    const cudaError_t e = iterate();
+    {
+      // a waiting snapshot goes before the next iteration (the mutex alone is not fair)
+      std::unique_lock<std::mutex> lock(mu);
+      cvSnap.wait_for(lock, std::chrono::seconds(1), [&] { return snapWaiters == 0 || stop.load(); });
+    }
+    cudaError_t e;
+    {
+      std::lock_guard<std::mutex> g(iterMu);
+      e = iterate();
+    }
     if (e != cudaSuccess) {
       std::lock_guard<std::mutex> lock(mu);
       loopError = HEPEM_CUDA_ERROR;
@@ -619,6 +707,147 @@ int hepem_server_reset_stats(hepem_server* s) {
   s->iterations = 0;
   s->trackSteps = 0;
   s->completed = 0;
+  return HEPEM_OK;
+}
+
+// ---- snapshot / resume -----------------------------------------------------------------
+// Layout (host byte order):
+//   "HEPEMSNP" | u32 version | u32 0 | u64 requests | u64 tracks |
+//   per request, in id order: i64 id | i64 n | u64 seed | i32 steps |
+//     u8 admitted | u8 cancelled | u16 0 | the 20 state arrays (hepem_track_state
+//     order, n elements each) | f64 edep[n] | f64 e_sec[n] | i32 n_sec[n] | i32 steps[n] |
+//   u64 FNV-1a checksum of everything before it.
+int hepem_server_snapshot(hepem_server* s, void* buf, size_t capacity, size_t* size) {
+  if (!s || !size) return hepem::set_error(HEPEM_BAD_ARG, "null argument");
+  hepem::TraceRange trace("hepem_server_snapshot", 0);
+  {
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->snapWaiters += 1;
+  }
+  struct Leave {
+    hepem_server* s;
+    ~Leave() {
+      {
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->snapWaiters -= 1;
+      }
+      s->cvSnap.notify_all();
+    }
+  } leave{s};
+  std::lock_guard<std::mutex> iter(s->iterMu);
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (s->loopError != HEPEM_OK) return hepem::set_error(s->loopError, "server loop stopped: " + s->loopErrorMsg);
+  std::vector<Request*> list;
+  for (auto& kv : s->reqs)
+    if (!kv.second->done) list.push_back(kv.second.get());
+  std::sort(list.begin(), list.end(), [](const Request* a, const Request* b) { return a->id < b->id; });
+  size_t per = 0;
+  for (size_t b : kStateSizes) per += b;
+  per += kSnapSumBytes;
+  size_t need = kSnapHeader + 8;
+  int64_t tracks = 0;
+  for (const Request* r : list) {
+    need += kSnapRecord + per * (size_t)r->n;
+    tracks += r->n;
+  }
+  *size = need;
+  if (!buf) return HEPEM_OK;
+  if (capacity < need) return hepem::set_error(HEPEM_BAD_ARG, "snapshot buffer too small");
+  uint8_t* p = static_cast<uint8_t*>(buf);
+  memcpy(p, kSnapMagic, 8);
+  const uint32_t ver[2] = {kSnapVersion, 0};
+  memcpy(p + 8, ver, 8);
+  const uint64_t counts[2] = {(uint64_t)list.size(), (uint64_t)tracks};
+  memcpy(p + 16, counts, 16);
+  p += kSnapHeader;
+  for (const Request* r : list) {
+    const int64_t n = r->n;
+    const int32_t steps = r->steps;
+    const uint8_t flags[4] = {(uint8_t)(r->slot0 >= 0), (uint8_t)r->cancelled.load(), 0, 0};
+    memcpy(p, &r->id, 8);
+    memcpy(p + 8, &n, 8);
+    memcpy(p + 16, &r->seed, 8);
+    memcpy(p + 24, &steps, 4);
+    memcpy(p + 28, flags, 4);
+    p += kSnapRecord;
+    if (r->slot0 >= 0) {
+      // resident: the state and sums as of the last completed iteration
+      for (int k = 0; k < 20; ++k) {
+        const cudaError_t e = cudaMemcpyAsync(p, s->state_ptr(k, r->slot0), kStateSizes[k] * n,
+                                              cudaMemcpyDeviceToHost, s->stream);
+        if (e != cudaSuccess) return hepem::set_error(HEPEM_CUDA_ERROR, cudaGetErrorString(e));
+        p += kStateSizes[k] * n;
+      }
+      const void* src[4] = {s->edepSum + r->slot0, s->eSecSum + r->slot0, s->nSecSum + r->slot0,
+                            s->stepSum + r->slot0};
+      const size_t sz[4] = {8, 8, 4, 4};
+      for (int k = 0; k < 4; ++k) {
+        const cudaError_t e = cudaMemcpyAsync(p, src[k], sz[k] * n, cudaMemcpyDeviceToHost, s->stream);
+        if (e != cudaSuccess) return hepem::set_error(HEPEM_CUDA_ERROR, cudaGetErrorString(e));
+        p += sz[k] * n;
+      }
+    } else {
+      memcpy(p, r->host.data(), r->host.size());
+      p += r->host.size();
+      memset(p, 0, kSnapSumBytes * n);
+      p += kSnapSumBytes * n;
+    }
+  }
+  const cudaError_t e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) return hepem::set_error(HEPEM_CUDA_ERROR, cudaGetErrorString(e));
+  const uint64_t sum = hepem::fnv1a(static_cast<const uint8_t*>(buf), need - 8);
+  memcpy(p, &sum, 8);
+  return HEPEM_OK;
+}
+
+int hepem_server_snapshot_check(const void* buf, size_t size, int64_t* n_requests, int64_t* n_tracks) {
+  std::vector<SnapRec> recs;
+  const int rc = parse_snapshot(buf, size, recs);
+  if (rc != HEPEM_OK) return rc;
+  int64_t t = 0;
+  for (const SnapRec& r : recs) t += r.n;
+  if (n_requests) *n_requests = (int64_t)recs.size();
+  if (n_tracks) *n_tracks = t;
+  return HEPEM_OK;
+}
+
+int hepem_server_resume(hepem_server* s, const void* buf, size_t size, int64_t max_ids, int64_t* old_ids,
+                        int64_t* new_ids, int64_t* n_requests) {
+  if (!s || !n_requests) return hepem::set_error(HEPEM_BAD_ARG, "null argument");
+  hepem::TraceRange trace("hepem_server_resume", (int64_t)size);
+  std::vector<SnapRec> recs;
+  const int rc = parse_snapshot(buf, size, recs);
+  if (rc != HEPEM_OK) return rc;
+  *n_requests = (int64_t)recs.size();
+  if ((int64_t)recs.size() > max_ids || (!recs.empty() && (!old_ids || !new_ids)))
+    return hepem::set_error(HEPEM_BAD_ARG, "id arrays smaller than the snapshot's request count");
+  for (const SnapRec& r : recs)
+    if (r.n > s->capacity)
+      return hepem::set_error(HEPEM_OOM_ADMISSION, "snapshot request larger than the server's memory budget");
+  std::vector<std::unique_ptr<Request>> made;
+  size_t per = 0;
+  for (size_t b : kStateSizes) per += b;
+  for (const SnapRec& q : recs) {
+    std::unique_ptr<Request> r(new Request());
+    r->n = q.n;
+    r->seed = q.seed;
+    r->steps = q.steps;
+    r->cancelled = q.cancelled;
+    r->host.assign(q.state, q.state + per * (size_t)q.n);
+    if (q.admitted) r->sums.assign(q.state + per * (size_t)q.n, q.state + (per + kSnapSumBytes) * (size_t)q.n);
+    r->tSubmit = now_s();
+    made.push_back(std::move(r));
+  }
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (s->loopError != HEPEM_OK) return hepem::set_error(s->loopError, "server loop stopped: " + s->loopErrorMsg);
+  for (size_t k = 0; k < made.size(); ++k) {
+    made[k]->id = s->nextId++;
+    old_ids[k] = recs[k].id;
+    new_ids[k] = made[k]->id;
+    s->waiting.push_back(made[k]->id);
+    s->reqs[made[k]->id] = std::move(made[k]);
+  }
+  s->cv.notify_all();
   return HEPEM_OK;
 }
 

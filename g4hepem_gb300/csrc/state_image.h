@@ -25,5 +25,7 @@ std::vector<uint8_t> serialize_image(const StateImage& img);
 StateImage deserialize_image(const void* data, size_t size);
 // Resolve the pointer fields against the arena base address `base`.
 void relocate(StateImage& img, DevTables& out, const void* base);
+// 64-bit FNV-1a hash (the checksum of the table image and of server snapshots).
+uint64_t fnv1a(const uint8_t* p, size_t n);
 
 }  // namespace hepem

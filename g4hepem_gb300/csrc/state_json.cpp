@@ -568,10 +568,6 @@ StateImage build_state_image_file(const char* path) {
 //   u64 FNV-1a checksum of everything before it.
 // Loading it skips parsing and validation of the JSON document: the arena was
 // validated when the image was made, and the image carries a checksum.
-namespace {
-const char kImgMagic[8] = {'H', 'E', 'P', 'E', 'M', 'I', 'M', 'G'};
-constexpr uint32_t kImgVersion = 1;
-
 uint64_t fnv1a(const uint8_t* p, size_t n) {
   uint64_t h = 1469598103934665603ull;
   for (size_t i = 0; i < n; ++i) {
@@ -580,6 +576,10 @@ uint64_t fnv1a(const uint8_t* p, size_t n) {
   }
   return h;
 }
+
+namespace {
+const char kImgMagic[8] = {'H', 'E', 'P', 'E', 'M', 'I', 'M', 'G'};
+constexpr uint32_t kImgVersion = 1;
 
 template <class T>
 void put_pod(std::vector<uint8_t>& out, const T& v) {

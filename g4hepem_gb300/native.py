@@ -99,7 +99,8 @@ EXPORTED = ["hepem_create", "hepem_create_from_file", "hepem_image_from_json", "
             "hepem_server_destroy", "hepem_sample_model", "hepem_stack_secondaries", "hepem_woodcock_gamma", "hepem_get_launch_config", "hepem_set_launch_config", "hepem_autotune",
             "hepem_set_table_l2_window", "hepem_step_limit_bytes", "hepem_howfar", "hepem_perform",
             "hepem_howfar_host", "hepem_perform_host", "hepem_electron_xs_stepping", "hepem_brem_select_target",
-            "hepem_conv_select_target", "hepem_gamma_xs", "hepem_step_subbatches"]
+            "hepem_conv_select_target", "hepem_gamma_xs", "hepem_step_subbatches", "hepem_server_snapshot",
+            "hepem_server_snapshot_check", "hepem_server_resume"]
 FORMS = {"plain": 0, "batched": 1, "mixed": 2}
 STATUS_CANCELLED, STATUS_TIMEOUT, STATUS_OOM_ADMISSION = 8, 5, 6
 
@@ -182,6 +183,11 @@ def lib():
         L.hepem_server_get_stats.argtypes = [_vp, C.POINTER(ServerStats)]
         L.hepem_server_reset_stats.argtypes = [_vp]
         L.hepem_server_destroy.argtypes = [_vp]
+        L.hepem_server_snapshot.argtypes = [_vp, _vp, C.c_size_t, C.POINTER(C.c_size_t)]
+        L.hepem_server_snapshot_check.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(C.c_int64),
+                                                  C.POINTER(C.c_int64)]
+        L.hepem_server_resume.argtypes = [_vp, C.c_char_p, C.c_size_t, C.c_int64, C.POINTER(C.c_int64),
+                                          C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         _LIB = L
     return _LIB
 
@@ -525,6 +531,35 @@ class Server:
     def cancel(self, rid: int):
         check(lib().hepem_server_cancel(self.h, rid))
 
+    def snapshot(self) -> bytes:
+        """hepem_server_snapshot: the unfinished requests as of the last
+        completed iteration (they keep running here)."""
+        L = lib()
+        while True:
+            size = C.c_size_t()
+            check(L.hepem_server_snapshot(self.h, None, 0, C.byref(size)))
+            buf = C.create_string_buffer(size.value)
+            got = C.c_size_t()
+            rc = L.hepem_server_snapshot(self.h, buf, size.value, C.byref(got))
+            if rc == 0:
+                return buf.raw[:got.value]
+            if got.value <= size.value:   # not a size change between the two calls
+                check(rc)
+
+    def resume(self, snap: bytes) -> dict:
+        """hepem_server_resume: submits the snapshot's requests; returns
+        {snapshot request id: request id on this server}."""
+        n = snapshot_check(snap)[0]
+        old = (C.c_int64 * max(n, 1))()
+        new = (C.c_int64 * max(n, 1))()
+        got = C.c_int64()
+        check(lib().hepem_server_resume(self.h, snap, len(snap), n, old, new, C.byref(got)))
+        ids = {}
+        for k, rec in enumerate(snapshot_records(snap)):
+            ids[old[k]] = new[k]
+            self._keep[new[k]] = rec["n"]
+        return ids
+
     def stats(self) -> dict:
         s = ServerStats()
         check(lib().hepem_server_get_stats(self.h, C.byref(s)))
@@ -543,6 +578,41 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def snapshot_check(snap: bytes):
+    """Validates a server snapshot (no GPU needed); returns (requests, tracks)."""
+    nr, nt = C.c_int64(), C.c_int64()
+    check(lib().hepem_server_snapshot_check(snap, len(snap), C.byref(nr), C.byref(nt)))
+    return nr.value, nt.value
+
+
+def snapshot_records(snap: bytes) -> list:
+    """The request records of a validated snapshot: id, n, seed, steps,
+    admitted, cancelled, and the track state (numpy arrays of STATE_FIELDS)."""
+    snapshot_check(snap)
+    nreq = int(np.frombuffer(snap, dtype=np.uint64, count=1, offset=16)[0])
+    off, out = 32, []
+    for _ in range(nreq):
+        rid, n = (int(x) for x in np.frombuffer(snap, dtype=np.int64, count=2, offset=off))
+        seed = int(np.frombuffer(snap, dtype=np.uint64, count=1, offset=off + 16)[0])
+        steps = int(np.frombuffer(snap, dtype=np.int32, count=1, offset=off + 24)[0])
+        admitted, cancelled = snap[off + 28], snap[off + 29]
+        off += 32
+        state = {}
+        for f, dt in STATE_FIELDS:
+            a = np.frombuffer(snap, dtype=dt, count=n, offset=off)
+            state[f] = a.copy()
+            off += a.nbytes
+        sums = {}
+        for f, dt in (("edep", np.float64), ("e_secondaries", np.float64), ("n_secondaries", np.int32),
+                      ("track_steps", np.int32)):
+            a = np.frombuffer(snap, dtype=dt, count=n, offset=off)
+            sums[f] = a.copy()
+            off += a.nbytes
+        out.append(dict(id=rid, n=n, seed=seed, steps=steps, admitted=bool(admitted), cancelled=bool(cancelled),
+                        state=state, sums=sums))
+    return out
 
 
 def image_from_json(json_text) -> bytes:

@@ -546,6 +546,25 @@ int  hepem_server_wait(hepem_server* s, int64_t request_id, double timeout_s,
 int  hepem_server_cancel(hepem_server* s, int64_t request_id);
 int  hepem_server_get_stats(hepem_server* s, hepem_server_stats* out);
 int  hepem_server_reset_stats(hepem_server* s);
+/* Snapshot of the unfinished requests (waiting or resident), taken between
+ * two iterations: each request's track state as of its last completed step,
+ * its per-track sums (deposit, secondary energy and count, steps) and its
+ * step count, with a checksum.  buf == NULL: *size = the bytes needed.  The
+ * requests keep running on this server.  Reference counterpart: none (the
+ * reference saves only the Geant4 RNG status, apps/examples/TestEm3/src/
+ * RunAction.cc:103); the state is plain SoA plus RNG cursors, so a snapshot
+ * is a copy. */
+int  hepem_server_snapshot(hepem_server* s, void* buf, size_t capacity, size_t* size);
+/* Validates a snapshot without a GPU; counts its requests and tracks. */
+int  hepem_server_snapshot_check(const void* buf, size_t size, int64_t* n_requests,
+                                 int64_t* n_tracks);
+/* Submits the requests of a snapshot to server s (built on the same tables):
+ * each resumes where it stopped and ends with the result it would have had
+ * without the interruption.  old_ids[k] / new_ids[k] (arrays of max_ids) map
+ * the snapshot's request ids to this server's; *n_requests = the count
+ * (HEPEM_BAD_ARG, nothing submitted, if it is above max_ids). */
+int  hepem_server_resume(hepem_server* s, const void* buf, size_t size, int64_t max_ids,
+                         int64_t* old_ids, int64_t* new_ids, int64_t* n_requests);
 /* Stops the thread after the current iteration and frees the pool. */
 int  hepem_server_destroy(hepem_server* s);
 

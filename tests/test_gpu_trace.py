@@ -65,7 +65,8 @@ def test_step_ranges(tmp_path):
     assert [k[0] for k in nodes["hepem_step_batched"]] == STAGES
     assert [k[0] for k in nodes["hepem_step_mixed"]] == STAGES + ["fp64_fallback"]
     assert [k[0] for k in nodes["hepem_howfar"]] == STAGES[:3] + ["fp64_fallback"]
-    assert [k[0] for k in nodes["hepem_perform"]] == STAGES[:1] + STAGES[3:] + ["fp64_fallback"]
+    # Perform: the sort, its own stage A kernels (the Perform phase), the queues
+    assert [k[0] for k in nodes["hepem_perform"]] == STAGES + ["fp64_fallback"]
     assert all(k[1] == 4096 for k in nodes["hepem_step_mixed"])
     # the host-buffer step: one batched step (a chunk of 4096 tracks) inside
     assert [k[0] for k in nodes["hepem_step_host_mixed"]] == STAGES + ["fp64_fallback"]
