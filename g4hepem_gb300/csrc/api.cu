@@ -58,6 +58,13 @@ int create_from_image(hepem::StateImage& img, hepem_ctx** out) {
   }
   c->arenaBytes = img.bytes.size();
   hepem::relocate(img, c->tables, c->arena);
+  // side streams of the batched steps; without them a step runs on one stream
+  bool sideOk = true;
+  for (cudaStream_t& st : c->side.st)
+    sideOk = sideOk && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
+  for (cudaEvent_t& ev : c->side.ev)
+    sideOk = sideOk && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
+  c->sideReady = sideOk;
   if (kTableWindowByDefault) hepem::set_table_window(c, 1);
   *out = c;
   return HEPEM_OK;
@@ -171,13 +178,24 @@ int hepem_destroy(hepem_ctx* c) {
   if (!c) return HEPEM_OK;
   cudaError_t e = cudaSuccess;
   if (c->arena) e = cudaFree(c->arena);
-  for (auto& sl : c->slot) {
-    if (sl.s) cudaStreamSynchronize(sl.s);
-    if (sl.buf) cudaFree(sl.buf);
-    if (sl.done) cudaEventDestroy(sl.done);
-    if (sl.s) cudaStreamDestroy(sl.s);
+  for (cudaStream_t ps : c->pipe)
+    if (ps) cudaStreamSynchronize(ps);
+  for (cudaStream_t st : c->side.st)
+    if (st) {
+      cudaStreamSynchronize(st);
+      cudaStreamDestroy(st);
+    }
+  for (cudaEvent_t ev : c->side.ev)
+    if (ev) cudaEventDestroy(ev);
+  if (c->pipeBuf) cudaFree(c->pipeBuf);
+  for (int k = 0; k < hepem_ctx::kMaxChunks; ++k) {
+    if (c->chunkIn[k]) cudaEventDestroy(c->chunkIn[k]);
+    if (c->chunkStepped[k]) cudaEventDestroy(c->chunkStepped[k]);
   }
+  for (cudaStream_t ps : c->pipe)
+    if (ps) cudaStreamDestroy(ps);
   if (c->start) cudaEventDestroy(c->start);
+  if (c->finished) cudaEventDestroy(c->finished);
   if (c->splitBuf) cudaFree(c->splitBuf);
   if (c->stageEvReady)
     for (auto& e2 : c->stageEv) cudaEventDestroy(e2);
@@ -384,12 +402,6 @@ int hepem_step_subbatches(const hepem_ctx* c, int form, int32_t nb, const hepem_
   return HEPEM_OK;
 }
 
-// chunks of a host-buffer step: more overlap of the copies against smaller,
-// less efficient device steps
-#ifndef HEPEM_HOST_CHUNKS
-#define HEPEM_HOST_CHUNKS 8
-#endif
-
 namespace {
 int step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem_track_state* out,
               const double* uniforms, int32_t nu, uint64_t seed, hepem_step_out* res, hepem_step_counters* counters,
@@ -403,76 +415,77 @@ int step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem
   hepem::TraceRange trace(mixed ? "hepem_step_host_mixed" : "hepem_step_host", n);
   std::lock_guard<std::mutex> lock(c->mu);
   cudaStream_t s = (cudaStream_t)stream;
-  // The batch is cut into chunks that cycle over kSlots streams, each with its
-  // own device buffers: the copy-in of one chunk, the step of the previous one
-  // and the copy-out of the one before overlap.
-  const int64_t m = std::min<int64_t>(
-      n, std::max<int64_t>(1 << 16, ((n + HEPEM_HOST_CHUNKS - 1) / HEPEM_HOST_CHUNKS + 255) / 256 * 256));
+  // The batch is cut into up to kMaxChunks chunks, each with a device buffer
+  // of its own, and the work goes to three streams: the copies in (one chunk
+  // after the other, as fast as the link takes them), the steps (each chunk
+  // once its copy is in, alone on the GPU) and the copies out (each chunk
+  // once stepped).  The link towards the host is the slowest of the three:
+  // it stays busy from the end of the first chunk's step to the end.
+  const int kc = hepem_ctx::kMaxChunks;
+  const int64_t m = std::min<int64_t>(n, std::max<int64_t>(1 << 16, ((n + kc - 1) / kc + 255) / 256 * 256));
   const int nChunks = (int)((n + m - 1) / m);
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
   size_t need = 0;
   for (size_t b : kStateSizes) need += al(b * m);
   for (size_t b : kOutSizes) need += al(b * m);
-  need += al(sizeof(double) * (size_t)m * nu) + al(sizeof(hepem_step_counters)) + al(hepem::batched_workspace_bytes(m));
+  need += al(sizeof(double) * (size_t)m * nu) + al(hepem::batched_workspace_bytes(m));
   // the precision form steps the chunk in place: room for its pre-step copy
   if (mixed) need += al(hepem::mixed_pre_state_bytes(m));
-  if (!c->slotsReady) {
-    for (int k = 0; k < hepem_ctx::kSlots; ++k) {
-      HEPEM_CUDA(cudaStreamCreateWithFlags(&c->slot[k].s, cudaStreamNonBlocking));
-      HEPEM_CUDA(cudaEventCreateWithFlags(&c->slot[k].done, cudaEventDisableTiming));
+  const size_t total = need * (size_t)nChunks + al(sizeof(hepem_step_counters));
+  if (!c->pipeReady) {
+    for (cudaStream_t& ps : c->pipe) HEPEM_CUDA(cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking));
+    for (int k = 0; k < kc; ++k) {
+      HEPEM_CUDA(cudaEventCreateWithFlags(&c->chunkIn[k], cudaEventDisableTiming));
+      HEPEM_CUDA(cudaEventCreateWithFlags(&c->chunkStepped[k], cudaEventDisableTiming));
     }
     HEPEM_CUDA(cudaEventCreateWithFlags(&c->start, cudaEventDisableTiming));
-    c->slotsReady = true;
+    HEPEM_CUDA(cudaEventCreateWithFlags(&c->finished, cudaEventDisableTiming));
+    c->pipeReady = true;
   }
+  if (total > c->pipeBytes) {
+    for (cudaStream_t ps : c->pipe) HEPEM_CUDA(cudaStreamSynchronize(ps));
+    if (c->pipeBuf) HEPEM_CUDA(cudaFree(c->pipeBuf));
+    c->pipeBuf = nullptr;
+    c->pipeBytes = 0;
+    HEPEM_CUDA(cudaMalloc(&c->pipeBuf, total));
+    c->pipeBytes = total;
+  }
+  const cudaStream_t sIn = c->pipe[0], sStep = c->pipe[1], sOut = c->pipe[2];
   HEPEM_CUDA(cudaEventRecord(c->start, s));
-  for (int k = 0; k < hepem_ctx::kSlots; ++k) {
-    hepem_ctx::Slot& sl = c->slot[k];
-    if (need > sl.bytes) {
-      HEPEM_CUDA(cudaStreamSynchronize(sl.s));
-      if (sl.buf) HEPEM_CUDA(cudaFree(sl.buf));
-      sl.buf = nullptr;
-      sl.bytes = 0;
-      HEPEM_CUDA(cudaMalloc(&sl.buf, need));
-      sl.bytes = need;
-    }
-    HEPEM_CUDA(cudaStreamWaitEvent(sl.s, c->start, 0));
-  }
+  for (cudaStream_t ps : c->pipe) HEPEM_CUDA(cudaStreamWaitEvent(ps, c->start, 0));
+  hepem_step_counters* cnt =
+      reinterpret_cast<hepem_step_counters*>(static_cast<uint8_t*>(c->pipeBuf) + need * (size_t)nChunks);
+  if (counters) HEPEM_CUDA(cudaMemsetAsync(cnt, 0, sizeof(*cnt), sStep));
   void* const* hin = reinterpret_cast<void* const*>(in);
   void* const* hout = reinterpret_cast<void* const*>(out);
   void* const* hres = reinterpret_cast<void* const*>(res);
   static_assert(sizeof(hepem_track_state) == 20 * sizeof(void*), "state struct layout");
   static_assert(sizeof(hepem_step_out) == 14 * sizeof(void*), "out struct layout");
-  hepem_step_counters* dcnt[hepem_ctx::kSlots] = {};
   for (int ch = 0; ch < nChunks; ++ch) {
     const int64_t off = (int64_t)ch * m;
     const int64_t mc = std::min<int64_t>(m, n - off);
-    hepem_ctx::Slot& sl = c->slot[ch % hepem_ctx::kSlots];
-    const cudaStream_t ss = sl.s;
-    uint8_t* p = (uint8_t*)sl.buf;
+    uint8_t* p = static_cast<uint8_t*>(c->pipeBuf) + need * (size_t)ch;
     void* dstate[20];
     void* dout[14];
     for (int k = 0; k < 20; ++k) { dstate[k] = p; p += al(kStateSizes[k] * m); }
     for (int k = 0; k < 14; ++k) { dout[k] = p; p += al(kOutSizes[k] * m); }
     double* du = (double*)p;
     p += al(sizeof(double) * (size_t)m * nu);
-    hepem_step_counters* cnt = (hepem_step_counters*)p;
-    p += al(sizeof(hepem_step_counters));
     void* dwork = p;
     p += al(hepem::batched_workspace_bytes(m));
     void* dpre = p;
-    if (counters && ch < hepem_ctx::kSlots) {
-      HEPEM_CUDA(cudaMemsetAsync(cnt, 0, sizeof(*cnt), ss));
-      dcnt[ch] = cnt;
-    }
     hepem_track_state ds;
     hepem_step_out dr;
     memcpy(&ds, dstate, sizeof(ds));
     memcpy(&dr, dout, sizeof(dr));
     for (int k = 0; k < 20; ++k)
       HEPEM_CUDA(cudaMemcpyAsync(dstate[k], (const uint8_t*)hin[k] + kStateSizes[k] * off, kStateSizes[k] * mc,
-                                 cudaMemcpyHostToDevice, ss));
+                                 cudaMemcpyHostToDevice, sIn));
     if (nu > 0)
-      HEPEM_CUDA(cudaMemcpyAsync(du, uniforms + off * nu, sizeof(double) * (size_t)mc * nu, cudaMemcpyHostToDevice, ss));
+      HEPEM_CUDA(cudaMemcpyAsync(du, uniforms + off * nu, sizeof(double) * (size_t)mc * nu, cudaMemcpyHostToDevice,
+                                 sIn));
+    HEPEM_CUDA(cudaEventRecord(c->chunkIn[ch], sIn));
+    HEPEM_CUDA(cudaStreamWaitEvent(sStep, c->chunkIn[ch], 0));
     hepem::BatchOpts o;
     o.cfg = &c->launch;
     o.mixed = mixed;
@@ -483,36 +496,29 @@ int step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem
       o.preState = &pre;
     }
     HEPEM_CUDA(hepem::launch_step_batched(c->tables, mc, ds, ds, du, nu, seed, dr, counters ? cnt : nullptr, dwork,
-                                          ss, c->sms, o));
+                                          sStep, c->sms, o));
+    HEPEM_CUDA(cudaEventRecord(c->chunkStepped[ch], sStep));
+    HEPEM_CUDA(cudaStreamWaitEvent(sOut, c->chunkStepped[ch], 0));
     // persistent per-track fields come back (type/imc/id/safety/boundary are inputs only)
     for (int k = 3; k < 20; ++k) {
       if (k == 11 || k == 12) continue;
       HEPEM_CUDA(cudaMemcpyAsync((uint8_t*)hout[k] + kStateSizes[k] * off, dstate[k], kStateSizes[k] * mc,
-                                 cudaMemcpyDeviceToHost, ss));
+                                 cudaMemcpyDeviceToHost, sOut));
     }
     for (int k = 0; k < 14; ++k)
       HEPEM_CUDA(cudaMemcpyAsync((uint8_t*)hres[k] + kOutSizes[k] * off, dout[k], kOutSizes[k] * mc,
-                                 cudaMemcpyDeviceToHost, ss));
+                                 cudaMemcpyDeviceToHost, sOut));
   }
   if (hout[0] != hin[0]) {
     for (int k : {0, 1, 2, 11, 12}) memcpy(hout[k], hin[k], kStateSizes[k] * n);
   }
-  hepem_step_counters hc[hepem_ctx::kSlots];
-  for (int k = 0; k < hepem_ctx::kSlots; ++k) {
-    if (dcnt[k]) HEPEM_CUDA(cudaMemcpyAsync(&hc[k], dcnt[k], sizeof(hc[k]), cudaMemcpyDeviceToHost, c->slot[k].s));
-    HEPEM_CUDA(cudaEventRecord(c->slot[k].done, c->slot[k].s));
-    HEPEM_CUDA(cudaStreamWaitEvent(s, c->slot[k].done, 0));
-  }
+  // every chunk's step precedes the last chunk's copies out on sOut
+  hepem_step_counters hc;
+  if (counters) HEPEM_CUDA(cudaMemcpyAsync(&hc, cnt, sizeof(hc), cudaMemcpyDeviceToHost, sOut));
+  HEPEM_CUDA(cudaEventRecord(c->finished, sOut));
+  HEPEM_CUDA(cudaStreamWaitEvent(s, c->finished, 0));
   HEPEM_CUDA(cudaStreamSynchronize(s));
-  if (counters) {
-    memset(counters, 0, sizeof(*counters));
-    for (int k = 0; k < hepem_ctx::kSlots; ++k) {
-      if (!dcnt[k]) continue;
-      const uint64_t* a = reinterpret_cast<const uint64_t*>(&hc[k]);
-      uint64_t* b = reinterpret_cast<uint64_t*>(counters);
-      for (size_t j = 0; j < sizeof(hepem_step_counters) / 8; ++j) b[j] += a[j];
-    }
-  }
+  if (counters) *counters = hc;
   return HEPEM_OK;
 }
 }  // namespace

@@ -22,22 +22,24 @@ struct hepem_ctx {
   float tableHitRatio = 0.0f;
   // launch configuration of the batched form (hepem_set_launch_config / hepem_autotune)
   hepem::LaunchCfg launch = hepem::default_launch_cfg();
-  // copy/compute pipeline of hepem_step_host (grow-only buffers, serialised by mu)
-  static constexpr int kSlots = 3;
-  struct Slot {
-    cudaStream_t s = nullptr;
-    cudaEvent_t done = nullptr;
-    void* buf = nullptr;
-    size_t bytes = 0;
-  };
+  // copy/compute pipeline of hepem_step_host: one stream for the copies in,
+  // one for the steps, one for the copies out, and a device buffer per chunk
+  // (grow-only, serialised by mu)
+  static constexpr int kMaxChunks = 8;
   std::mutex mu;
-  Slot slot[kSlots];
-  cudaEvent_t start = nullptr;
-  bool slotsReady = false;
+  cudaStream_t pipe[3] = {};  // copies in, steps, copies out
+  cudaEvent_t chunkIn[kMaxChunks] = {}, chunkStepped[kMaxChunks] = {};
+  cudaEvent_t start = nullptr, finished = nullptr;
+  void* pipeBuf = nullptr;
+  size_t pipeBytes = 0;
+  bool pipeReady = false;
   // device buffer of the host-buffer split step (hepem_howfar_host /
   // hepem_perform_host; grow-only, serialised by mu)
   void* splitBuf = nullptr;
   size_t splitBytes = 0;
+  // side streams of the batched steps (created with the context)
+  hepem::SideStreams side;
+  bool sideReady = false;
   // per-stage timing of the batched form (hepem_profile_stages)
   bool profile = false;
   bool stageEvReady = false;
@@ -54,6 +56,7 @@ inline void apply_table_window(const hepem_ctx* c, BatchOpts& o) {
   o.tableBase = c->arena;
   o.tableBytes = c->tableWindow;
   o.tableHitRatio = c->tableHitRatio;
+  o.side = c->sideReady ? const_cast<SideStreams*>(&c->side) : nullptr;
 }
 // set (enable != 0) or clear the window; see hepem_set_table_l2_window
 int set_table_window(hepem_ctx* c, int enable);

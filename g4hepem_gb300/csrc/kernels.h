@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "g4hepem_gb300.h"
 #include "tables.h"
@@ -103,6 +104,15 @@ struct LaunchCfg {
 LaunchCfg default_launch_cfg();
 bool valid_launch_cfg(const LaunchCfg& c);
 int stage_occupancy(int kernel, int block);
+// side streams of a context and the events that fork and join them (the
+// batched step overlaps independent stage kernels on them); mu serialises
+// the enqueue of one step's forks and joins against another thread's
+constexpr int kSideStreams = 3;
+struct SideStreams {
+  cudaStream_t st[kSideStreams] = {};
+  cudaEvent_t ev[kSideStreams + 2] = {};
+  std::mutex mu;
+};
 // optional inputs of a batched step
 struct BatchOpts {
   cudaEvent_t* ev = nullptr;         // stage timing: kNumStageEvents events
@@ -126,6 +136,8 @@ struct BatchOpts {
   int phase = kPhaseStep;
   double* gstep = nullptr;
   Limits limits = {};
+  // side streams for independent stages (null, or with stage timing: one stream)
+  SideStreams* side = nullptr;
 };
 // the index list and per-track RNG keys of a sub-batch step: active[p] =
 // offset_b + (p - prefix[b]) and keys[that index] = seed_b for the

@@ -1110,9 +1110,9 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
   // the stage kernels: with a table window, launched with it as a launch
   // attribute (the caller's stream is left as it is)
   cudaError_t le = cudaSuccess;
-  auto stage = [&](StageFn f, int grid, int block) {
+  auto stage = [&](StageFn f, int grid, int block, cudaStream_t st) {
     if (o.tableBytes == 0) {
-      f<<<grid, block, 0, s>>>(T, in, out, uniforms, nu, seed, res, w, counters);
+      f<<<grid, block, 0, st>>>(T, in, out, uniforms, nu, seed, res, w, counters);
       return;
     }
     cudaLaunchAttribute attr[1];
@@ -1126,62 +1126,93 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
     lc.gridDim = dim3(grid);
     lc.blockDim = dim3(block);
     lc.dynamicSmemBytes = 0;
-    lc.stream = s;
+    lc.stream = st;
     lc.attrs = attr;
     lc.numAttrs = 1;
     const cudaError_t x = cudaLaunchKernelEx(&lc, f, T, in, out, uniforms, nu, seed, res, w, counters);
     if (le == cudaSuccess) le = x;
   };
-  if (o.phase != kPhaseStep) {
-    // the split step: its stage A kernels (256 threads, occupancy grids)
-    const int ph = o.phase - 1;
-    for (int q = 0; q < 2; ++q) {
-      trace.next(stage_name(q + 1));
-      if (o.mixed)
-        stage(K.splitMixed[ph][q], sms * K.occSplitMixed[ph][q], 256);
-      else
-        stage(K.split[ph][q], sms * K.occSplit[ph][q], 256);
-      mark();
-    }
-    if (o.phase == kPhaseHowFar) {
-      if (o.mixed) {
-        trace.next("fp64_fallback");
-        stage(K.finalSplit[0], sms * K.occFinalSplit[0], 256);
-      }
-      const cudaError_t e3 = cudaGetLastError();
-      return le != cudaSuccess ? le : e3;
-    }
-  }
-  for (int q = o.phase == kPhaseStep ? 0 : 2; q < kNumStageKernels; ++q) {
-    const int b = bs_index(cfg.block[q]);
+  // stage kernel q (0, 1: stage A of e+- / gammas, of the phase; 2..: the
+  // interaction queues) on stream st: the precision form's FP32 kernel where
+  // one exists, else the FP64 one, at the configured block size and CTAs per SM
+  auto launch_q = [&](int q, cudaStream_t st) {
     trace.next(stage_name(q + 1));
-    StageFn const finalFn = o.phase == kPhasePerform ? K.finalSplit[1] : K.final_[1];
-    const int finalOcc = o.phase == kPhasePerform ? K.occFinalSplit[1] : K.occFinal[1];
-    if (o.mixed && K.mixed[b][q]) {
-      // precision form: the FP32 kernel (its FP64 fallbacks run after the last stage)
-      const int om = K.occMixed[b][q];
-      const int pm = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < om ? cfg.ctasPerSM[q] : om;
-      stage(K.mixed[b][q], sms * pm, kBlockSizes[b]);
-      if (q == kNumStageKernels - 1) {
-        trace.next("fp64_fallback");
-        stage(finalFn, sms * finalOcc, 256);
-      }
-      mark();
-      continue;
+    if (q < 2 && o.phase != kPhaseStep) {
+      const int ph = o.phase - 1;
+      if (o.mixed)
+        stage(K.splitMixed[ph][q], sms * K.occSplitMixed[ph][q], 256, st);
+      else
+        stage(K.split[ph][q], sms * K.occSplit[ph][q], 256, st);
+      return;
     }
-    if (o.mixed && q == kNumStageKernels - 1) {
-      const int occ = K.occ[b][q];
-      const int per = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < occ ? cfg.ctasPerSM[q] : occ;
-      stage(K.fn[b][q], sms * per, kBlockSizes[b]);
-      trace.next("fp64_fallback");
-      stage(finalFn, sms * finalOcc, 256);
-      mark();
-      continue;
-    }
-    const int occ = K.occ[b][q];
+    const int b = bs_index(cfg.block[q]);
+    const bool fp32 = o.mixed && K.mixed[b][q];
+    const int occ = fp32 ? K.occMixed[b][q] : K.occ[b][q];
     const int per = cfg.ctasPerSM[q] > 0 && cfg.ctasPerSM[q] < occ ? cfg.ctasPerSM[q] : occ;
-    stage(K.fn[b][q], sms * per, kBlockSizes[b]);
-    mark();
+    stage(fp32 ? K.mixed[b][q] : K.fn[b][q], sms * per, kBlockSizes[b], st);
+  };
+  // the precision form's FP64 fallback kernel of the phase (after every stage)
+  auto launch_final = [&](cudaStream_t st) {
+    trace.next("fp64_fallback");
+    if (o.phase == kPhaseHowFar)
+      stage(K.finalSplit[0], sms * K.occFinalSplit[0], 256, st);
+    else if (o.phase == kPhasePerform)
+      stage(K.finalSplit[1], sms * K.occFinalSplit[1], 256, st);
+    else
+      stage(K.final_[1], sms * K.occFinal[1], 256, st);
+  };
+  SideStreams* sd = o.ev ? nullptr : o.side;
+  if (!sd) {
+    // one stream, stage by stage (the stage events of hepem_profile_stages
+    // time each stage alone)
+    const int qEnd = o.phase == kPhaseHowFar ? 2 : kNumStageKernels;
+    for (int q = 0; q < qEnd; ++q) {
+      launch_q(q, s);
+      if (o.mixed && q == kNumStageKernels - 1) launch_final(s);
+      mark();
+    }
+    if (o.phase == kPhaseHowFar && o.mixed) launch_final(s);
+  } else {
+    // Independent stages overlap: each kernel's last, slowest tracks leave
+    // its SMs idle, which the kernels on the other streams fill.  The gamma
+    // chain (stage A, conversion, Compton, photoelectric) runs on side
+    // stream 0 beside the e+- chain; after the e+- stage A the two
+    // bremsstrahlung queues go to side streams 1 and 2 and the other e+-
+    // queues stay on the caller's stream, which then waits for all three
+    // and runs the FP64 fallback.  The enqueue holds the lock, so that
+    // another thread's use of the same side streams and events cannot
+    // interleave with these waits.
+    std::lock_guard<std::mutex> lock(sd->mu);
+    auto fork = [&](cudaEvent_t ev, cudaStream_t to) {
+      if (cudaEventRecord(ev, s) == cudaSuccess) cudaStreamWaitEvent(to, ev, 0);
+    };
+    auto join = [&](cudaStream_t from, cudaEvent_t ev) {
+      if (cudaEventRecord(ev, from) == cudaSuccess) cudaStreamWaitEvent(s, ev, 0);
+    };
+    fork(sd->ev[0], sd->st[0]);
+    launch_q(0, s);
+    launch_q(1, sd->st[0]);
+    if (o.phase == kPhaseHowFar) {
+      join(sd->st[0], sd->ev[2]);
+      if (o.mixed) launch_final(s);
+    } else {
+      if (cudaEventRecord(sd->ev[1], s) == cudaSuccess) {
+        cudaStreamWaitEvent(sd->st[1], sd->ev[1], 0);
+        cudaStreamWaitEvent(sd->st[2], sd->ev[1], 0);
+      }
+      launch_q(2 + kQBremSB, sd->st[1]);
+      launch_q(2 + kQBremRB, sd->st[2]);
+      for (int q = 2; q < kNumStageKernels; ++q) {
+        const int Q = q - 2;
+        if (Q == kQBremSB || Q == kQBremRB) continue;
+        // queues before kQConversion are filled by the e+- stage A, the rest by the gamma one
+        launch_q(q, Q < kQConversion ? s : sd->st[0]);
+      }
+      join(sd->st[0], sd->ev[2]);
+      join(sd->st[1], sd->ev[3]);
+      join(sd->st[2], sd->ev[4]);
+      if (o.mixed) launch_final(s);
+    }
   }
   const cudaError_t e2 = cudaGetLastError();
   return le != cudaSuccess ? le : e2;
