@@ -299,8 +299,11 @@ int step_batched(const hepem_ctx* c, int64_t n, const hepem_track_state* in, hep
   // e+- tracks that reach an FP32 interaction (their FP64 fallback restarts there)
   const bool preCopy = mixed && in->ekin == out->ekin;
   const size_t wsBytes = hepem::batched_workspace_bytes(n);
+  const size_t preBytes = preCopy ? hepem::mixed_pre_state_bytes(n) : 0;
+  // no caller uniforms: room to draw the streams' first values ahead
+  const size_t fillBytes = hepem::wants_prefill(n, nu) ? hepem::prefill_bytes(n, 0) : 0;
   void* ws = nullptr;
-  HEPEM_CUDA(cudaMallocAsync(&ws, wsBytes + (preCopy ? hepem::mixed_pre_state_bytes(n) : 0), s));
+  HEPEM_CUDA(cudaMallocAsync(&ws, wsBytes + preBytes + fillBytes, s));
   hepem::BatchOpts o;
   o.ev = c->profile ? const_cast<cudaEvent_t*>(c->stageEv) : nullptr;
   o.cfg = &c->launch;
@@ -311,6 +314,7 @@ int step_batched(const hepem_ctx* c, int64_t n, const hepem_track_state* in, hep
     pre = hepem::carve_pre_state(static_cast<uint8_t*>(ws) + wsBytes, n, *in);
     o.preState = &pre;
   }
+  if (fillBytes) o.prefill = static_cast<uint8_t*>(ws) + wsBytes + preBytes;
   cudaError_t e = hepem::launch_step_batched(c->tables, n, *in, *out, uniforms, nu, seed, *res, counters, ws, s,
                                              c->sms, o);
   cudaError_t f = cudaFreeAsync(ws, s);
@@ -364,8 +368,11 @@ int hepem_step_subbatches(const hepem_ctx* c, int form, int32_t nb, const hepem_
   const bool preCopy = mixed && in->ekin == out->ekin;
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
   const size_t wsBytes = al(hepem::batched_workspace_bytes(total));
+  const size_t preBytes = preCopy ? al(hepem::mixed_pre_state_bytes(maxIdx)) : 0;
+  // no caller uniforms: room to draw the streams' first values ahead
+  const size_t fillBytes = hepem::wants_prefill(total, nu) ? hepem::prefill_bytes(total, maxIdx) : 0;
   const size_t need = wsBytes + al(4 * (size_t)total) + al(8 * (size_t)maxIdx) + al(sizeof(hepem_subbatch) * nb) +
-                      al(8 * (size_t)(nb + 1)) + (preCopy ? hepem::mixed_pre_state_bytes(maxIdx) : 0);
+                      al(8 * (size_t)(nb + 1)) + preBytes + fillBytes;
   void* ws = nullptr;
   HEPEM_CUDA(cudaMallocAsync(&ws, need, s));
   uint8_t* p = static_cast<uint8_t*>(ws) + wsBytes;
@@ -394,6 +401,7 @@ int hepem_step_subbatches(const hepem_ctx* c, int form, int32_t nb, const hepem_
       pre = hepem::carve_pre_state(p, maxIdx, *in);
       o.preState = &pre;
     }
+    if (fillBytes) o.prefill = p + preBytes;
     e = hepem::launch_step_batched(c->tables, total, *in, *out, uniforms, nu, 0, *res, counters, ws, s, c->sms, o);
   }
   const cudaError_t f = cudaFreeAsync(ws, s);
@@ -430,7 +438,11 @@ int step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem
   for (size_t b : kOutSizes) need += al(b * m);
   need += al(sizeof(double) * (size_t)m * nu) + al(hepem::batched_workspace_bytes(m));
   // the precision form steps the chunk in place: room for its pre-step copy
-  if (mixed) need += al(hepem::mixed_pre_state_bytes(m));
+  const size_t preBytes = mixed ? al(hepem::mixed_pre_state_bytes(m)) : 0;
+  need += preBytes;
+  // no caller uniforms: room to draw the streams' first values ahead
+  const bool fill = hepem::wants_prefill(m, nu);
+  if (fill) need += hepem::prefill_bytes(m, 0);
   const size_t total = need * (size_t)nChunks + al(sizeof(hepem_step_counters));
   if (!c->pipeReady) {
     for (cudaStream_t& ps : c->pipe) HEPEM_CUDA(cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking));
@@ -495,6 +507,7 @@ int step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem
       pre = hepem::carve_pre_state(dpre, m, ds);
       o.preState = &pre;
     }
+    if (fill) o.prefill = static_cast<uint8_t*>(dpre) + preBytes;
     HEPEM_CUDA(hepem::launch_step_batched(c->tables, mc, ds, ds, du, nu, seed, dr, counters ? cnt : nullptr, dwork,
                                           sStep, c->sms, o));
     HEPEM_CUDA(cudaEventRecord(c->chunkStepped[ch], sStep));

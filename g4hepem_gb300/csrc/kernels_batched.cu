@@ -81,10 +81,26 @@ struct Work {
   double* gstep;
   Limits limits;
   int phase;
-  // the batch: n tracks, active[0..n) of larger arrays or all
+  // the batch: n tracks, active[0..n) of larger arrays or all; with nDev,
+  // *nDev tracks (n is then an upper bound, set by the launch)
   int64_t n;
   const int32_t* active;
+  const uint32_t* nDev;
+  // no caller uniforms: the first kPrefill values of each stepped track's
+  // stream, row prefillPos[i] (active list) or i, or null
+  const double* prefill;
+  const int32_t* prefillPos;
 };
+
+// the track's stream values drawn ahead (Work::prefill), when there are any
+__device__ __forceinline__ void use_prefill(const Work& w, int64_t i, Rng& rng) {
+  if (w.prefill) {
+    const int64_t row = w.prefillPos ? (int64_t)w.prefillPos[i] : i;
+    rng.u = w.prefill + row * kPrefill;
+    rng.n = kPrefill;
+    rng.filled = true;
+  }
+}
 
 __device__ __forceinline__ uint64_t key_of(const Work& w, int64_t i, uint64_t seed) {
   return w.seeds ? w.seeds[i] : seed;
@@ -147,6 +163,9 @@ static Work carve(void* ws, int64_t n) {
   w.phase = kPhaseStep;
   w.n = n;
   w.active = nullptr;
+  w.nDev = nullptr;
+  w.prefill = nullptr;
+  w.prefillPos = nullptr;
   w.counts = reinterpret_cast<uint32_t*>(p);
   p += rnd(64 * sizeof(uint32_t));
   w.hist = reinterpret_cast<uint32_t*>(p);
@@ -178,6 +197,34 @@ __device__ __forceinline__ int sort_key(int type, int imc, double e, int ncb, in
   return ((type * ncb) + (imc % ncb)) * neb + eb;
 }
 
+// ---- 0. no caller uniforms: the first kPrefill values of each stream --------------
+// Row p of `pre` (track i = active[p], or p) gets stream values 0..kPrefill-1
+// of track i, the same values Rng::flat draws in place (rng.cuh: Philox block
+// (k >> 1, id, 0, 0x48455045) keyed by the track's seed, two values a block);
+// pos[i] = p for an active list.
+__global__ void __launch_bounds__(256) prefill_kernel(int64_t n, const int32_t* __restrict__ active,
+                                                      const uint32_t* __restrict__ nDev,
+                                                      const hepem_track_state in,
+                                                      const uint64_t* __restrict__ seeds, uint64_t seed,
+                                                      double* __restrict__ pre, int32_t* __restrict__ pos) {
+  if (nDev && (int64_t)*nDev < n) n = *nDev;
+  constexpr int kPairs = kPrefill / 2;
+  const int64_t total = n * kPairs;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = g / kPairs;
+    const uint32_t pair = (uint32_t)(g - p * kPairs);
+    const int64_t i = active ? (int64_t)active[p] : p;
+    const uint64_t key = seeds ? seeds[i] : seed;
+    uint32_t c0 = pair, c1 = (uint32_t)in.id[i], c2 = 0u, c3 = 0x48455045u;
+    philox4x32_10(c0, c1, c2, c3, (uint32_t)key, (uint32_t)(key >> 32));
+    double2 v;
+    v.x = u52_to_double(((uint64_t)c0 << 20) | (uint64_t)(c1 >> 12));
+    v.y = u52_to_double(((uint64_t)c2 << 20) | (uint64_t)(c3 >> 12));
+    reinterpret_cast<double2*>(pre + p * kPrefill)[pair] = v;
+    if (pos && pair == 0) pos[i] = (int32_t)p;
+  }
+}
+
 // ---- 1. sort: histogram, scan, scatter ----------------------------------------------
 __global__ void __launch_bounds__(256) sort_hist_kernel(const __grid_constant__ DevTables T, int64_t n,
                                                         const int32_t* __restrict__ active,
@@ -188,6 +235,7 @@ __global__ void __launch_bounds__(256) sort_hist_kernel(const __grid_constant__ 
   const int nkeys = 3 * ncb * neb;
   for (int k = threadIdx.x; k < nkeys; k += blockDim.x) sh[k] = 0;
   __syncthreads();
+  if (w.nDev && (int64_t)*w.nDev < n) n = *w.nDev;
   StepCount cnt = {};
   const int lane = threadIdx.x & 31;
   for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
@@ -275,6 +323,7 @@ __global__ void __launch_bounds__(256) sort_scatter_kernel(const __grid_constant
   const int nkeys = 3 * ncb * neb;
   const int lane = threadIdx.x & 31;
   const int64_t tile = 256 * kScatterItems;
+  if (w.nDev && (int64_t)*w.nDev < n) n = *w.nDev;
   for (int64_t base = blockIdx.x * tile; base < n; base += (int64_t)gridDim.x * tile) {
     for (int k = threadIdx.x; k < nkeys; k += 256) sh[k] = 0;
     __syncthreads();
@@ -474,6 +523,7 @@ __device__ __forceinline__ int charged_item(const DevTables& T, const hepem_trac
   Track t;
   Rng rng;
   load_track(in, idx, t, rng, uniforms, nu, key_of(w, idx, seed), type);
+  use_prefill(w, idx, rng);
   int32_t c0 = rng.cursor;
   if (MODE == kStageMixed) {
     MixedEl M{T, rng, t, false};
@@ -543,6 +593,7 @@ __device__ __forceinline__ int gamma_item(const DevTables& T, const hepem_track_
   Track t;
   Rng rng;
   load_track(in, idx, t, rng, uniforms, nu, key_of(w, idx, seed), 2);
+  use_prefill(w, idx, rng);
   int32_t c0 = rng.cursor;
   t.isEl = false;
   if (MODE == kStageMixed) {
@@ -687,6 +738,7 @@ __device__ bool stage_b_one(const DevTables& T, const hepem_track_state& in, con
   t.nsec = 0;
   rng.u = uniforms + (int64_t)i * nu;
   rng.n = nu;
+  use_prefill(w, i, rng);
   rng.cursor = out.rng_cursor[i];
   rng.id = in.id[i];
   rng.overflow = 0u;
@@ -803,6 +855,7 @@ __device__ void charged_full_step(const DevTables& T, const hepem_track_state& i
   Track t;
   Rng rng;
   load_track(src, i, t, rng, uniforms, nu, key_of(w, i, seed), type);
+  use_prefill(w, i, rng);
   Physics P{T, rng, t};
   int32_t c0 = rng.cursor;
   if (PHASE == kPhaseHowFar) {
@@ -861,6 +914,7 @@ __device__ void gamma_full_step(const DevTables& T, const hepem_track_state& in,
   Track t;
   Rng rng;
   load_track(in, i, t, rng, uniforms, nu, key_of(w, i, seed), 2);
+  use_prefill(w, i, rng);
   const int32_t c0 = rng.cursor;
   t.isEl = false;
   Physics P{T, rng, t};
@@ -1098,7 +1152,20 @@ cudaError_t launch_step_batched(const DevTables& T, int64_t n, const hepem_track
   const int64_t blocks = (n + 255) / 256;
   const int gC = (int)(blocks < (int64_t)sms * 8 ? blocks : (int64_t)sms * 8);
   w.active = o.active;
+  w.nDev = o.nDev;
   TraceStages trace(n);
+  if (o.prefill && wants_prefill(n, nu)) {
+    trace.next("prefill");
+    double* pre = static_cast<double*>(o.prefill);
+    int32_t* pos = o.active
+                       ? reinterpret_cast<int32_t*>(static_cast<uint8_t*>(o.prefill) + prefill_bytes(n, 0))
+                       : nullptr;
+    const int64_t pb = (n * (kPrefill / 2) + 255) / 256;
+    const int gP = (int)(pb < (int64_t)sms * 16 ? pb : (int64_t)sms * 16);
+    prefill_kernel<<<gP, 256, 0, s>>>(n, o.active, o.nDev, in, o.seeds, seed, pre, pos);
+    w.prefill = pre;
+    w.prefillPos = pos;
+  }
   trace.next("sort");
   mark();
   sort_hist_kernel<<<gC, 256, nkeys * sizeof(uint32_t), s>>>(T, n, o.active, in, out, res, w, ncb, neb, counters);

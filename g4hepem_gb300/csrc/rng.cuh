@@ -71,11 +71,16 @@ struct Rng {
   uint64_t seed;
   bool gaussValid;
   double gaussValue;
+  // u holds the stream's first n values drawn ahead by the library (the
+  // caller passed no uniforms): every draw still counts as past the caller's
+  // buffer, as if drawn here
+  bool filled = false;
 
   __device__ __forceinline__ double flat() {
     double v;
     if (cursor < n) {
       v = __ldg(u + cursor);
+      if (filled) overflow = 1u;
     } else {
       overflow = 1u;
       v = philox_uniform(seed, id, cursor);

@@ -155,6 +155,56 @@ __global__ void reduce_kernel(const int64_t* __restrict__ slot0, const int64_t* 
   }
 }
 
+// Staged state of whole requests (admission and retirement): per request,
+// the 20 state arrays of its n tracks one after the other, each starting on
+// a 16-byte boundary, at the request's offset in the staging buffer.
+__host__ __device__ constexpr size_t stage_field_size(int k) {
+  return k == 0 || k == 12 || k == 16 || k == 17 ? 1 : (k == 1 || k == 2 || k == 19) ? 4 : 8;
+}
+__host__ __device__ inline size_t stage_span(size_t bytes) { return (bytes + 15) & ~size_t(15); }
+inline size_t staged_bytes(int64_t n) {
+  size_t b = 0;
+  for (int k = 0; k < 20; ++k) b += stage_span(stage_field_size(k) * (size_t)n);
+  return b;
+}
+__device__ __forceinline__ void copy_elem(uint8_t* d, const uint8_t* s, size_t size) {
+  if (size == 8) *reinterpret_cast<uint64_t*>(d) = *reinterpret_cast<const uint64_t*>(s);
+  else if (size == 4) *reinterpret_cast<uint32_t*>(d) = *reinterpret_cast<const uint32_t*>(s);
+  else *d = *s;
+}
+// request r = blockIdx.y: its staged state to (ADMIT) or from (!ADMIT) its
+// pool slots [slot0[r], slot0[r] + cnt[r]); on admission also its RNG key and
+// zero per-track sums
+template <bool ADMIT>
+__global__ void stage_kernel(const int64_t* __restrict__ slot0, const int64_t* __restrict__ cnt,
+                             const int64_t* __restrict__ off, const uint64_t* __restrict__ reqSeed,
+                             uint8_t* __restrict__ stage, const hepem_track_state st, uint64_t* __restrict__ seeds,
+                             double* __restrict__ d0, double* __restrict__ d1, int32_t* __restrict__ i0,
+                             int32_t* __restrict__ i1) {
+  const int r = blockIdx.y;
+  const int64_t a = slot0[r], m = cnt[r];
+  void* const* pool = reinterpret_cast<void* const*>(&st);
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m; k += (int64_t)gridDim.x * blockDim.x) {
+    size_t o = (size_t)off[r];
+#pragma unroll
+    for (int f = 0; f < 20; ++f) {
+      const size_t sz = stage_field_size(f);
+      uint8_t* pp = static_cast<uint8_t*>(pool[f]) + sz * (size_t)(a + k);
+      uint8_t* sp = stage + o + sz * (size_t)k;
+      if (ADMIT) copy_elem(pp, sp, sz);
+      else copy_elem(sp, pp, sz);
+      o += stage_span(sz * (size_t)m);
+    }
+    if (ADMIT) {
+      seeds[a + k] = reqSeed[r];
+      d0[a + k] = 0.0;
+      d1[a + k] = 0.0;
+      i0[a + k] = 0;
+      i1[a + k] = 0;
+    }
+  }
+}
+
 __global__ void fill_seed_kernel(uint64_t* __restrict__ seeds, int64_t a, int64_t m, uint64_t seed,
                                  double* __restrict__ d0, double* __restrict__ d1, int32_t* __restrict__ i0,
                                  int32_t* __restrict__ i1) {
@@ -252,6 +302,13 @@ struct hepem_server {
   int64_t *hSlot0 = nullptr, *hCnt = nullptr, *hOff = nullptr, *hOutI = nullptr;
   double* hOutD = nullptr;
   uint32_t *hNActive = nullptr, *hAlive = nullptr;
+  // staged admission / retirement: pinned host and device staging buffers and
+  // per-iteration tables of the staged requests (slot0, n, offset, seed)
+  size_t stageBytes = 0;
+  uint8_t *hStage = nullptr, *dStage = nullptr;
+  int64_t *dStSlot0 = nullptr, *dStN = nullptr, *dStOff = nullptr;
+  int64_t *hStSlot0 = nullptr, *hStN = nullptr, *hStOff = nullptr;
+  uint64_t *dStSeed = nullptr, *hStSeed = nullptr;
   // free slot ranges: start -> length
   std::map<int64_t, int64_t> freeRanges;
   // requests
@@ -330,6 +387,47 @@ cudaError_t hepem_server::iterate() {
       activeReq.push_back(r->id);
     }
   }
+  // admission through the staging buffers: the admitted requests' state
+  // packed into pinned memory, one copy, one kernel to the pool slots
+  {
+    size_t used = 0;
+    int64_t ns = 0, maxN = 0;
+    std::vector<Request*> direct;
+    for (Request* r : admitted) {
+      const size_t need = staged_bytes(r->n);
+      if (!r->sums.empty() || need > stageBytes - used || ns == 65535) {
+        direct.push_back(r);
+        continue;
+      }
+      size_t o = used, t = 0;
+      for (int k = 0; k < 20; ++k) {
+        const size_t b = kStateSizes[k] * (size_t)r->n;
+        memcpy(hStage + o, r->host.data() + t, b);
+        o += stage_span(b);
+        t += b;
+      }
+      hStSlot0[ns] = r->slot0;
+      hStN[ns] = r->n;
+      hStOff[ns] = (int64_t)used;
+      hStSeed[ns] = r->seed;
+      ns += 1;
+      maxN = std::max(maxN, r->n);
+      used += need;
+    }
+    if (ns > 0) {
+      SRV_CUDA(cudaMemcpyAsync(dStage, hStage, used, cudaMemcpyHostToDevice, stream));
+      SRV_CUDA(cudaMemcpyAsync(dStSlot0, hStSlot0, 8 * ns, cudaMemcpyHostToDevice, stream));
+      SRV_CUDA(cudaMemcpyAsync(dStN, hStN, 8 * ns, cudaMemcpyHostToDevice, stream));
+      SRV_CUDA(cudaMemcpyAsync(dStOff, hStOff, 8 * ns, cudaMemcpyHostToDevice, stream));
+      SRV_CUDA(cudaMemcpyAsync(dStSeed, hStSeed, 8 * ns, cudaMemcpyHostToDevice, stream));
+      const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>((maxN + 255) / 256, 64));
+      stage_kernel<true><<<dim3(gx, (unsigned)ns), 256, 0, stream>>>(dStSlot0, dStN, dStOff, dStSeed, dStage, st,
+                                                                     seeds, edepSum, eSecSum, nSecSum, stepSum);
+      SRV_CUDA(cudaGetLastError());
+    }
+    admitted.swap(direct);
+  }
+  // the rest (larger than the staging space left, or resumed with sums): array by array
   for (Request* r : admitted) {
     size_t o = 0;
     for (int k = 0; k < 20; ++k) {
@@ -376,13 +474,13 @@ cudaError_t hepem_server::iterate() {
   collect_kernel<<<g, 256, 0, stream>>>(nr, dSlot0, dOff, total, st.ekin, cfg.min_energy, active, dNActive,
                                         dAlive);
   SRV_CUDA(cudaGetLastError());
-  SRV_CUDA(cudaMemcpyAsync(hNActive, dNActive, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
-  SRV_CUDA(cudaStreamSynchronize(stream));
-  const int64_t nAct = *hNActive;
+  // the step over the collected tracks: the kernels read their number from
+  // the device (total is its upper bound), so the host does not wait here
   trace.next("server_step");
-  if (nAct > 0) {
+  {
     hepem::BatchOpts o;
     o.active = active;
+    o.nDev = dNActive;
     o.seeds = seeds;
     o.cfg = &ctx->launch;
     hepem::apply_table_window(ctx, o);
@@ -392,13 +490,15 @@ cudaError_t hepem_server::iterate() {
       preState = hepem::carve_pre_state(pre, capacity, st);
       o.preState = &preState;
     }
-    SRV_CUDA(hepem::launch_step_batched(ctx->tables, nAct, st, st, nullptr, 0, 0, res, nullptr, work, stream,
+    SRV_CUDA(hepem::launch_step_batched(ctx->tables, total, st, st, nullptr, 0, 0, res, nullptr, work, stream,
                                         ctx->sms, o));
     account_kernel<<<g, 256, 0, stream>>>(active, dNActive, res, edepSum, eSecSum, nSecSum, stepSum);
     SRV_CUDA(cudaGetLastError());
   }
+  SRV_CUDA(cudaMemcpyAsync(hNActive, dNActive, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
   SRV_CUDA(cudaMemcpyAsync(hAlive, dAlive, sizeof(uint32_t) * nr, cudaMemcpyDeviceToHost, stream));
   SRV_CUDA(cudaStreamSynchronize(stream));
+  const int64_t nAct = *hNActive;
   trace.next("server_retire");
   // retire: nothing alive before this step, or the step budget is used up
   std::vector<int64_t> fin;
@@ -419,8 +519,24 @@ cudaError_t hepem_server::iterate() {
     SRV_CUDA(cudaGetLastError());
     SRV_CUDA(cudaMemcpyAsync(hOutD, dOutD, sizeof(double) * 2 * nf, cudaMemcpyDeviceToHost, stream));
     SRV_CUDA(cudaMemcpyAsync(hOutI, dOutI, sizeof(int64_t) * 2 * nf, cudaMemcpyDeviceToHost, stream));
+    // final states: packed on the device into the staging buffer, one copy
+    // out (requests beyond its space: array by array)
+    size_t used = 0;
+    int64_t ns = 0, maxN = 0;
+    std::vector<char> staged(nf, 0);
     for (int64_t q = 0; q < nf; ++q) {
       Request* r = act[fin[q]];
+      const size_t need = staged_bytes(r->n);
+      if (need <= stageBytes - used && ns < 65535) {
+        hStSlot0[ns] = r->slot0;
+        hStN[ns] = r->n;
+        hStOff[ns] = (int64_t)used;
+        ns += 1;
+        maxN = std::max(maxN, r->n);
+        used += need;
+        staged[q] = 1;
+        continue;
+      }
       size_t o = 0;
       for (int k = 0; k < 20; ++k) {
         SRV_CUDA(cudaMemcpyAsync(r->host.data() + o, state_ptr(k, r->slot0), kStateSizes[k] * r->n,
@@ -428,7 +544,31 @@ cudaError_t hepem_server::iterate() {
         o += kStateSizes[k] * r->n;
       }
     }
+    if (ns > 0) {
+      SRV_CUDA(cudaMemcpyAsync(dStSlot0, hStSlot0, 8 * ns, cudaMemcpyHostToDevice, stream));
+      SRV_CUDA(cudaMemcpyAsync(dStN, hStN, 8 * ns, cudaMemcpyHostToDevice, stream));
+      SRV_CUDA(cudaMemcpyAsync(dStOff, hStOff, 8 * ns, cudaMemcpyHostToDevice, stream));
+      const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>((maxN + 255) / 256, 64));
+      stage_kernel<false><<<dim3(gx, (unsigned)ns), 256, 0, stream>>>(dStSlot0, dStN, dStOff, nullptr, dStage, st,
+                                                                      nullptr, nullptr, nullptr, nullptr, nullptr);
+      SRV_CUDA(cudaGetLastError());
+      SRV_CUDA(cudaMemcpyAsync(hStage, dStage, used, cudaMemcpyDeviceToHost, stream));
+    }
     SRV_CUDA(cudaStreamSynchronize(stream));
+    {
+      int64_t j = 0;
+      for (int64_t q = 0; q < nf; ++q) {
+        if (!staged[q]) continue;
+        Request* r = act[fin[q]];
+        size_t o = (size_t)hStOff[j++], t = 0;
+        for (int k = 0; k < 20; ++k) {
+          const size_t b = kStateSizes[k] * (size_t)r->n;
+          memcpy(r->host.data() + t, hStage + o, b);
+          o += stage_span(b);
+          t += b;
+        }
+      }
+    }
     const double t = now_s();
     std::lock_guard<std::mutex> lock(mu);
     for (int64_t q = 0; q < nf; ++q) {
@@ -542,14 +682,19 @@ int hepem_server_create(const hepem_ctx* ctx, const hepem_server_config* cfg, he
   p += al(hepem::batched_workspace_bytes(C));
   if (cfg->precision) s->pre = p;
   // request tables, same layout on the device and in pinned host memory:
-  // slot0[R] cnt[R] off[R+1] outI[2R] outD[2R] nActive[1] alive[R]
+  // slot0[R] cnt[R] off[R+1] outI[2R] outD[2R] nActive[1] alive[R], then the
+  // staged requests' stSlot0[R] stN[R] stOff[R] stSeed[R], then the staging
+  // buffer (the state of up to 1M tracks of admitted or retired requests per
+  // iteration, at least the largest request the pool holds)
   const int64_t R = s->maxReq;
-  size_t tabOff[7];
+  const int64_t stageTracks = std::min<int64_t>(C, 1 << 20);
+  s->stageBytes = staged_bytes(stageTracks) + 16 * 20;
+  size_t tabOff[12];
   {
-    const size_t sz[7] = {8 * (size_t)R, 8 * (size_t)R, 8 * (size_t)(R + 1), 16 * (size_t)R, 16 * (size_t)R, 4,
-                          4 * (size_t)R};
+    const size_t sz[12] = {8 * (size_t)R, 8 * (size_t)R, 8 * (size_t)(R + 1), 16 * (size_t)R, 16 * (size_t)R, 4,
+                           4 * (size_t)R, 8 * (size_t)R, 8 * (size_t)R, 8 * (size_t)R, 8 * (size_t)R, s->stageBytes};
     size_t o = 0;
-    for (int k = 0; k < 7; ++k) {
+    for (int k = 0; k < 12; ++k) {
       tabOff[k] = o;
       o += al(sz[k]);
     }
@@ -578,6 +723,16 @@ int hepem_server_create(const hepem_ctx* ctx, const hepem_server_config* cfg, he
   s->hOutD = (double*)(hTab + tabOff[4]);
   s->hNActive = (uint32_t*)(hTab + tabOff[5]);
   s->hAlive = (uint32_t*)(hTab + tabOff[6]);
+  s->dStSlot0 = (int64_t*)(dTab + tabOff[7]);
+  s->dStN = (int64_t*)(dTab + tabOff[8]);
+  s->dStOff = (int64_t*)(dTab + tabOff[9]);
+  s->dStSeed = (uint64_t*)(dTab + tabOff[10]);
+  s->dStage = dTab + tabOff[11];
+  s->hStSlot0 = (int64_t*)(hTab + tabOff[7]);
+  s->hStN = (int64_t*)(hTab + tabOff[8]);
+  s->hStOff = (int64_t*)(hTab + tabOff[9]);
+  s->hStSeed = (uint64_t*)(hTab + tabOff[10]);
+  s->hStage = hTab + tabOff[11];
   s->freeRanges[0] = C;
   hepem_server* raw = s.release();
   raw->loop = std::thread([raw] { raw->run(); });

@@ -68,6 +68,80 @@ def test_subbatches_equal_one_call_per_subbatch(native, gpu_ctx, form, in_place)
     assert int(cnt[0].item()) == steps
 
 
+@pytest.mark.parametrize("form", ["batched", "mixed"])
+def test_subbatches_without_uniforms(native, gpu_ctx, form):
+    """n_uniform = 0 over more than 2^20 tracks: the library draws the first
+    values of every stream ahead (one row per stepped track, found through the
+    active list) and the rest in place; the results equal a step of each
+    sub-batch alone, which draws every value in place (the FP64 form: the
+    plain form's), bit for bit, the flag of draws past the (empty) buffer
+    included."""
+    import torch
+    ctx = gpu_ctx(T16)
+    # more than 2^20 tracks stepped: the library draws ahead (smaller batches draw in place)
+    total = (1 << 20) + 60000
+    st = W.mixed_batch(total, n_couples=16, seed=62, emin=1e-3, emax=1e5)
+    batches = [(0, 500000, 11), (520000, 300000, 12), (830000, total - 830000, 13)]
+    sin = native.state_to_torch(st)
+    sout = native.state_to_torch(st)
+    res = native.alloc_out_torch(total)
+    ctx.step_subbatches(batches, sin, sout, None, 0, res, form=form)
+    torch.cuda.synchronize()
+    got, got_res = native.to_numpy(sout), native.to_numpy(res)
+    slots = {f: k for f, _, k in native.OUT_FIELDS}
+    drawn = []
+    for a, n, seed in batches:
+        e = a + n
+        s1 = native.state_to_torch({k: v[a:e] for k, v in st.items()})
+        o1 = native.empty_state_torch(n)
+        r1 = native.alloc_out_torch(n)
+        ctx.step(s1, o1, None, 0, seed, r1, form="plain" if form == "batched" else form)
+        torch.cuda.synchronize()
+        o1, r1 = native.to_numpy(o1), native.to_numpy(r1)
+        for k in native.STATE_OUT_FIELDS:
+            assert np.array_equal(got[k][a:e], o1[k], equal_nan=True), (a, k)
+        for k, v in r1.items():
+            m = slots[k]
+            assert np.array_equal(got_res[k][a * m:e * m], v, equal_nan=True), (a, k)
+        drawn.append(o1["rng_cursor"] - st["rng_cursor"][a:e])
+    drawn = np.concatenate(drawn)
+    # some tracks drew past the values drawn ahead (32), every drawing track raised the flag
+    assert drawn.max() > 32
+    flags = np.concatenate([got_res["flags"][a:a + n] for a, n, _ in batches])
+    assert np.array_equal(flags & 1, (drawn > 0).astype(np.uint8))
+
+
+@pytest.mark.parametrize("form", ["batched", "mixed"])
+def test_large_step_without_uniforms(native, gpu_ctx, form):
+    """n_uniform = 0 over more than 2^20 tracks in one dense call: equal, bit
+    for bit, to the same tracks stepped in two calls below 2^20 tracks (which
+    draw in place), and for the FP64 form to the plain form."""
+    import torch
+    ctx = gpu_ctx(T16)
+    n = (1 << 20) + 4096
+    st = W.mixed_batch(n, n_couples=16, seed=63, emin=1e-3, emax=1e5)
+    sin = native.state_to_torch(st)
+    sout = native.empty_state_torch(n)
+    res = native.alloc_out_torch(n)
+    ctx.step(sin, sout, None, 0, 77, res, form=form)
+    torch.cuda.synchronize()
+    got, got_res = native.to_numpy(sout), native.to_numpy(res)
+    slots = {f: k for f, _, k in native.OUT_FIELDS}
+    for a, e in ((0, n // 2), (n // 2, n)):
+        m = e - a
+        s1 = native.state_to_torch({k: v[a:e] for k, v in st.items()})
+        o1 = native.empty_state_torch(m)
+        r1 = native.alloc_out_torch(m)
+        ctx.step(s1, o1, None, 0, 77, r1, form="plain" if form == "batched" else form)
+        torch.cuda.synchronize()
+        o1, r1 = native.to_numpy(o1), native.to_numpy(r1)
+        for k in native.STATE_OUT_FIELDS:
+            assert np.array_equal(got[k][a:e], o1[k], equal_nan=True), (a, k)
+        for k, v in r1.items():
+            q = slots[k]
+            assert np.array_equal(got_res[k][a * q:e * q], v, equal_nan=True), (a, k)
+
+
 def test_subbatches_reject_overlaps_and_bad_forms(native, gpu_ctx):
     ctx = gpu_ctx(T16)
     st = native.state_to_torch(W.mixed_batch(1000, n_couples=16, seed=3))
