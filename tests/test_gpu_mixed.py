@@ -1,7 +1,8 @@
 """Precision form (hepem_step_mixed) against the FP64 path.
 
 The FP64 batched path is bit-identical to the reference (test_gpu_parity);
-here the precision form must give the same discrete outcomes on every track
+here the precision form -- against that path, and directly against the CPU
+port (the oracle) -- must give the same discrete outcomes on every track
 (interaction, number and type of secondaries, flags, uniforms consumed, Gauss
 cache state, which tracks stop) and continuous outputs within 1e-5 relative:
   energies, deposits, step lengths, MSC range data   |d| <= 1e-5 |x|
@@ -113,6 +114,22 @@ def test_mixed_matches_fp64(native, gpu_ctx, table, nc, n):
     print(f"\nfp64 fallback {mix[2][12]} of {charged} e+- tracks ({frac:.2e});",
           {k: f"{v[0]:.2e}/{v[1]:.2e}" for k, v in errs.items()})
     assert frac < 0.02
+
+
+@pytest.mark.parametrize("table,nc", [(T3, 3), (T16, 16)])
+def test_mixed_matches_port_directly(native, gpu_ctx, port, table, nc):
+    """The precision form against the oracle itself (the CPU port, bit-exact
+    with the reference build), not through the FP64 GPU path: the same
+    contract, on 200k tracks and the same uniforms."""
+    ctx = gpu_ctx(table)
+    st = W.mixed_batch(200000, n_couples=nc, seed=57)
+    p = port(table)
+    u = p.fill_uniforms(st["id"], NU, SEED)
+    ref_out, ref_res = p.step_mt(st, u, NU, SEED, threads=8)
+    mix = run(native, ctx, st, "mixed")
+    # the port keeps no counters: the contract's counter check is left to the other tests
+    errs = compare(st, (ref_out, ref_res, mix[2]), mix)
+    print("\nprecision form vs oracle:", {k: f"{v[0]:.2e}/{v[1]:.2e}" for k, v in errs.items()})
 
 
 def test_mixed_wide_energy_range(native, gpu_ctx):

@@ -161,7 +161,8 @@ def test_in_place_equals_out_of_place(native, gpu_ctx):
 
 
 def test_host_entry_point_equals_device_entry_point(native, gpu_ctx):
-    st = W.mixed_batch(30000, seed=9)
+    # 600,001 tracks: every chunk of the host pipeline in use, the last one ragged
+    st = W.mixed_batch(600001, seed=9)
     out_d, res_d, _ = gpu_step(native, gpu_ctx(T3), st, 21, 64)
     u = W.philox_uniforms(21, st["id"], 64).reshape(-1)
     out_h = {k: np.empty_like(v) for k, v in st.items()}
