@@ -221,6 +221,37 @@ int hepem_autotune(hepem_ctx* c, int64_t n, const hepem_track_state* in, const d
     }
   }
   best.sortEBins = bestBins;
+  // 3. the choice against the default on the whole step as it runs outside
+  //    the tuner (no stage events: independent stages overlap on the side
+  //    streams, which the per-stage times above cannot see): the faster of the two
+  auto whole = [&](const hepem::LaunchCfg& cfg, int reps, float* ms) -> cudaError_t {
+    hepem::BatchOpts o;
+    o.cfg = &cfg;
+    hepem::apply_table_window(c, o);
+    *ms = 1e30f;
+    for (int r = 0; r < reps; ++r) {
+      cudaError_t x = cudaEventRecord(sc.ev[0], s);
+      if (x == cudaSuccess)
+        x = hepem::launch_step_batched(c->tables, n, *in, sc.st, uniforms, nu, seed, sc.res, nullptr, sc.work, s,
+                                       c->sms, o);
+      if (x == cudaSuccess) x = cudaEventRecord(sc.ev[1], s);
+      if (x == cudaSuccess) x = cudaEventSynchronize(sc.ev[1]);
+      if (x != cudaSuccess) return x;
+      float t = 0.0f;
+      cudaEventElapsedTime(&t, sc.ev[0], sc.ev[1]);
+      *ms = std::min(*ms, t);
+    }
+    return cudaSuccess;
+  };
+  const hepem::LaunchCfg def = hepem::default_launch_cfg();
+  float msBest = 0.0f, msDef = 0.0f;
+  e = whole(best, 3, &msBest);
+  if (e == cudaSuccess) e = whole(def, 3, &msDef);
+  if (e == cudaSuccess && msBest > msDef) {
+    best = def;
+    e = run(best, 2, bestMs, &total);
+  }
+  if (e != cudaSuccess) return hepem::set_error(HEPEM_CUDA_ERROR, std::string("autotune: ") + cudaGetErrorString(e));
   if (out) to_public(best, bestMs, out);
   if (apply) c->launch = best;
   return HEPEM_OK;

@@ -470,10 +470,11 @@ int  hepem_set_launch_config(hepem_ctx* ctx, const hepem_launch_config* cfg);
  * reference reads its tables through the ordinary caches
  * (G4HepEm/G4HepEmData/src/G4HepEmData.cc:78-101 copies them to the device). */
 int  hepem_set_table_l2_window(hepem_ctx* ctx, int enable, int64_t* window_bytes);
-/* Times the batched step on the caller's batch (device pointers; the batch is
- * read, outputs go to scratch) under every candidate configuration and returns
- * the fastest in `out`; apply != 0 also makes it the context's configuration.
- * Synchronises the stream. */
+/* Times the FP64 batched step on the caller's batch (device pointers; the
+ * batch is read, outputs go to scratch) under every candidate configuration,
+ * kernel by kernel, then the whole step with the choice against the default
+ * configuration, and returns the faster of the two in `out`; apply != 0 also
+ * makes it the context's configuration.  Synchronises the stream. */
 int  hepem_autotune(hepem_ctx* ctx, int64_t n, const hepem_track_state* in,
                     const double* uniforms, int32_t n_uniform, uint64_t seed,
                     int apply, hepem_launch_config* out, void* stream);
