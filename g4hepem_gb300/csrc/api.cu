@@ -176,15 +176,15 @@ int hepem_create_from_image(const void* image, size_t size, hepem_ctx** out) {
 
 int hepem_destroy(hepem_ctx* c) {
   if (!c) return HEPEM_OK;
-  cudaError_t e = cudaSuccess;
-  if (c->arena) e = cudaFree(c->arena);
+  // the context's own streams finish before the tables they read go away
   for (cudaStream_t ps : c->pipe)
     if (ps) cudaStreamSynchronize(ps);
   for (cudaStream_t st : c->side.st)
-    if (st) {
-      cudaStreamSynchronize(st);
-      cudaStreamDestroy(st);
-    }
+    if (st) cudaStreamSynchronize(st);
+  cudaError_t e = cudaSuccess;
+  if (c->arena) e = cudaFree(c->arena);
+  for (cudaStream_t st : c->side.st)
+    if (st) cudaStreamDestroy(st);
   for (cudaEvent_t ev : c->side.ev)
     if (ev) cudaEventDestroy(ev);
   if (c->pipeBuf) cudaFree(c->pipeBuf);
