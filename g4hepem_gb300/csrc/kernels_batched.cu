@@ -500,13 +500,17 @@ __device__ __forceinline__ void fb_push(bool trip, int32_t idx, uint8_t kind, co
 
 // The FP32 stages are latency bound (dependent table gathers and special
 // functions per track): they are compiled for more resident warps per SM
-// (stage A: 32 warps, 64 registers; stage B: 24 warps, 80 registers); the FP64
-// stages keep their registers (their FP64 pipe is the limit).
+// (stage A e+-: 32 warps, 64 registers; stage A gamma and stage B: 24 warps,
+// 80 registers); the FP64 stages keep their registers (their FP64 pipe is the
+// limit).
 #ifndef HEPEM_MIXED_A_WARPS
 #define HEPEM_MIXED_A_WARPS 32
 #endif
 #ifndef HEPEM_MIXED_B_WARPS
 #define HEPEM_MIXED_B_WARPS 24
+#endif
+#ifndef HEPEM_MIXED_G_WARPS
+#define HEPEM_MIXED_G_WARPS 24
 #endif
 // PHASE kPhaseStep: HowFar and Perform up to the interaction (the fused step);
 // kPhaseHowFar: HowFar only, into the step-limit record (nothing queued);
@@ -690,7 +694,8 @@ __global__ void __launch_bounds__(BS, MODE == kStageMixed ? HEPEM_MIXED_A_WARPS 
 
 // The gammas in sort order (perm[nEm + nEp, ...)).
 template <int BS, int MODE, int PHASE = kPhaseStep>
-__global__ void __launch_bounds__(BS) stage_a_gamma_kernel(const __grid_constant__ DevTables T,
+__global__ void __launch_bounds__(BS, MODE == kStageMixed ? HEPEM_MIXED_G_WARPS * 32 / BS : 1)
+    stage_a_gamma_kernel(const __grid_constant__ DevTables T,
                                                             const hepem_track_state in, const hepem_track_state out,
                                                             const double* __restrict__ uniforms, int nu,
                                                             uint64_t seed, const hepem_step_out res, const Work w,

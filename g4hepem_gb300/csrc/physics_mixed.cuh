@@ -1111,17 +1111,35 @@ static __device__ __noinline__ double gamma_pe_xs64(const DevTables& T, int imat
 
 // The FP64 interaction choice of Physics::gamma_select for a drawn uniform u,
 // from the FP64 total cross section (out of line: taken only when the FP32
-// choice is too close to call); leaves the photoelectric cross section in
-// t.peXS as the FP64 path does
-static __device__ __noinline__ int gamma_select64(const DevTables& T, Track& t, Rng& rng, double u) {
+// choice is too close to call), with the photoelectric cross section that the
+// FP64 path leaves in Track::peXS.  The track's couple and energy come by
+// value: a reference to the caller's track or stream would keep them in local
+// memory for the whole kernel.
+struct GammaSelect64 {
+  int winner;
+  double peXS;
+};
+static __device__ __noinline__ GammaSelect64 gamma_select64(const DevTables& T, int imc, double e, double u) {
+  Track t;
+  t.imc = imc;
+  t.setE(e);
+  t.peXS = 0.0;
+  Rng rng;  // nothing is drawn here
+  rng.u = nullptr;
+  rng.n = 0;
+  rng.cursor = 0;
+  rng.id = 0;
+  rng.overflow = 0u;
+  rng.seed = 0;
+  rng.gaussValid = false;
+  rng.gaussValue = 0.0;
   Physics P{T, rng, t};
   const double tot = P.gamma_total_xs();
   const double tmfp = tot > 0. ? 1. / tot : kLarge;
-  const double e = t.e;
   const DevGamma& g = T.gm;
   if (e > g.eMax1) {
     const double le = t.logE();
-    const int st = ld(&T.couples[t.imc].mat) * g.dataPerMat + g.nData0 + g.nData1;
+    const int st = ld(&T.couples[imc].mat) * g.dataPerMat + g.nData0 + g.nData1;
     double mx = 0.0, cp = 0.0;
     int pid = 2;
     do {
@@ -1129,10 +1147,9 @@ static __device__ __noinline__ int gamma_select64(const DevTables& T, Track& t, 
       cp += mx * tmfp;
       ++pid;
     } while (pid < 6 && u > cp);
-    t.peXS = mx;
-    return pid - 3;
+    return {pid - 3, mx};
   }
-  return (u > tmfp * t.peXS) ? 1 : 2;
+  return {(u > tmfp * t.peXS) ? 1 : 2, t.peXS};
 }
 
 // What the FP32 HowFar of MixedG leaves for its Perform.
@@ -1257,8 +1274,9 @@ struct MixedG {
       winner = u > mfp * pe ? 1 : 2;
     }
     if (tie) {
-      winner = gamma_select64(T, t, rng, ud);
-      if (winner != 2) t.peXS = 0.0;
+      const GammaSelect64 s64 = gamma_select64(T, t.imc, t.e, ud);
+      winner = s64.winner;
+      t.peXS = winner == 2 ? s64.peXS : 0.0;
     } else {
       t.peXS = winner == 2 ? gamma_pe_xs64(T, imat, e) : 0.0;
     }
