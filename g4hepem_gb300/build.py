@@ -80,7 +80,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(compile_unit, UNITS))
     tmp = OUT + ".tmp"
-    r = subprocess.run([cc, "-shared", ARCH, "-o", tmp] + objs + ["-lcudart", "-ldl"], capture_output=True, text=True)
+    r = subprocess.run([cc, "-shared", ARCH, "-o", tmp] + objs + ["-lcudart", "-ldl", "-lpthread"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, OUT)

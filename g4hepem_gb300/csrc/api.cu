@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <thread>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -523,7 +524,23 @@ int step_host(const hepem_ctx* cc, int64_t n, const hepem_track_state* in, hepem
                                  cudaMemcpyDeviceToHost, sOut));
   }
   if (hout[0] != hin[0]) {
-    for (int k : {0, 1, 2, 11, 12}) memcpy(hout[k], hin[k], kStateSizes[k] * n);
+    // the fields a step does not change (type, couple, id, safety, boundary
+    // status: 18 B per track), copied on the host while the device works, in
+    // four threads (one thread copies ~15 GB/s: 5 ms for 4M tracks, as long
+    // as the device pipeline itself)
+    const int kPass[5] = {0, 1, 2, 11, 12};
+    auto part = [&](int j, int parts) {
+      for (int k : kPass) {
+        const size_t b = kStateSizes[k] * (size_t)n;
+        const size_t lo = b * j / parts, hi = b * (j + 1) / parts;
+        memcpy(static_cast<uint8_t*>(hout[k]) + lo, static_cast<const uint8_t*>(hin[k]) + lo, hi - lo);
+      }
+    };
+    const int parts = n >= (1 << 18) ? 4 : 1;
+    std::vector<std::thread> th;
+    for (int j = 1; j < parts; ++j) th.emplace_back(part, j, parts);
+    part(0, parts);
+    for (std::thread& x : th) x.join();
   }
   // every chunk's step precedes the last chunk's copies out on sOut
   hepem_step_counters hc;
