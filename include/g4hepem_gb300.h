@@ -27,7 +27,10 @@
  *   uniforms the step consumed.  Tracks that read past n_uniform get bit 0 of
  *   flags set and are counted in hepem_step_counters.rng_overflow; the stream
  *   continues deterministically instead of wrapping.  Filling the buffer with
- *   hepem_philox_uniform() makes the stream seamless.
+ *   hepem_philox_uniform() makes the stream seamless.  With n_uniform = 0 and
+ *   at least 2^20 tracks, the batched forms draw the first 32 values of each
+ *   stepped track's stream ahead into their workspace; the values, the flag
+ *   and the counters are those of the draws in place.
  */
 #ifndef G4HEPEM_GB300_H
 #define G4HEPEM_GB300_H
