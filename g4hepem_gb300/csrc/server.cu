@@ -293,22 +293,21 @@ struct hepem_server {
   int32_t* active = nullptr;
   void* work = nullptr;
   void* pre = nullptr;                 // precision form: pre-step copy (mixed_pre_state_bytes)
-  // per-iteration request tables (device + pinned host mirrors)
+  // per-iteration request tables, the same layout on the device and in pinned
+  // host memory, each table group packed so that it moves in one copy:
+  //   req:   slot0[m] cnt[m] off[m + 1]  (m = the iteration's requests)
+  //   alive: nActive, alive[m]
+  //   out:   outD[2m] outI[2m]           (sums of the retired requests)
+  //   st:    slot0[m] n[m] off[m] seed[m] (staged admission / retirement)
+  // and the staging buffer of the admitted and retired requests' state
   int64_t maxReq = 0;
   size_t tableBytes = 0;
-  int64_t *dSlot0 = nullptr, *dCnt = nullptr, *dOff = nullptr, *dOutI = nullptr;
-  double* dOutD = nullptr;
-  uint32_t *dNActive = nullptr, *dAlive = nullptr;
-  int64_t *hSlot0 = nullptr, *hCnt = nullptr, *hOff = nullptr, *hOutI = nullptr;
-  double* hOutD = nullptr;
-  uint32_t *hNActive = nullptr, *hAlive = nullptr;
-  // staged admission / retirement: pinned host and device staging buffers and
-  // per-iteration tables of the staged requests (slot0, n, offset, seed)
+  int64_t *dReq = nullptr, *hReq = nullptr;
+  uint32_t *dAliveT = nullptr, *hAliveT = nullptr;
+  int64_t *dOutT = nullptr, *hOutT = nullptr;
+  int64_t *dStT = nullptr, *hStT = nullptr;
   size_t stageBytes = 0;
   uint8_t *hStage = nullptr, *dStage = nullptr;
-  int64_t *dStSlot0 = nullptr, *dStN = nullptr, *dStOff = nullptr;
-  int64_t *hStSlot0 = nullptr, *hStN = nullptr, *hStOff = nullptr;
-  uint64_t *dStSeed = nullptr, *hStSeed = nullptr;
   // free slot ranges: start -> length
   std::map<int64_t, int64_t> freeRanges;
   // requests
@@ -392,7 +391,8 @@ cudaError_t hepem_server::iterate() {
   {
     size_t used = 0;
     int64_t ns = 0, maxN = 0;
-    std::vector<Request*> direct;
+    std::vector<Request*> direct, adm;
+    std::vector<int64_t> offs;
     for (Request* r : admitted) {
       const size_t need = staged_bytes(r->n);
       if (!r->sums.empty() || need > stageBytes - used || ns == 65535) {
@@ -406,23 +406,25 @@ cudaError_t hepem_server::iterate() {
         o += stage_span(b);
         t += b;
       }
-      hStSlot0[ns] = r->slot0;
-      hStN[ns] = r->n;
-      hStOff[ns] = (int64_t)used;
-      hStSeed[ns] = r->seed;
+      adm.push_back(r);
+      offs.push_back((int64_t)used);
       ns += 1;
       maxN = std::max(maxN, r->n);
       used += need;
     }
     if (ns > 0) {
+      for (int64_t q = 0; q < ns; ++q) {
+        hStT[q] = adm[q]->slot0;
+        hStT[ns + q] = adm[q]->n;
+        hStT[2 * ns + q] = offs[q];
+        hStT[3 * ns + q] = (int64_t)adm[q]->seed;
+      }
       SRV_CUDA(cudaMemcpyAsync(dStage, hStage, used, cudaMemcpyHostToDevice, stream));
-      SRV_CUDA(cudaMemcpyAsync(dStSlot0, hStSlot0, 8 * ns, cudaMemcpyHostToDevice, stream));
-      SRV_CUDA(cudaMemcpyAsync(dStN, hStN, 8 * ns, cudaMemcpyHostToDevice, stream));
-      SRV_CUDA(cudaMemcpyAsync(dStOff, hStOff, 8 * ns, cudaMemcpyHostToDevice, stream));
-      SRV_CUDA(cudaMemcpyAsync(dStSeed, hStSeed, 8 * ns, cudaMemcpyHostToDevice, stream));
+      SRV_CUDA(cudaMemcpyAsync(dStT, hStT, 32 * ns, cudaMemcpyHostToDevice, stream));
       const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>((maxN + 255) / 256, 64));
-      stage_kernel<true><<<dim3(gx, (unsigned)ns), 256, 0, stream>>>(dStSlot0, dStN, dStOff, dStSeed, dStage, st,
-                                                                     seeds, edepSum, eSecSum, nSecSum, stepSum);
+      stage_kernel<true><<<dim3(gx, (unsigned)ns), 256, 0, stream>>>(
+          dStT, dStT + ns, dStT + 2 * ns, reinterpret_cast<const uint64_t*>(dStT + 3 * ns), dStage, st, seeds,
+          edepSum, eSecSum, nSecSum, stepSum);
       SRV_CUDA(cudaGetLastError());
     }
     admitted.swap(direct);
@@ -457,19 +459,21 @@ cudaError_t hepem_server::iterate() {
   const double t0 = now_s();
   const int64_t nr = (int64_t)act.size();
   int64_t total = 0;
+  int64_t* hSlot0 = hReq;
+  int64_t* hOff = hReq + nr;
   for (int64_t k = 0; k < nr; ++k) {
     hSlot0[k] = act[k]->slot0;
-    hCnt[k] = act[k]->n;
     hOff[k] = total;
     total += act[k]->n;
   }
   hOff[nr] = total;
   trace.next("server_collect");
-  SRV_CUDA(cudaMemcpyAsync(dSlot0, hSlot0, sizeof(int64_t) * nr, cudaMemcpyHostToDevice, stream));
-  SRV_CUDA(cudaMemcpyAsync(dCnt, hCnt, sizeof(int64_t) * nr, cudaMemcpyHostToDevice, stream));
-  SRV_CUDA(cudaMemcpyAsync(dOff, hOff, sizeof(int64_t) * (nr + 1), cudaMemcpyHostToDevice, stream));
-  SRV_CUDA(cudaMemsetAsync(dNActive, 0, sizeof(uint32_t), stream));
-  SRV_CUDA(cudaMemsetAsync(dAlive, 0, sizeof(uint32_t) * nr, stream));
+  SRV_CUDA(cudaMemcpyAsync(dReq, hReq, sizeof(int64_t) * (2 * nr + 1), cudaMemcpyHostToDevice, stream));
+  SRV_CUDA(cudaMemsetAsync(dAliveT, 0, sizeof(uint32_t) * (nr + 1), stream));
+  const int64_t* dSlot0 = dReq;
+  const int64_t* dOff = dReq + nr;
+  uint32_t* dNActive = dAliveT;
+  uint32_t* dAlive = dAliveT + 1;
   const int g = (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)ctx->sms * 16));
   collect_kernel<<<g, 256, 0, stream>>>(nr, dSlot0, dOff, total, st.ekin, cfg.min_energy, active, dNActive,
                                         dAlive);
@@ -495,10 +499,10 @@ cudaError_t hepem_server::iterate() {
     account_kernel<<<g, 256, 0, stream>>>(active, dNActive, res, edepSum, eSecSum, nSecSum, stepSum);
     SRV_CUDA(cudaGetLastError());
   }
-  SRV_CUDA(cudaMemcpyAsync(hNActive, dNActive, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
-  SRV_CUDA(cudaMemcpyAsync(hAlive, dAlive, sizeof(uint32_t) * nr, cudaMemcpyDeviceToHost, stream));
+  SRV_CUDA(cudaMemcpyAsync(hAliveT, dAliveT, sizeof(uint32_t) * (nr + 1), cudaMemcpyDeviceToHost, stream));
+  const uint32_t* hAlive = hAliveT + 1;
   SRV_CUDA(cudaStreamSynchronize(stream));
-  const int64_t nAct = *hNActive;
+  const int64_t nAct = hAliveT[0];
   trace.next("server_retire");
   // retire: nothing alive before this step, or the step budget is used up
   std::vector<int64_t> fin;
@@ -510,27 +514,29 @@ cudaError_t hepem_server::iterate() {
   if (!fin.empty()) {
     const int64_t nf = (int64_t)fin.size();
     for (int64_t q = 0; q < nf; ++q) {
-      hSlot0[q] = act[fin[q]]->slot0;
-      hCnt[q] = act[fin[q]]->n;
+      hReq[q] = act[fin[q]]->slot0;
+      hReq[nf + q] = act[fin[q]]->n;
     }
-    SRV_CUDA(cudaMemcpyAsync(dSlot0, hSlot0, sizeof(int64_t) * nf, cudaMemcpyHostToDevice, stream));
-    SRV_CUDA(cudaMemcpyAsync(dCnt, hCnt, sizeof(int64_t) * nf, cudaMemcpyHostToDevice, stream));
-    reduce_kernel<<<(unsigned)nf, 256, 0, stream>>>(dSlot0, dCnt, edepSum, eSecSum, nSecSum, stepSum, dOutD, dOutI);
+    SRV_CUDA(cudaMemcpyAsync(dReq, hReq, sizeof(int64_t) * 2 * nf, cudaMemcpyHostToDevice, stream));
+    reduce_kernel<<<(unsigned)nf, 256, 0, stream>>>(dReq, dReq + nf, edepSum, eSecSum, nSecSum, stepSum,
+                                                    reinterpret_cast<double*>(dOutT), dOutT + 2 * nf);
     SRV_CUDA(cudaGetLastError());
-    SRV_CUDA(cudaMemcpyAsync(hOutD, dOutD, sizeof(double) * 2 * nf, cudaMemcpyDeviceToHost, stream));
-    SRV_CUDA(cudaMemcpyAsync(hOutI, dOutI, sizeof(int64_t) * 2 * nf, cudaMemcpyDeviceToHost, stream));
+    SRV_CUDA(cudaMemcpyAsync(hOutT, dOutT, sizeof(int64_t) * 4 * nf, cudaMemcpyDeviceToHost, stream));
+    const double* hOutD = reinterpret_cast<const double*>(hOutT);
+    const int64_t* hOutI = hOutT + 2 * nf;
     // final states: packed on the device into the staging buffer, one copy
     // out (requests beyond its space: array by array)
     size_t used = 0;
     int64_t ns = 0, maxN = 0;
     std::vector<char> staged(nf, 0);
+    std::vector<Request*> ret;
+    std::vector<int64_t> offs;
     for (int64_t q = 0; q < nf; ++q) {
       Request* r = act[fin[q]];
       const size_t need = staged_bytes(r->n);
       if (need <= stageBytes - used && ns < 65535) {
-        hStSlot0[ns] = r->slot0;
-        hStN[ns] = r->n;
-        hStOff[ns] = (int64_t)used;
+        ret.push_back(r);
+        offs.push_back((int64_t)used);
         ns += 1;
         maxN = std::max(maxN, r->n);
         used += need;
@@ -545,12 +551,16 @@ cudaError_t hepem_server::iterate() {
       }
     }
     if (ns > 0) {
-      SRV_CUDA(cudaMemcpyAsync(dStSlot0, hStSlot0, 8 * ns, cudaMemcpyHostToDevice, stream));
-      SRV_CUDA(cudaMemcpyAsync(dStN, hStN, 8 * ns, cudaMemcpyHostToDevice, stream));
-      SRV_CUDA(cudaMemcpyAsync(dStOff, hStOff, 8 * ns, cudaMemcpyHostToDevice, stream));
+      for (int64_t q = 0; q < ns; ++q) {
+        hStT[q] = ret[q]->slot0;
+        hStT[ns + q] = ret[q]->n;
+        hStT[2 * ns + q] = offs[q];
+      }
+      SRV_CUDA(cudaMemcpyAsync(dStT, hStT, 24 * ns, cudaMemcpyHostToDevice, stream));
       const unsigned gx = (unsigned)std::max<int64_t>(1, std::min<int64_t>((maxN + 255) / 256, 64));
-      stage_kernel<false><<<dim3(gx, (unsigned)ns), 256, 0, stream>>>(dStSlot0, dStN, dStOff, nullptr, dStage, st,
-                                                                      nullptr, nullptr, nullptr, nullptr, nullptr);
+      stage_kernel<false><<<dim3(gx, (unsigned)ns), 256, 0, stream>>>(dStT, dStT + ns, dStT + 2 * ns, nullptr,
+                                                                      dStage, st, nullptr, nullptr, nullptr,
+                                                                      nullptr, nullptr);
       SRV_CUDA(cudaGetLastError());
       SRV_CUDA(cudaMemcpyAsync(hStage, dStage, used, cudaMemcpyDeviceToHost, stream));
     }
@@ -560,7 +570,7 @@ cudaError_t hepem_server::iterate() {
       for (int64_t q = 0; q < nf; ++q) {
         if (!staged[q]) continue;
         Request* r = act[fin[q]];
-        size_t o = (size_t)hStOff[j++], t = 0;
+        size_t o = (size_t)offs[j++], t = 0;
         for (int k = 0; k < 20; ++k) {
           const size_t b = kStateSizes[k] * (size_t)r->n;
           memcpy(r->host.data() + t, hStage + o, b);
@@ -689,12 +699,12 @@ int hepem_server_create(const hepem_ctx* ctx, const hepem_server_config* cfg, he
   const int64_t R = s->maxReq;
   const int64_t stageTracks = std::min<int64_t>(C, 1 << 20);
   s->stageBytes = staged_bytes(stageTracks) + 16 * 20;
-  size_t tabOff[12];
+  size_t tabOff[5];
   {
-    const size_t sz[12] = {8 * (size_t)R, 8 * (size_t)R, 8 * (size_t)(R + 1), 16 * (size_t)R, 16 * (size_t)R, 4,
-                           4 * (size_t)R, 8 * (size_t)R, 8 * (size_t)R, 8 * (size_t)R, 8 * (size_t)R, s->stageBytes};
+    const size_t sz[5] = {8 * (size_t)(2 * R + 1), 4 * (size_t)(R + 1), 32 * (size_t)R, 32 * (size_t)R,
+                          s->stageBytes};
     size_t o = 0;
-    for (int k = 0; k < 12; ++k) {
+    for (int k = 0; k < 5; ++k) {
       tabOff[k] = o;
       o += al(sz[k]);
     }
@@ -709,30 +719,16 @@ int hepem_server_create(const hepem_ctx* ctx, const hepem_server_config* cfg, he
     cudaStreamDestroy(s->stream);
     return hepem::set_error(HEPEM_CUDA_ERROR, std::string("server tables: ") + cudaGetErrorString(e));
   }
-  s->dSlot0 = (int64_t*)(dTab + tabOff[0]);
-  s->dCnt = (int64_t*)(dTab + tabOff[1]);
-  s->dOff = (int64_t*)(dTab + tabOff[2]);
-  s->dOutI = (int64_t*)(dTab + tabOff[3]);
-  s->dOutD = (double*)(dTab + tabOff[4]);
-  s->dNActive = (uint32_t*)(dTab + tabOff[5]);
-  s->dAlive = (uint32_t*)(dTab + tabOff[6]);
-  s->hSlot0 = (int64_t*)(hTab + tabOff[0]);
-  s->hCnt = (int64_t*)(hTab + tabOff[1]);
-  s->hOff = (int64_t*)(hTab + tabOff[2]);
-  s->hOutI = (int64_t*)(hTab + tabOff[3]);
-  s->hOutD = (double*)(hTab + tabOff[4]);
-  s->hNActive = (uint32_t*)(hTab + tabOff[5]);
-  s->hAlive = (uint32_t*)(hTab + tabOff[6]);
-  s->dStSlot0 = (int64_t*)(dTab + tabOff[7]);
-  s->dStN = (int64_t*)(dTab + tabOff[8]);
-  s->dStOff = (int64_t*)(dTab + tabOff[9]);
-  s->dStSeed = (uint64_t*)(dTab + tabOff[10]);
-  s->dStage = dTab + tabOff[11];
-  s->hStSlot0 = (int64_t*)(hTab + tabOff[7]);
-  s->hStN = (int64_t*)(hTab + tabOff[8]);
-  s->hStOff = (int64_t*)(hTab + tabOff[9]);
-  s->hStSeed = (uint64_t*)(hTab + tabOff[10]);
-  s->hStage = hTab + tabOff[11];
+  s->dReq = (int64_t*)(dTab + tabOff[0]);
+  s->dAliveT = (uint32_t*)(dTab + tabOff[1]);
+  s->dOutT = (int64_t*)(dTab + tabOff[2]);
+  s->dStT = (int64_t*)(dTab + tabOff[3]);
+  s->dStage = dTab + tabOff[4];
+  s->hReq = (int64_t*)(hTab + tabOff[0]);
+  s->hAliveT = (uint32_t*)(hTab + tabOff[1]);
+  s->hOutT = (int64_t*)(hTab + tabOff[2]);
+  s->hStT = (int64_t*)(hTab + tabOff[3]);
+  s->hStage = hTab + tabOff[4];
   s->freeRanges[0] = C;
   hepem_server* raw = s.release();
   raw->loop = std::thread([raw] { raw->run(); });
@@ -1013,8 +1009,8 @@ int hepem_server_destroy(hepem_server* s) {
   if (s->loop.joinable()) s->loop.join();
   cudaStreamSynchronize(s->stream);
   cudaFree(s->pool);
-  cudaFree(s->dSlot0);
-  cudaFreeHost(s->hSlot0);
+  cudaFree(s->dReq);
+  cudaFreeHost(s->hReq);
   cudaStreamDestroy(s->stream);
   delete s;
   return HEPEM_OK;
