@@ -358,6 +358,78 @@ def c3_batching(torch, N, args):
             "mixed_vs_plain": ms_plain / ms_mixed_graph}
 
 
+def f_rows(torch, N, ctx, sout, res, hbm):
+    """The rows after the step: secondary stacking with production cuts on the
+    4M-track step's own results (hepem_stack_secondaries), and Woodcock γ
+    tracking of 2^22 γ in a 50-cell Pb / lAr sampling calorimeter
+    (hepem_woodcock_gamma), each timed with CUDA events around the call."""
+    def timed(fn, reps=5, before=None):
+        fn()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(reps):
+            if before:
+                before()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.median(ms))
+
+    n = sout["ekin"].numel()
+    out = N.empty_state_torch(2 * n)
+    edep = torch.zeros(n, dtype=torch.float64, device="cuda")
+    holder = {}
+
+    def stack():
+        holder["r"] = ctx.stack_secondaries(sout, res, True, 1 << 30, 2 * n, out=out, edep_cut=edep)
+    ms_stack = timed(stack)
+    n_stacked = int(holder["r"][1].item())
+    n_sec = int(res["n_sec"].to(torch.int64).sum().item())
+    # algorithmic bytes: per parent its secondary count, couple and safety; per
+    # secondary its slot (type, energy, direction); per stacked track a full state
+    alg = n * (1 + 4 + 8) + n_sec * 33 + n_stacked * 120 + n * 8
+    stacking = {"workload": "the secondaries of one 4,194,304-track precision-form step, production cuts applied",
+                "parents": n, "secondaries": n_sec, "stacked": n_stacked, "ms_per_call": ms_stack,
+                "value": n / (ms_stack / 1e3), "unit": "parent tracks/s",
+                "roofline": {"bound": "hbm", "achieved": alg / (ms_stack / 1e3) / 1e9, "peak": hbm, "unit": "GB/s",
+                             "frac": alg / (ms_stack / 1e3) / 1e9 / hbm, "algorithmic_bytes_per_call": alg}}
+
+    from g4hepem_gb300 import workload as W
+    ng = 1 << 22
+    z = [0.0]
+    imc = []
+    for _ in range(50):
+        z += [z[-1] + 2.3, z[-1] + 2.3 + 5.7]
+        imc += [2, 1]
+    st = W.mixed_batch(ng, n_couples=3, seed=23, emin=0.05, emax=1000.0, frac=(1.0, 0.0, 0.0))
+    rng = np.random.default_rng(23)
+    pos0 = [torch.from_numpy(a).cuda() for a in (rng.uniform(-180.0, 180.0, ng), rng.uniform(-180.0, 180.0, ng),
+                                                 rng.uniform(0.0, z[-1], ng))]
+    pos = [a.clone() for a in pos0]
+    box = {"half_x": 200.0, "half_y": 200.0, "z_bounds": torch.tensor(z, dtype=torch.float64, device="cuda"),
+           "layer_imc": torch.tensor(imc, dtype=torch.int32, device="cuda"), "wdt_imc": 2, "energy_limit": 0.2}
+    gin = N.state_to_torch(st)
+    gout = N.empty_state_torch(ng)
+    gres = N.alloc_out_torch(ng)
+    u = N.fill_uniforms(gin["id"], 32, SEED)
+    reached = torch.zeros(ng, dtype=torch.uint8, device="cuda")
+
+    def reset():
+        for a, b in zip(pos, pos0):
+            a.copy_(b)
+        reached.zero_()
+    ms_wdt = timed(lambda: ctx.woodcock_gamma(gin, gout, tuple(pos), box, u, 32, SEED, gres, reached),
+                   before=reset)
+    woodcock = {"workload": "4,194,304 γ, 50 keV-1 GeV log-uniform, in a 50-cell G4_Pb / G4_lAr calorimeter "
+                            "(2.3 / 5.7 mm slabs, Pb the Woodcock reference), 32 uniforms per track",
+                "ms_per_call": ms_wdt, "value": ng / (ms_wdt / 1e3), "unit": "γ tracks/s (to an interaction or "
+                "out of the box)", "reached_interaction": int(reached.sum().item())}
+    return {"stacking": stacking, "woodcock": woodcock}
+
+
 def c4_serving(torch, N, args):
     """Serving: an event stream through the serving form
     (hepem_server_*).  A request is one event's track batch, log-normal in size
@@ -729,6 +801,7 @@ def main():
     ap.add_argument("--no-c3", action="store_true")
     ap.add_argument("--no-c4", action="store_true")
     ap.add_argument("--no-c5", action="store_true")
+    ap.add_argument("--no-f", action="store_true", help="skip the stacking and Woodcock rows")
     ap.add_argument("--form", default="mixed", choices=["mixed", "batched"],
                     help="form timed as the headline value (the other FP64 forms are reported beside it)")
     args = ap.parse_args()
@@ -865,6 +938,10 @@ def main():
     c3 = None if args.no_c3 else c3_batching(torch, N, args)
     c4 = None if args.no_c4 else c4_serving(torch, N, args)
     c5 = None if args.no_c5 else c5_precision(torch, N, args)
+    # the rows after the step, on the precision-form step's results
+    ctx.step(sin, sout, u, NU, SEED, res, form="mixed")
+    torch.cuda.synchronize()
+    rows_f = None if args.no_f else f_rows(torch, N, ctx, sout, res, hbm)
     # per-stage device times of one more step of each batched form: CUDA events
     # recorded on the launching stream around every stage (hepem_profile_stages)
     import ctypes as C
@@ -945,6 +1022,7 @@ def main():
                 "entry_point": "hepem_step_batched" if other == "batched" else "hepem_step_mixed"},
             "vs_plain_fp64": ms_plain / ms_step, "roofline": roof, "roofline_fp64": fp64, "roofline_fp32": fp32,
             "stage_ms": stages, "c1_lookup": c1, "c3_batching": c3, "c4_serving": c4, "c5_precision": c5,
+            "f_rows": rows_f,
             "cpu_baseline": cpu, "clocks": clk,
             "counters": {"uniforms_per_step": uniforms_consumed, "secondaries_per_step": secondaries,
                          "interactions": [int(x) for x in c[4:12]]}}
